@@ -1,0 +1,365 @@
+"""Benchmark: SSB-shaped three-way star join with group-by at SF20 on one GB300.
+
+A step is one execution of the star-join plan (supplier semi join on region,
+part join on category, date join; group by (d_year, p_brand1); SUM(lo_revenue))
+over 120,000,000 seeded fact rows through the C-ABI executor, from plan text
+to result rows in host memory.
+
+  value      fact rows/s with the base columns resident in HBM (timed with
+             CUDA events on the executor's stream over exactly K steps)
+  e2e        the same metric with HOST (pinned) base columns: every step
+             registers the tables (H2D copies, segment min/max) and executes
+  roofline   the dominant kernel (the fused fact-side chain): algorithmic bytes
+             (4 fact columns x 4 B x rows) / its CUDA-event duration, against
+             the measured HBM copy bandwidth
+  cpu_baseline  the CPU oracle (operator-at-a-time C/OpenMP restatement of
+             the reference executor) on a bounded row sample, host cores
+
+--impl reference times the reference path's CPU restatement (the oracle port:
+the reference itself needs AdaptiveCpp, oneDPL and Thrift and cannot be built
+here) on the same metric.  Under torchrun (--gpus N > 1) each rank runs its
+own fact partition (weak scaling, no collective on the data path); rank 0
+prints the line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "rows/s & %HBM roofline (SF20 star join)"
+UNIT = "rows/s"
+SF = 20.0
+REGION, CATEGORY = 2, 11
+PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "fused_chain_star_sf20.txt")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--sf", type=float, default=SF)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg):
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def sum_over_ranks(pg, v: float) -> float:
+    if pg is None:
+        return v
+    import torch
+
+    t = torch.tensor([v], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.SUM)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "20"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        time.sleep(0.05)
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """DRAM bytes per launch of the fused chain from the committed ncu summary."""
+    if not os.path.exists(PROFILE_SUMMARY):
+        return None
+    for line in open(PROFILE_SUMMARY):
+        if line.startswith("traffic_bytes_per_launch_sf20:"):
+            try:
+                return int(float(line.split(":", 1)[1].strip()))
+            except ValueError:
+                return None
+    return None
+
+
+def dims_host(sf):
+    from sycldb_gb300 import ssb
+
+    d = ssb.gen_dims(sf)
+    return {t: d[t] for t in ("supplier", "part", "ddate")}
+
+
+# ---------------------------------------------------------------------- CPU
+def cpu_oracle_run(sample_rows: int, sf: float, steps: int, warmup: int, salt: int = 0):
+    """The oracle on the first `sample_rows` fact rows; returns rows/s, threads."""
+    from oracle import build_oracle
+
+    build_oracle.build_oracle()
+    from oracle import oracle as O
+    from sycldb_gb300 import plans, ssb
+
+    fact = ssb.gen_lineorder_host(sample_rows, ssb.QUERY_COLUMNS["star"], sf, salt=salt)
+    dims = dims_host(sf)
+    tables = {"lineorder": O.make_table("lineorder", fact)}
+    for t, cols in dims.items():
+        tables[t] = O.make_table(t, cols)
+    plan = plans.plan_star(REGION, CATEGORY)
+    ex = O.OracleExecutor(tables)
+    for _ in range(warmup):
+        ex.execute(plan)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        ex.execute(plan)
+    dt = time.perf_counter() - t0
+    return sample_rows * steps / dt, O.lib().o_num_threads(), dt / steps * 1e3
+
+
+def run_reference(args, rank, world, pg):
+    if rank != 0:
+        return 0
+    from sycldb_gb300 import ssb
+
+    n_full = ssb.fact_rows(args.sf)
+    sample = max(1, n_full // 16)
+    value, cores, ms = cpu_oracle_run(sample, args.sf, args.steps, args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/uint64", "data": "synthetic",
+        "config": {"workload": workload_name(args.sf), "sample_fact_rows": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": "first %d of %d fact rows per step (1/16), full dimensions" % (sample, n_full)},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "CPU restatement of the reference executor (oracle port: C/OpenMP kernels, operator at a "
+                "time); the reference's SYCL CPU path needs AdaptiveCpp, oneDPL and Thrift, absent here",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def workload_name(sf):
+    return ("SSB-shaped star join SF%g: %d fact rows x (partkey, suppkey, orderdate, revenue); supplier %d, "
+            "part %d, date 2556; s_region=%d semi join, p_category=%d, group by (d_year, p_brand1), "
+            "SUM(lo_revenue)" % (sf, int(6e6 * sf), int(2000 * sf), int(54000 * sf), REGION, CATEGORY))
+
+
+# ---------------------------------------------------------------------- GPU
+def run_ours(args, rank, world, local, pg):
+    import torch
+
+    from sycldb_gb300 import build, capi, plans, ssb
+
+    build.build()
+    torch.cuda.set_device(local)
+    from sycldb_gb300.engine import Engine
+
+    L = capi.lib()
+    sf = args.sf
+    n = ssb.fact_rows(sf)
+    cols = ssb.QUERY_COLUMNS["star"]
+    plan = plans.plan_star(REGION, CATEGORY)
+    dims = dims_host(sf)
+    fact = ssb.gen_lineorder_device(n, cols, sf, salt=rank)
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.Stream()
+    eng = Engine(fuse=True, profile=True, stream=stream.cuda_stream)
+    eng.load_table("lineorder", fact)
+    for t, c in dims.items():
+        eng.load_table(t, c)
+
+    res = None
+    for _ in range(max(3, args.warmup)):
+        res = eng.execute(plan)
+    n_groups = res.nrows
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.1)
+    barrier(pg)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = L.sdb_launch_count()
+    fused_ms, fused_launches = 0.0, 0
+    ev0.record(stream)
+    for _ in range(args.steps):
+        eng.execute(plan)
+        st = eng.kernel_stats()
+        if "fused_chain" in st:
+            fused_launches += st["fused_chain"][0]
+            fused_ms += st["fused_chain"][1]
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    launches = L.sdb_launch_count() - launches0
+    barrier(pg)
+    clk = clocks.stop()
+    elapsed_ms = ev0.elapsed_time(ev1)
+    stats_last = eng.kernel_stats()
+    elapsed_ms = max_over_ranks(pg, elapsed_ms)
+    ms_per_step = elapsed_ms / args.steps
+    total_rows = sum_over_ranks(pg, float(n)) * args.steps
+    value = total_rows / (elapsed_ms / 1e3)
+
+    # roofline of the dominant kernel
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 4 * len(cols) * n
+    per_launch_ms = fused_ms / max(1, fused_launches)
+    achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if fused_launches else None
+    traffic = profile_traffic()
+    roof = {"kernel": "k_chain (fused semi+full+full probe + group-by)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
+            "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+            "launch_ms": per_launch_ms, "launches": fused_launches}
+
+    # e2e through the C ABI with host (pinned) buffers
+    e2e = run_e2e(args, eng, plan, n, cols, sf, rank, stream, pg)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int32/uint64", "data": "synthetic (seeded SplitMix64 columns, SSB SF20 shapes)",
+        "config": {"workload": workload_name(sf), "fact_rows_per_gpu": n, "groups": n_groups,
+                   "l2": "inputs larger than L2 (%.2f GB of fact columns per step)" % (alg_bytes / 1e9),
+                   "segment_rows": 1 << 28, "fused": True, "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "roofline": roof,
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "kernel_ms_last_step": {k: v[1] for k, v in stats_last.items()},
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu_baseline:
+        sample = max(1, n // 16)
+        v, cores, _ = cpu_oracle_run(sample, sf, steps=3, warmup=1)
+        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "3 runs on the first %d of %d fact rows (1/16), full dimensions" % (sample, n)}
+    eng.close()
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_e2e(args, eng, plan, n, cols, sf, rank, stream, pg):
+    import torch
+
+    from sycldb_gb300 import ssb
+
+    pinned = {c: torch.empty(n, dtype=torch.int32, pin_memory=True) for c in cols}
+    host = ssb.gen_lineorder_host(n, cols, sf, salt=rank, out={c: t.numpy() for c, t in pinned.items()})
+    dims = dims_host(sf)
+    h2d = sum(a.nbytes for a in host.values()) + sum(a.nbytes for d in dims.values() for a in d.values())
+
+    def step():
+        eng.load_table("lineorder", host)
+        for t, c in dims.items():
+            eng.load_table(t, c)
+        return eng.execute(plan)
+
+    for _ in range(2):
+        r = step()
+    d2h = sum(c.nbytes for c in r.columns)
+    torch.cuda.synchronize()
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        step()
+    torch.cuda.synchronize()
+    dt = max_over_ranks(pg, time.perf_counter() - t0)
+    rows = sum_over_ranks(pg, float(n)) * args.e2e_steps
+    return {"value": rows / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+            "ms_per_step": dt / args.e2e_steps * 1e3, "steps": args.e2e_steps,
+            "timing": "host wall clock around load_table(host pinned columns) + execute, synchronised"}
+
+
+def main():
+    args = parse_args()
+    rank, world, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        rc = run_reference(args, rank, world, pg)
+    else:
+        rc = run_ours(args, rank, world, local, pg)
+    if pg is not None:
+        pg.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())

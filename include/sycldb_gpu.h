@@ -1,0 +1,339 @@
+/*
+ * sycldb_gpu.h -- C ABI of the GB300 (sm_103a) operator library.
+ *
+ * This is the drop-in boundary for the SYCLDB physical-operator path.  In the
+ * reference the boundary is a C++ class interface: Segment::*_operator
+ * factories build KernelDefinition objects (models/models.hpp:604-986), and
+ * KernelData::execute switches on KernelType and submits one SYCL
+ * parallel_for per kernel (models/execution.hpp:30-46, 260-497).  Each
+ * sdb_* kernel entry below replaces one arm of that switch, or one of the
+ * inline kernels that TransientTable submits itself; the comment on each
+ * entry names the reference code it replaces.
+ *
+ * Conventions (all entries):
+ *   - Every pointer argument is a device pointer unless stated otherwise.
+ *     The caller owns every buffer; no kernel entry allocates.  Hash tables
+ *     and group-by slot arrays must arrive zeroed, as the reference's
+ *     memory_manager::alloc_zero regions do.
+ *   - Work is enqueued on `stream` and returns without waiting (the reference
+ *     waits after every KernelBundle, models/execution.hpp:628; results are
+ *     the same).  A NULL stream is the legacy default stream.
+ *   - Return value: SDB_OK (0) or a negative sdb_status.  sdb_last_error()
+ *     gives the message of the last failure on the calling thread.
+ *   - Enum values are the reference's: comp_op and logical_op
+ *     (kernels/selection.hpp:7-21), BinaryOp (kernels/aggregation.hpp:11-17).
+ *   - Integer semantics are the reference's: int32 columns, uint8 (bool)
+ *     flags, uint64 sums of sign-extended int32 values, int32 arithmetic that
+ *     wraps.  Division by zero yields 0 and INT_MIN / -1 yields INT_MIN (both
+ *     undefined in the reference).
+ *   - Out-of-range hash-table or group-by slots (which the reference would
+ *     write out of bounds) are skipped and counted in a device error word;
+ *     sdb_device_errors() reads and clears it.
+ */
+#ifndef SYCLDB_GPU_H
+#define SYCLDB_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Same type as cudaStream_t / CUstream. */
+typedef struct CUstream_st *sdb_stream_t;
+
+typedef enum sdb_status {
+    SDB_OK = 0,
+    SDB_ERR_INVALID = -1,     /* bad argument (the reference throws std::invalid_argument / runtime_error) */
+    SDB_ERR_CUDA = -2,        /* CUDA launch or API failure */
+    SDB_ERR_NOMEM = -3,       /* allocator budget exceeded (the reference throws std::bad_alloc) */
+    SDB_ERR_TIMEOUT = -4,     /* a bounded device or host wait ran out */
+    SDB_ERR_UNSUPPORTED = -5, /* plan shape the executor does not handle */
+    SDB_ERR_DEVICE = -6       /* device-side check failed (see sdb_device_errors) */
+} sdb_status;
+
+typedef enum sdb_comp_op { SDB_EQ = 0, SDB_NE = 1, SDB_LT = 2, SDB_LE = 3, SDB_GT = 4, SDB_GE = 5 } sdb_comp_op;
+typedef enum sdb_logical_op { SDB_NONE = 0, SDB_AND = 1, SDB_OR = 2 } sdb_logical_op;
+typedef enum sdb_binary_op { SDB_MUL = 0, SDB_DIV = 1, SDB_ADD = 2, SDB_SUB = 3 } sdb_binary_op;
+
+/* ---------------------------------------------------------------- library */
+
+/* Message of the last failed call on this thread ("" if none). */
+const char *sdb_last_error(void);
+/* Library version string. */
+const char *sdb_version(void);
+/* sizeof of an ABI struct by name ("sdb_operand", "sdb_chain_op",
+ * "sdb_chain_desc", "sdb_engine_config"), 0 if unknown: lets bindings check
+ * their layouts. */
+size_t sdb_abi_sizeof(const char *type_name);
+/* Number of kernels this library has launched in this process (host-side
+ * counter; cudaMemset/cudaMemcpy calls are not counted). */
+uint64_t sdb_launch_count(void);
+/* Reads and clears the device-side error counter (out-of-range slots skipped
+ * by the build and group-by kernels).  Synchronises `stream`. */
+int sdb_device_errors(uint64_t *count, sdb_stream_t stream);
+
+/* ------------------------------------------------- operator kernels (K1-K16) */
+
+/* K1: flags[i] = v.  Replaces queue.fill<bool> of the flag buffers
+ * (models/transient_table.hpp:86,105). */
+int sdb_fill_u8(uint8_t *flags, uint64_t n, uint8_t v, sdb_stream_t stream);
+
+/* K2: out[i] = logical(logic_op, in[i], compare(cmp_op, col[i], v)).
+ * Replaces SelectionKernelLiteral (kernels/selection.hpp:157-186),
+ * KernelData::execute arm at models/execution.hpp:305-321.
+ * in and out may alias. */
+int sdb_select_lit(const int32_t *col, int32_t v, int cmp_op, int logic_op,
+                   const uint8_t *in, uint8_t *out, uint64_t n, sdb_stream_t stream);
+
+/* K3: out[i] = logical(logic_op, in[i], compare(cmp_op, a[i], b[i])).
+ * Replaces SelectionKernelColumns (kernels/selection.hpp:127-155). */
+int sdb_select_cols(const int32_t *a, const int32_t *b, int cmp_op, int logic_op,
+                    const uint8_t *in, uint8_t *out, uint64_t n, sdb_stream_t stream);
+
+/* K4: out[i] = logical(logic_op, in[i], local[i]).
+ * Replaces LogicalKernel (kernels/selection.hpp:106-125), the last step of
+ * Segment::search_operator (models/models.hpp:704-715). */
+int sdb_logical(int logic_op, const uint8_t *in, const uint8_t *local, uint8_t *out,
+                uint64_t n, sdb_stream_t stream);
+
+/* K5: dst[i] = v.  Replaces FillKernel (kernels/projection.hpp:7-21). */
+int sdb_fill_i32(int32_t *dst, int32_t v, uint64_t n, sdb_stream_t stream);
+
+/* K6: if (flags[i]) res[i] = a op b; other rows are left untouched.
+ * Replaces PerformOperationKernelColumns / LiteralFirst / LiteralSecond
+ * (kernels/aggregation.hpp:50-72, 102-125, 155-178). */
+int sdb_binop_cc(int32_t *res, const int32_t *a, const int32_t *b, int bin_op,
+                 const uint8_t *flags, uint64_t n, sdb_stream_t stream);
+int sdb_binop_lc(int32_t *res, int32_t a, const int32_t *b, int bin_op,
+                 const uint8_t *flags, uint64_t n, sdb_stream_t stream);
+int sdb_binop_cl(int32_t *res, const int32_t *a, int32_t b, int bin_op,
+                 const uint8_t *flags, uint64_t n, sdb_stream_t stream);
+
+/* K7: *acc += sum over rows of (uint64)(int64)(flags[i] ? col[i] : 0).
+ * Accumulates (does not overwrite), like the sycl::reduction without
+ * initialize_to_identity of AggregateOperationKernel
+ * (kernels/aggregation.hpp:208-228; models/execution.hpp:458-476). */
+int sdb_sum_i32_u64(const int32_t *col, const uint8_t *flags, uint64_t n, uint64_t *acc,
+                    sdb_stream_t stream);
+
+/* K8: dense group-by SUM.  For each flagged row, slot
+ *   h = (int)((uint64)(int)(sum_j (keys[j][i]-mins[j]) * prod_{l<j}(maxs[l]-mins[l]+1)) % P)
+ * (int arithmetic that wraps); the first row to claim occ[h] writes its key
+ * values to out_keys[j][h]; out_sum[h] += (uint64)(int64)val[i].
+ * Replaces GroupByAggregateKernel (kernels/aggregation.hpp:278-344).
+ * keys/out_keys are HOST arrays of g device pointers; mins/maxs are HOST
+ * arrays of g ints; 1 <= g <= 8.  occ and out_sum must arrive zeroed. */
+int sdb_groupby_sum(const int32_t *const *keys, const int32_t *mins, const int32_t *maxs, int g,
+                    const int32_t *val, const uint8_t *flags, uint64_t n, uint64_t P,
+                    int32_t *const *out_keys, uint64_t *out_sum, uint32_t *occ, sdb_stream_t stream);
+
+/* K9: flags[s] = occ[s] != 0.  Replaces the group-by final-flags kernel
+ * (models/transient_table.hpp:1544-1558). */
+int sdb_occ_to_flags(const uint32_t *occ, uint8_t *flags, uint64_t P, sdb_stream_t stream);
+
+/* K10: ht[key[i]-min] = flags[i] (bool, false written too).
+ * Replaces BuildKeysHTKernel (kernels/join.hpp:17-33). */
+int sdb_ht_build_keys(const int32_t *key, const uint8_t *flags, uint64_t n,
+                      uint8_t *ht, int32_t min, int32_t len, sdb_stream_t stream);
+
+/* K11: out[i] = in[i] && min <= key[i] <= max && ht[key[i]-min].
+ * Replaces FilterJoinKernel (kernels/join.hpp:129-173). */
+int sdb_probe_semi(const int32_t *key, const uint8_t *in, uint8_t *out, uint64_t n,
+                   const uint8_t *ht, int32_t min, int32_t max, sdb_stream_t stream);
+
+/* K12: interleaved {occ, val} table: ht2[2h] = flags[i]; if flags[i]
+ * ht2[2h+1] = val[i], h = key[i]-min.
+ * Replaces BuildKeyValsHTKernel (kernels/join.hpp:60-93). */
+int sdb_ht_build_kv(const int32_t *key, const int32_t *val, const uint8_t *flags, uint64_t n,
+                    int32_t *ht2, int32_t min, int32_t len, sdb_stream_t stream);
+
+/* K13: if in[i] && min <= key[i] <= max && ht2[2h] == 1:
+ * val_out[i] = ht2[2h+1], out[i] = 1; else out[i] = 0.
+ * Replaces FullJoinKernel (kernels/join.hpp:256-312). */
+int sdb_probe_full(const int32_t *key, int32_t *val_out, const uint8_t *in, uint8_t *out,
+                   uint64_t n, const int32_t *ht2, int32_t min, int32_t max, sdb_stream_t stream);
+
+/* K14: ids[0..count) = indices of set flags, in increasing order; *count
+ * (device word) = how many.  Replaces build_row_ids
+ * (models/transient_table.hpp:535-599), whose atomic append gives the same
+ * set in an unspecified order.  `scratch` is device memory of at least
+ * sdb_compact_scratch_bytes(n) bytes. */
+size_t sdb_compact_scratch_bytes(uint64_t n);
+int sdb_compact_row_ids(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t *count,
+                        void *scratch, size_t scratch_bytes, sdb_stream_t stream);
+
+/* K15: dst[i] = src[ids[i]] for i < *count (count is a device word, cap
+ * bounds it).  Replaces the gather of Segment::compress_sync
+ * (models/models.hpp:1019-1063). */
+int sdb_gather_i32(const int32_t *src, const int32_t *ids, const uint32_t *count,
+                   int32_t *dst, uint64_t cap, sdb_stream_t stream);
+int sdb_gather_u64(const uint64_t *src, const int32_t *ids, const uint32_t *count,
+                   uint64_t *dst, uint64_t cap, sdb_stream_t stream);
+
+/* K16: *out = number of set flags (overwrites).  Replaces
+ * count_true_flags (kernels/common.hpp:30-110). */
+int sdb_count_flags(const uint8_t *flags, uint64_t n, uint64_t *out, sdb_stream_t stream);
+
+/* Segment statistics computed at load: minmax[0] = min, minmax[1] = max of
+ * col[0..n) (n >= 1).  Replaces the host scan of the Segment constructor
+ * (models/models.hpp:71-77). */
+int sdb_min_max_i32(const int32_t *col, uint64_t n, int32_t *minmax, sdb_stream_t stream);
+
+/* ------------------------------------------------------ fused operator chain */
+
+/* One pass over a segment that applies a KernelBundle's kernels in order with
+ * the row's flag held in a register.  It computes what the composed K2-K13 +
+ * K7/K8 launches compute (the reference's disabled call-sequence fusion,
+ * models/execution.hpp:546-615, had the same intent). */
+#define SDB_CHAIN_MAX_OPS 16
+#define SDB_CHAIN_MAX_REGS 8
+#define SDB_CHAIN_MAX_KEYS 4
+
+typedef enum sdb_operand_kind { SDB_SRC_COL = 0, SDB_SRC_REG = 1, SDB_SRC_LIT = 2 } sdb_operand_kind;
+
+typedef struct sdb_operand {
+    int32_t kind;        /* sdb_operand_kind */
+    int32_t reg;         /* SDB_SRC_REG: register index */
+    int32_t lit;         /* SDB_SRC_LIT: value */
+    int32_t pad;
+    const int32_t *col;  /* SDB_SRC_COL: column (device) */
+} sdb_operand;
+
+typedef enum sdb_chain_op_kind {
+    SDB_OP_SELECT = 0,        /* flag = logical(logic_op, flag, compare(cmp_op, a, b)) */
+    SDB_OP_SEARCH_RANGE = 1,  /* flag = logical(logic_op, flag, lo <= a && a <= hi) */
+    SDB_OP_SEARCH_POINTS = 2, /* flag = logical(logic_op, flag, a == lo || a == hi) */
+    SDB_OP_SEMI_PROBE = 3,    /* flag = flag && lo <= a <= hi && ht8[a-lo] */
+    SDB_OP_FULL_PROBE = 4,    /* flag = flag && lo <= a <= hi && ht2[2(a-lo)] == 1; reg[out_reg] = ht2[2(a-lo)+1] */
+    SDB_OP_BINOP = 5,         /* if flag: reg[out_reg] = a bin_op b */
+    SDB_OP_FILL = 6           /* reg[out_reg] = a (a literal), every row */
+} sdb_chain_op_kind;
+
+typedef struct sdb_chain_op {
+    int32_t kind;        /* sdb_chain_op_kind */
+    int32_t cmp_op;
+    int32_t logic_op;
+    int32_t bin_op;
+    sdb_operand a;
+    sdb_operand b;
+    int32_t lo, hi;      /* SEARCH bounds or probe min/max */
+    int32_t out_reg;     /* FULL_PROBE / BINOP / FILL */
+    int32_t pad;
+    const void *ht;      /* SEMI: uint8[hi-lo+1]; FULL: int32[2*(hi-lo+1)] */
+    int32_t *out_col;    /* FULL_PROBE / BINOP / FILL: if non-NULL the register
+                            is also stored where the composed kernel stores it */
+} sdb_chain_op;
+
+typedef enum sdb_chain_terminal {
+    SDB_TERM_FLAGS = 0,   /* write the final flags to flags_out */
+    SDB_TERM_SUM = 1,     /* *sum_out += sum of value over surviving rows (K7) */
+    SDB_TERM_GROUPBY = 2  /* dense group-by SUM into out_keys/out_sum/occ (K8) */
+} sdb_chain_terminal;
+
+typedef struct sdb_chain_desc {
+    uint64_t n;                 /* rows of this segment */
+    const uint8_t *flags_in;    /* NULL: every row starts with flag = true */
+    uint8_t *flags_out;         /* final flags (required for SDB_TERM_FLAGS, optional otherwise) */
+    int32_t n_ops;
+    int32_t terminal;           /* sdb_chain_terminal */
+    sdb_chain_op ops[SDB_CHAIN_MAX_OPS];
+    sdb_operand value;          /* SUM / GROUPBY value */
+    uint64_t *sum_out;          /* SUM: accumulated */
+    int32_t n_keys;             /* GROUPBY */
+    int32_t pad;
+    sdb_operand keys[SDB_CHAIN_MAX_KEYS];
+    int32_t key_min[SDB_CHAIN_MAX_KEYS];
+    int32_t key_max[SDB_CHAIN_MAX_KEYS];
+    uint64_t P;
+    int32_t *out_keys[SDB_CHAIN_MAX_KEYS];
+    uint64_t *out_sum;
+    uint32_t *occ;
+} sdb_chain_desc;
+
+/* Launch one fused pass.  The descriptor is read on the host (copied into
+ * the launch); its pointers are device pointers. */
+int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream);
+
+/* ------------------------------------------------------ synthetic SSB data */
+
+/* Counter-based generator shared by host and device: value of row `row` of
+ * stream `stream_id` under `seed`, uniform in [lo, hi]. */
+int32_t sdb_gen_uniform_host(uint64_t seed, uint64_t stream_id, uint64_t row, int32_t lo, int32_t hi);
+/* Fill dst[0..n) with rows [row0, row0+n) of a uniform stream (device). */
+int sdb_gen_uniform(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, uint64_t stream_id,
+                    int32_t lo, int32_t hi, sdb_stream_t stream);
+/* Same on the host (dst is host memory), multi-threaded. */
+int sdb_gen_uniform_cpu(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, uint64_t stream_id,
+                        int32_t lo, int32_t hi);
+/* dst[i] = YYYYMMDD of day (day0 + i) counted from 1992-01-01 (host). */
+int sdb_gen_datekeys_cpu(int32_t *dst, uint64_t n, int64_t day0);
+/* lo_orderdate-style column: YYYYMMDD of a uniform day in [0, ndays). */
+int sdb_gen_dates(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, uint64_t stream_id,
+                  int32_t ndays, sdb_stream_t stream);
+int sdb_gen_dates_cpu(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, uint64_t stream_id,
+                      int32_t ndays);
+
+/* ------------------------------------------------------------ host executor */
+
+/* The executor above the kernels: Table/Column/Segment storage, TransientTable
+ * with its pending per-segment kernel phases, and the plan-node dispatch of
+ * executor::execute_ddor_plan (executor/ddor_executor.cpp:22-245).  Plans are
+ * JSON text in the shape of the Thrift PlanResult (server/thrift/
+ * calciteserver.thrift:22-80): {"rels": [{"id":0, "relOp":"TABLE_SCAN",
+ * "tables":["ssb","lineorder"]}, ...]}. */
+typedef struct sdb_engine sdb_engine;
+typedef struct sdb_result sdb_result;
+
+typedef struct sdb_engine_config {
+    uint64_t arena_bytes;       /* device budget for intermediates (memory_manager budget) */
+    uint64_t segment_rows;      /* rows per segment; 0 = 2^28 (common.hpp:12) */
+    int32_t fuse;               /* 1: run fusable kernel runs as one sdb_fused_chain pass */
+    int32_t profile;            /* 1: time every launch with CUDA events */
+    sdb_stream_t stream;        /* NULL: the engine creates its own stream */
+} sdb_engine_config;
+
+/* Parses a plan and derives its execution order and group-by columns
+ * (operations/preprocessing.cpp:104-275) without touching a device.
+ * *n_rels = number of plan nodes; order (optional, n_rels entries) = the DAG
+ * execution order. */
+int sdb_plan_check(const char *plan_json, int *n_rels, int *order, int order_cap);
+
+int sdb_engine_create(const sdb_engine_config *cfg, sdb_engine **out);
+int sdb_engine_destroy(sdb_engine *eng);
+
+/* Register a base table.  cols[c] points at nrows int32 values, or is NULL
+ * for a column that is not loaded.  on_device = 1: device pointers used in
+ * place (caller keeps them alive); 0: host pointers, copied to the device
+ * (pinned memory gives full bandwidth).  Computes per-segment min/max
+ * (synchronises the engine stream).  Re-registering a name replaces it. */
+int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const int32_t *const *cols,
+                          uint64_t nrows, int on_device);
+
+/* Execute one plan; on success *out holds the result rows (host memory). */
+int sdb_engine_execute(sdb_engine *eng, const char *plan_json, sdb_result **out);
+
+/* Result: flagged rows of the final table in row order, non-null columns in
+ * order (executor/result_writer.cpp:41-67).  Column type 0 = int32,
+ * 1 = uint64. */
+int sdb_result_shape(const sdb_result *r, int *ncols, uint64_t *nrows);
+int sdb_result_column(const sdb_result *r, int c, int *type, const void **data);
+/* Writes the rows as the reference's .res file does (space-separated, one
+ * row per line). */
+int sdb_result_write_res(const sdb_result *r, const char *path);
+void sdb_result_free(sdb_result *r);
+
+/* Per-kernel launch statistics of the last execute (profile = 1):
+ * name of kernel kind k, launches, total milliseconds.  Returns the number of
+ * kinds when k is out of range. */
+int sdb_engine_kernel_stats(const sdb_engine *eng, int k, const char **name, uint64_t *launches,
+                            double *total_ms);
+/* Device milliseconds of the last execute (CUDA events around the plan). */
+int sdb_engine_last_plan_ms(const sdb_engine *eng, double *ms);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SYCLDB_GPU_H */

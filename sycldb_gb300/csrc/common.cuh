@@ -1,0 +1,114 @@
+// Device helpers shared by the operator kernels and the fused chain kernel.
+//
+// The arithmetic follows the reference kernels exactly:
+//   compare()   kernels/selection.hpp:61-81
+//   logical()   kernels/selection.hpp:83-96  (NONE returns the new value)
+//   binop()     kernels/aggregation.hpp:19-35 (int32, wrapping)
+//   HASH()      kernels/join.hpp:11-15       ((x - min) % len, identity in range)
+//   slot()      kernels/aggregation.hpp:315-321
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sycldb_gpu.h"
+
+namespace sdb {
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the
+                           // device's own count at run time; this is a default)
+
+__host__ __device__ __forceinline__ bool compare(int cmp, int32_t a, int32_t b)
+{
+    switch (cmp) {
+    case SDB_EQ: return a == b;
+    case SDB_NE: return a != b;
+    case SDB_LT: return a < b;
+    case SDB_LE: return a <= b;
+    case SDB_GT: return a > b;
+    case SDB_GE: return a >= b;
+    default: return false;
+    }
+}
+
+__host__ __device__ __forceinline__ bool logical(int logic, bool a, bool b)
+{
+    switch (logic) {
+    case SDB_AND: return a && b;
+    case SDB_OR: return a || b;
+    case SDB_NONE: return b;
+    default: return false;
+    }
+}
+
+// 4-row bit masks: bit j is row j of a 4-row group.
+__host__ __device__ __forceinline__ uint32_t logical4(int logic, uint32_t a, uint32_t b)
+{
+    switch (logic) {
+    case SDB_AND: return a & b;
+    case SDB_OR: return a | b;
+    case SDB_NONE: return b;
+    default: return 0u;
+    }
+}
+
+__host__ __device__ __forceinline__ int32_t binop(int32_t a, int32_t b, int op)
+{
+    switch (op) {
+    case SDB_MUL: return (int32_t)((uint32_t)a * (uint32_t)b);
+    case SDB_DIV:
+        if (b == 0) return 0;
+        if (a == INT32_MIN && b == -1) return INT32_MIN;
+        return a / b;
+    case SDB_ADD: return (int32_t)((uint32_t)a + (uint32_t)b);
+    case SDB_SUB: return (int32_t)((uint32_t)a - (uint32_t)b);
+    default: return 0;
+    }
+}
+
+// HASH(x, len, min) = (x - min) % len in int.  Returns -1 when len == 0.
+__host__ __device__ __forceinline__ int64_t ht_slot(int32_t x, int32_t len, int32_t mn)
+{
+    int32_t d = (int32_t)((uint32_t)x - (uint32_t)mn);
+    if (len == 0) return -1;
+    if (len == -1) return 0;
+    return (int64_t)(d % len);
+}
+
+// Group-by slot: hash = sum_j (k_j - min_j) * mult_j in wrapping int, then
+// `hash %= prod_ranges` with hash converted to uint64 and the result stored
+// back into an int.
+__host__ __device__ __forceinline__ int64_t group_slot(uint32_t hash, uint64_t P)
+{
+    return (int64_t)(int32_t)(uint32_t)((uint64_t)(int64_t)(int32_t)hash % P);
+}
+
+__host__ __device__ __forceinline__ uint64_t widen(int32_t v)
+{
+    return (uint64_t)(int64_t)v;
+}
+
+inline bool aligned(const void *p, uintptr_t a)
+{
+    return p == nullptr || (reinterpret_cast<uintptr_t>(p) % a) == 0;
+}
+
+// Grid for a grid-stride loop over `work` items of `threads` threads each.
+inline unsigned grid_for(uint64_t work, int threads, int blocks_per_sm = 8)
+{
+    uint64_t b = (work + threads - 1) / threads;
+    uint64_t cap = (uint64_t)kSMs * blocks_per_sm;
+    if (b > cap) b = cap;
+    if (b == 0) b = 1;
+    return (unsigned)b;
+}
+
+}  // namespace sdb
+
+// Host-side error plumbing shared by all translation units (errors.cpp).
+int sdb_set_error(int status, const char *fmt, ...);
+// Counts one kernel launch and checks it; sdb_count_launches adds the
+// extra launches of entry points that launch several kernels.
+int sdb_check_launch(const char *what);
+void sdb_count_launches(unsigned n);
+void sdb_errors_add_reader(unsigned long long (*reader)(cudaStream_t));

@@ -1,0 +1,1717 @@
+// Host executor above the C ABI kernels.
+//
+// This restates the reference's operator API for one GPU:
+//   memory_manager      operations/memory_manager.{hpp,cpp}   (bump regions, zeroed region)
+//   Segment/Column/Table models/models.hpp:20-1802            (int32 segments of <= 2^28 rows, min/max stats)
+//   KernelData/Bundle   models/execution.hpp:30-651           (KernelType switch -> one C ABI call)
+//   TransientTable      models/transient_table.hpp:20-1928    (flags, pending phases, apply_*)
+//   execute_ddor_plan   executor/ddor_executor.cpp:22-245     (plan-node dispatch)
+//   parse_execution_info operations/preprocessing.cpp:14-275  (group-by columns, DAG order)
+// SYCL queues and events become one CUDA stream; kernels of a segment run in
+// phase order on that stream, so no host wait is needed between bundles (the
+// reference waits after each one).  Everything lives on the device: the
+// reference's host-side kernel paths (used when a segment is not on a
+// device) are not needed, so LITERAL projections fill on the device.
+//
+// With fusion on, each segment's bundle is scanned for runs of fusable
+// kernels (selections, SEARCH triples, semi/full probes, projections) ending
+// optionally in a SUM or group-by; a run becomes one sdb_fused_chain pass that
+// computes the same outputs (the reference's own call-sequence fusion,
+// models/execution.hpp:546-615, is disabled).
+#include <algorithm>
+#include <chrono>
+#include <cstdio>
+#include <cstring>
+#include <deque>
+#include <fstream>
+#include <map>
+#include <memory>
+#include <new>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "plan.hpp"
+#include "sycldb_gpu.h"
+
+int sdb_set_error(int status, const char *fmt, ...);
+
+namespace sdb {
+
+constexpr uint64_t kDefaultSegment = 1ull << 28;  // common.hpp:12
+
+// kernels/types.cpp:3-21
+const std::map<std::string, std::set<int>> &table_column_indices()
+{
+    static const std::map<std::string, std::set<int>> m = {
+        {"lineorder", {2, 3, 4, 5, 8, 9, 11, 12, 13}},
+        {"part", {0, 2, 3, 4}},
+        {"supplier", {0, 3, 4, 5}},
+        {"customer", {0, 3, 4, 5}},
+        {"ddate", {0, 4, 5}},
+    };
+    return m;
+}
+
+const std::map<std::string, int> &table_column_numbers()
+{
+    static const std::map<std::string, int> m = {
+        {"lineorder", 17}, {"part", 9}, {"supplier", 7}, {"customer", 8}, {"ddate", 17}};
+    return m;
+}
+
+// Tables may be registered under "<schema table>@<tag>" (e.g. one fact
+// partition per tag); the schema is that of the part before '@'.
+std::string base_name(const std::string &name)
+{
+    size_t at = name.find('@');
+    return at == std::string::npos ? name : name.substr(0, at);
+}
+
+struct Error : std::runtime_error {
+    int status;
+    Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
+};
+
+#define SDB_CUDA(x)                                                                                   \
+    do {                                                                                              \
+        cudaError_t e_ = (x);                                                                         \
+        if (e_ != cudaSuccess) throw ::sdb::Error(SDB_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+inline void check(int st)
+{
+    if (st != SDB_OK) throw Error(st, sdb_last_error());
+}
+
+// ------------------------------------------------------------------ strings
+// kernels/selection.hpp:23-49, kernels/aggregation.hpp:37-48
+int get_comp_op(const std::string &op)
+{
+    if (op == "==") return SDB_EQ;
+    if (op == ">=") return SDB_GE;
+    if (op == "<=") return SDB_LE;
+    if (op == "<") return SDB_LT;
+    if (op == ">") return SDB_GT;
+    if (op == "!=" || op == "<>") return SDB_NE;
+    return SDB_EQ;
+}
+
+int get_logical_op(const std::string &op)
+{
+    if (op == "AND") return SDB_AND;
+    if (op == "OR") return SDB_OR;
+    return SDB_NONE;
+}
+
+bool is_filter_logical(const std::string &op)
+{
+    for (char c : op)
+        if (!std::isalpha((unsigned char)c)) return false;
+    return true;
+}
+
+int get_op_from_string(const std::string &op)
+{
+    if (op == "*") return SDB_MUL;
+    if (op == "/") return SDB_DIV;
+    if (op == "+") return SDB_ADD;
+    if (op == "-") return SDB_SUB;
+    throw Error(SDB_ERR_INVALID, "Unknown operation: " + op);
+}
+
+// std::stoi as the reference's Segment::search_operator uses it.
+int32_t stoi_ref(const std::string &s)
+{
+    try {
+        return (int32_t)std::stoi(s);
+    } catch (const std::exception &) {
+        throw Error(SDB_ERR_INVALID, "SEARCH bound is not an integer: '" + s + "'");
+    }
+}
+
+// ------------------------------------------------------------------ memory
+// Device bump allocator with a zeroed region of budget/64
+// (operations/memory_manager.cpp:219-233); reset per query.  Allocations are
+// 256-byte aligned (the reference aligns to 8).
+class MemoryManager {
+public:
+    MemoryManager() = default;
+    ~MemoryManager() { release(); }
+
+    void init(uint64_t budget, cudaStream_t s)
+    {
+        release();
+        size_ = budget;
+        zsize_ = std::max<uint64_t>(budget >> 6, 1u << 20);
+        SDB_CUDA(cudaMalloc(&base_, size_));
+        SDB_CUDA(cudaMalloc(&zbase_, zsize_));
+        SDB_CUDA(cudaMemsetAsync(zbase_, 0, zsize_, s));
+        used_ = zused_ = zdirty_ = 0;
+    }
+
+    void release()
+    {
+        if (base_) cudaFree(base_);
+        if (zbase_) cudaFree(zbase_);
+        base_ = zbase_ = nullptr;
+    }
+
+    template <typename T>
+    T *alloc(uint64_t count)
+    {
+        uint64_t bytes = (count * sizeof(T) + 255) & ~(uint64_t)255;
+        if (bytes == 0) bytes = 256;
+        if (used_ + bytes > size_)
+            throw Error(SDB_ERR_NOMEM, "Memory manager out of memory: requested " + std::to_string(bytes) +
+                                           " bytes, " + std::to_string(size_ - used_) + " bytes available");
+        T *p = reinterpret_cast<T *>(base_ + used_);
+        used_ += bytes;
+        peak_ = std::max(peak_, used_);
+        return p;
+    }
+
+    template <typename T>
+    T *alloc_zero(uint64_t count)
+    {
+        uint64_t bytes = (count * sizeof(T) + 255) & ~(uint64_t)255;
+        if (bytes == 0) bytes = 256;
+        if (zused_ + bytes > zsize_)
+            throw Error(SDB_ERR_NOMEM, "Memory manager out of zeroed memory: requested " + std::to_string(bytes) +
+                                           " bytes, " + std::to_string(zsize_ - zused_) + " bytes available");
+        T *p = reinterpret_cast<T *>(zbase_ + zused_);
+        zused_ += bytes;
+        zdirty_ = std::max(zdirty_, zused_);
+        return p;
+    }
+
+    // memory_manager::reset (operations/memory_manager.cpp:71-90): rewind and
+    // re-zero what the zeroed region handed out.
+    void reset(cudaStream_t s)
+    {
+        used_ = 0;
+        if (zdirty_) SDB_CUDA(cudaMemsetAsync(zbase_, 0, zdirty_, s));
+        zused_ = zdirty_ = 0;
+    }
+
+    uint64_t peak() const { return peak_; }
+
+private:
+    char *base_ = nullptr, *zbase_ = nullptr;
+    uint64_t size_ = 0, used_ = 0, peak_ = 0;
+    uint64_t zsize_ = 0, zused_ = 0, zdirty_ = 0;
+};
+
+// ------------------------------------------------------------------ storage
+struct Segment {
+    int32_t *data = nullptr;   // int32 rows (device)
+    uint64_t *agg = nullptr;   // uint64 rows of an aggregate result (device)
+    uint64_t nrows = 0;
+    int32_t min = 0, max = 0;
+};
+
+struct Column {
+    std::vector<Segment> segments;
+    bool is_aggregate_result = false;
+
+    // models/models.hpp:1257-1272
+    std::pair<int32_t, int32_t> get_min_max() const
+    {
+        if (is_aggregate_result) throw Error(SDB_ERR_INVALID, "can't get min/max of aggregate result column");
+        if (segments.empty()) throw Error(SDB_ERR_INVALID, "column is not loaded");
+        int32_t mn = segments[0].min, mx = segments[0].max;
+        for (size_t i = 1; i < segments.size(); i++) {
+            mn = std::min(mn, segments[i].min);
+            mx = std::max(mx, segments[i].max);
+        }
+        return {mn, mx};
+    }
+};
+
+std::vector<std::pair<uint64_t, uint64_t>> split_rows(uint64_t n, uint64_t seg)
+{
+    std::vector<std::pair<uint64_t, uint64_t>> out;
+    for (uint64_t s = 0; s < n; s += seg) out.emplace_back(s, std::min(seg, n - s));
+    return out;
+}
+
+struct Table {
+    std::string name;
+    std::vector<Column> columns;
+    uint64_t nrows = 0;
+    std::vector<int32_t *> owned;  // device copies made by load_table
+};
+
+// ------------------------------------------------------------------ kernels
+enum class KernelType : uint8_t {  // models/execution.hpp:30-46
+    EmptyKernel,
+    LogicalKernel,
+    SelectionKernelColumns,
+    SelectionKernelLiteral,
+    FillKernel,
+    PerformOperationKernelColumns,
+    PerformOperationKernelLiteralFirst,
+    PerformOperationKernelLiteralSecond,
+    BuildKeysHTKernel,
+    FilterJoinKernel,
+    BuildKeyValsHTKernel,
+    FullJoinKernel,
+    AggregateOperationKernel,
+    GroupByAggregateKernel,
+};
+
+const char *kernel_name(KernelType t)
+{
+    switch (t) {
+    case KernelType::EmptyKernel: return "empty";
+    case KernelType::LogicalKernel: return "logical";
+    case KernelType::SelectionKernelColumns: return "select_cols";
+    case KernelType::SelectionKernelLiteral: return "select_lit";
+    case KernelType::FillKernel: return "fill_i32";
+    case KernelType::PerformOperationKernelColumns: return "binop_cc";
+    case KernelType::PerformOperationKernelLiteralFirst: return "binop_lc";
+    case KernelType::PerformOperationKernelLiteralSecond: return "binop_cl";
+    case KernelType::BuildKeysHTKernel: return "ht_build_keys";
+    case KernelType::FilterJoinKernel: return "probe_semi";
+    case KernelType::BuildKeyValsHTKernel: return "ht_build_kv";
+    case KernelType::FullJoinKernel: return "probe_full";
+    case KernelType::AggregateOperationKernel: return "sum";
+    case KernelType::GroupByAggregateKernel: return "groupby";
+    }
+    return "?";
+}
+
+// Type-erased operator: the fields a KernelDefinition subclass would hold.
+struct KernelData {
+    KernelType type = KernelType::EmptyKernel;
+    uint64_t n = 0;
+    int cmp = 0, logic = 0, bin = 0;
+    const int32_t *a = nullptr, *b = nullptr;
+    int32_t la = 0, lb = 0;
+    const uint8_t *in = nullptr, *local = nullptr;
+    uint8_t *out = nullptr;
+    int32_t *res = nullptr;            // fill / perform result, full-join value output
+    void *ht = nullptr;
+    int32_t ht_min = 0, ht_max = 0, ht_len = 0;
+    uint64_t *agg_res = nullptr;
+    std::vector<const int32_t *> keys;  // group-by
+    std::vector<int32_t> mins, maxs;
+    std::vector<int32_t *> out_keys;
+    uint64_t P = 0;
+    uint32_t *occ = nullptr;
+
+    // KernelData::execute (models/execution.hpp:260-497): one C ABI call.
+    int execute(cudaStream_t s) const
+    {
+        auto st = (sdb_stream_t)s;
+        switch (type) {
+        case KernelType::EmptyKernel: return SDB_OK;
+        case KernelType::LogicalKernel: return sdb_logical(logic, in, local, out, n, st);
+        case KernelType::SelectionKernelColumns: return sdb_select_cols(a, b, cmp, logic, in, out, n, st);
+        case KernelType::SelectionKernelLiteral: return sdb_select_lit(a, lb, cmp, logic, in, out, n, st);
+        case KernelType::FillKernel: return sdb_fill_i32(res, la, n, st);
+        case KernelType::PerformOperationKernelColumns: return sdb_binop_cc(res, a, b, bin, in, n, st);
+        case KernelType::PerformOperationKernelLiteralFirst: return sdb_binop_lc(res, la, b, bin, in, n, st);
+        case KernelType::PerformOperationKernelLiteralSecond: return sdb_binop_cl(res, a, lb, bin, in, n, st);
+        case KernelType::BuildKeysHTKernel:
+            return sdb_ht_build_keys(a, in, n, static_cast<uint8_t *>(ht), ht_min, ht_len, st);
+        case KernelType::FilterJoinKernel:
+            return sdb_probe_semi(a, in, out, n, static_cast<const uint8_t *>(ht), ht_min, ht_max, st);
+        case KernelType::BuildKeyValsHTKernel:
+            return sdb_ht_build_kv(a, b, in, n, static_cast<int32_t *>(ht), ht_min, ht_len, st);
+        case KernelType::FullJoinKernel:
+            return sdb_probe_full(a, res, in, out, n, static_cast<const int32_t *>(ht), ht_min, ht_max, st);
+        case KernelType::AggregateOperationKernel: return sdb_sum_i32_u64(a, in, n, agg_res, st);
+        case KernelType::GroupByAggregateKernel:
+            return sdb_groupby_sum(keys.data(), mins.data(), maxs.data(), (int)keys.size(), a, in, n, P,
+                                   out_keys.data(), agg_res, occ, st);
+        }
+        return sdb_set_error(SDB_ERR_INVALID, "Unknown kernel type");
+    }
+};
+
+struct KernelBundle {  // models/execution.hpp:500-651 (one device, no host wait)
+    std::vector<KernelData> kernels;
+    bool on_device = true;
+    int device_index = 0;
+    void add_kernel(KernelData k) { kernels.push_back(std::move(k)); }
+};
+
+// ------------------------------------------------------------------ profiling
+struct Profiler {
+    bool on = false;
+    struct Rec { std::string name; cudaEvent_t a, b; };
+    std::vector<Rec> recs;
+    std::vector<cudaEvent_t> pool;
+    std::map<std::string, std::pair<uint64_t, double>> stats;
+
+    cudaEvent_t ev()
+    {
+        if (!pool.empty()) {
+            cudaEvent_t e = pool.back();
+            pool.pop_back();
+            return e;
+        }
+        cudaEvent_t e;
+        SDB_CUDA(cudaEventCreate(&e));
+        return e;
+    }
+    void begin(cudaStream_t s, const std::string &name, cudaEvent_t &a)
+    {
+        if (!on) return;
+        a = ev();
+        SDB_CUDA(cudaEventRecord(a, s));
+        recs.push_back({name, a, nullptr});
+    }
+    void end(cudaStream_t s)
+    {
+        if (!on) return;
+        cudaEvent_t b = ev();
+        SDB_CUDA(cudaEventRecord(b, s));
+        recs.back().b = b;
+    }
+    void collect()
+    {
+        for (auto &r : recs) {
+            float ms = 0;
+            if (r.b && cudaEventSynchronize(r.b) == cudaSuccess && cudaEventElapsedTime(&ms, r.a, r.b) == cudaSuccess) {
+                auto &st = stats[r.name];
+                st.first += 1;
+                st.second += ms;
+            }
+            pool.push_back(r.a);
+            if (r.b) pool.push_back(r.b);
+        }
+        recs.clear();
+    }
+    ~Profiler()
+    {
+        for (auto e : pool) cudaEventDestroy(e);
+    }
+};
+
+struct Engine;
+
+// ------------------------------------------------------------------ fusion
+// Turns runs of a segment's kernel list into sdb_fused_chain launches.
+struct Fuser {
+    static bool fusable(KernelType t)
+    {
+        switch (t) {
+        case KernelType::SelectionKernelLiteral:
+        case KernelType::SelectionKernelColumns:
+        case KernelType::LogicalKernel:
+        case KernelType::FilterJoinKernel:
+        case KernelType::FullJoinKernel:
+        case KernelType::PerformOperationKernelColumns:
+        case KernelType::PerformOperationKernelLiteralFirst:
+        case KernelType::PerformOperationKernelLiteralSecond:
+        case KernelType::FillKernel:
+        case KernelType::AggregateOperationKernel:
+        case KernelType::GroupByAggregateKernel:
+            return true;
+        default:
+            return false;
+        }
+    }
+
+    // Builds a chain from ks[i..]; returns the index after the last kernel
+    // consumed, or i when no chain of two or more kernels could be formed.
+    static size_t build(const std::vector<const KernelData *> &ks, size_t i,
+                        const std::set<const uint8_t *> &all_true, sdb_chain_desc &c)
+    {
+        std::memset(&c, 0, sizeof c);
+        const KernelData &first = *ks[i];
+        const uint8_t *cur = nullptr;
+        std::unordered_map<const int32_t *, int> regmap;  // column produced in-chain -> register
+        int nregs = 0;
+        size_t j = i;
+        bool terminal = false, flags_in_set = false;
+        c.n = first.n;
+
+        auto operand = [&](const int32_t *col) {
+            sdb_operand o{};
+            auto it = regmap.find(col);
+            if (it != regmap.end()) {
+                o.kind = SDB_SRC_REG;
+                o.reg = it->second;
+            } else {
+                o.kind = SDB_SRC_COL;
+                o.col = col;
+            }
+            return o;
+        };
+        auto lit = [](int32_t v) {
+            sdb_operand o{};
+            o.kind = SDB_SRC_LIT;
+            o.lit = v;
+            return o;
+        };
+
+        while (j < ks.size() && c.n_ops < SDB_CHAIN_MAX_OPS && !terminal) {
+            const KernelData &k = *ks[j];
+            if (k.n != c.n || !fusable(k.type)) break;
+            sdb_chain_op op{};
+            size_t consumed = 1;
+            // The first kernel fixes the chain's input flags.
+            const uint8_t *kin = k.in;
+            if (k.type == KernelType::SelectionKernelLiteral && k.in == k.out) {
+                // SEARCH: select(local,NONE) ; select(local,AND|OR) ; logical(in, local, out)
+                if (j + 2 >= ks.size()) break;
+                const KernelData &k2 = *ks[j + 1], &k3 = *ks[j + 2];
+                if (k2.type != KernelType::SelectionKernelLiteral || k3.type != KernelType::LogicalKernel) break;
+                if (k2.in != k.out || k2.out != k.out || k3.local != k.out || k.a != k2.a || k.logic != SDB_NONE ||
+                    k2.n != c.n || k3.n != c.n)
+                    break;
+                if (k.cmp == SDB_GE && k2.cmp == SDB_LE && k2.logic == SDB_AND) {
+                    op.kind = SDB_OP_SEARCH_RANGE;
+                } else if (k.cmp == SDB_EQ && k2.cmp == SDB_EQ && k2.logic == SDB_OR) {
+                    op.kind = SDB_OP_SEARCH_POINTS;
+                } else {
+                    break;
+                }
+                op.a = operand(k.a);
+                op.lo = k.lb;
+                op.hi = k2.lb;
+                op.logic_op = k3.logic;
+                kin = k3.in;
+                if (cur && kin != cur) break;
+                cur = k3.out;
+                consumed = 3;
+            } else {
+                if (cur && kin != cur) break;
+                switch (k.type) {
+                case KernelType::SelectionKernelLiteral:
+                    op.kind = SDB_OP_SELECT;
+                    op.cmp_op = k.cmp;
+                    op.logic_op = k.logic;
+                    op.a = operand(k.a);
+                    op.b = lit(k.lb);
+                    cur = k.out;
+                    break;
+                case KernelType::SelectionKernelColumns:
+                    op.kind = SDB_OP_SELECT;
+                    op.cmp_op = k.cmp;
+                    op.logic_op = k.logic;
+                    op.a = operand(k.a);
+                    op.b = operand(k.b);
+                    cur = k.out;
+                    break;
+                case KernelType::FilterJoinKernel:
+                    op.kind = SDB_OP_SEMI_PROBE;
+                    op.a = operand(k.a);
+                    op.lo = k.ht_min;
+                    op.hi = k.ht_max;
+                    op.ht = k.ht;
+                    cur = k.out;
+                    break;
+                case KernelType::FullJoinKernel:
+                    if (nregs >= SDB_CHAIN_MAX_REGS) goto done;
+                    op.kind = SDB_OP_FULL_PROBE;
+                    op.a = operand(k.a);
+                    op.lo = k.ht_min;
+                    op.hi = k.ht_max;
+                    op.ht = k.ht;
+                    op.out_reg = nregs;
+                    op.out_col = k.res;
+                    regmap[k.res] = nregs++;
+                    cur = k.out;
+                    break;
+                case KernelType::PerformOperationKernelColumns:
+                case KernelType::PerformOperationKernelLiteralFirst:
+                case KernelType::PerformOperationKernelLiteralSecond:
+                    if (nregs >= SDB_CHAIN_MAX_REGS) goto done;
+                    op.kind = SDB_OP_BINOP;
+                    op.bin_op = k.bin;
+                    op.a = k.type == KernelType::PerformOperationKernelLiteralFirst ? lit(k.la) : operand(k.a);
+                    op.b = k.type == KernelType::PerformOperationKernelLiteralSecond ? lit(k.lb) : operand(k.b);
+                    op.out_reg = nregs;
+                    op.out_col = k.res;
+                    regmap[k.res] = nregs++;
+                    if (!cur) cur = k.in;  // reads flags without changing them
+                    break;
+                case KernelType::FillKernel:
+                    if (nregs >= SDB_CHAIN_MAX_REGS) goto done;
+                    op.kind = SDB_OP_FILL;
+                    op.a = lit(k.la);
+                    op.out_reg = nregs;
+                    op.out_col = k.res;
+                    regmap[k.res] = nregs++;
+                    break;
+                case KernelType::AggregateOperationKernel:
+                    if (!cur) cur = k.in;
+                    c.terminal = SDB_TERM_SUM;
+                    c.value = operand(k.a);
+                    c.sum_out = k.agg_res;
+                    terminal = true;
+                    break;
+                case KernelType::GroupByAggregateKernel:
+                    if (k.keys.size() > SDB_CHAIN_MAX_KEYS) goto done;
+                    if (!cur) cur = k.in;
+                    c.terminal = SDB_TERM_GROUPBY;
+                    c.value = operand(k.a);
+                    c.n_keys = (int32_t)k.keys.size();
+                    for (size_t q = 0; q < k.keys.size(); q++) {
+                        c.keys[q] = operand(k.keys[q]);
+                        c.key_min[q] = k.mins[q];
+                        c.key_max[q] = k.maxs[q];
+                        c.out_keys[q] = k.out_keys[q];
+                    }
+                    c.P = k.P;
+                    c.out_sum = k.agg_res;
+                    c.occ = k.occ;
+                    terminal = true;
+                    break;
+                default:
+                    goto done;
+                }
+            }
+            if (!flags_in_set && kin) {
+                c.flags_in = kin;
+                flags_in_set = true;
+            }
+            if (!terminal) c.ops[c.n_ops++] = op;
+            j += consumed;
+        }
+    done:
+        const size_t count = j - i;
+        if (count < 2) return i;
+        // The input flags are not read when they are an untouched all-true
+        // buffer, or when the first op overwrites them (logic NONE).
+        if (c.flags_in && all_true.count(c.flags_in)) c.flags_in = nullptr;
+        if (c.n_ops > 0 &&
+            (c.ops[0].kind == SDB_OP_SELECT || c.ops[0].kind == SDB_OP_SEARCH_RANGE ||
+             c.ops[0].kind == SDB_OP_SEARCH_POINTS) &&
+            c.ops[0].logic_op == SDB_NONE)
+            c.flags_in = nullptr;
+        // Terminal: flags for a plain run; aggregates leave every
+        // intermediate dead (apply_aggregate replaces flags and columns).
+        if (!terminal) {
+            c.terminal = SDB_TERM_FLAGS;
+            c.flags_out = const_cast<uint8_t *>(cur);
+        } else {
+            for (int q = 0; q < c.n_ops; q++) c.ops[q].out_col = nullptr;
+            c.flags_out = nullptr;
+        }
+        if (!terminal && !c.flags_out) return i;
+        return j;
+    }
+};
+
+// ------------------------------------------------------------------ engine state
+struct Engine {
+    sdb_engine_config cfg{};
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    uint64_t seg = kDefaultSegment;
+    MemoryManager mm;
+    std::map<std::string, std::unique_ptr<Table>> tables;
+    Profiler prof;
+    double last_plan_ms = 0;
+    cudaEvent_t plan_a = nullptr, plan_b = nullptr;
+    // flag buffers known to hold all-true (filled at TransientTable creation
+    // and not written since)
+    std::set<const uint8_t *> all_true;
+
+    void run_kernel(const KernelData &k)
+    {
+        cudaEvent_t a = nullptr;
+        prof.begin(stream, kernel_name(k.type), a);
+        check(k.execute(stream));
+        prof.end(stream);
+        if (k.out) all_true.erase(k.out);
+    }
+
+    void run_chain(const sdb_chain_desc &c)
+    {
+        cudaEvent_t a = nullptr;
+        prof.begin(stream, "fused_chain", a);
+        check(sdb_fused_chain(&c, (sdb_stream_t)stream));
+        prof.end(stream);
+        if (c.flags_out) all_true.erase(c.flags_out);
+    }
+
+    // KernelBundle::execute for one segment, fusing runs when enabled.
+    void run_kernels(const std::vector<const KernelData *> &ks)
+    {
+        size_t i = 0;
+        while (i < ks.size()) {
+            if (cfg.fuse && Fuser::fusable(ks[i]->type)) {
+                sdb_chain_desc c;
+                size_t j = Fuser::build(ks, i, all_true, c);
+                if (j > i) {
+                    run_chain(c);
+                    i = j;
+                    continue;
+                }
+            }
+            run_kernel(*ks[i]);
+            i++;
+        }
+    }
+};
+
+// ------------------------------------------------------------------ TransientTable
+class TransientTable {
+public:
+    Engine &E;
+    uint64_t nrows;
+    uint8_t *flags = nullptr;
+    uint8_t *flags_secondary = nullptr;
+    std::vector<Column *> current_columns;
+    std::deque<Column> materialized_columns;
+    Column *group_by_column = nullptr;
+    uint64_t group_by_column_index = 0;
+    std::vector<std::vector<KernelBundle>> pending_kernels;
+
+    // models/transient_table.hpp:52-156: flags filled with true.
+    TransientTable(Engine &e, Table *base) : E(e), nrows(base->nrows)
+    {
+        flags = E.mm.alloc<uint8_t>(nrows);
+        check(sdb_fill_u8(flags, nrows, 1, (sdb_stream_t)E.stream));
+        E.all_true.insert(flags);
+        for (Column &c : base->columns) current_columns.push_back(&c);
+    }
+
+    uint64_t seg() const { return E.seg; }
+    std::vector<std::pair<uint64_t, uint64_t>> segs() const { return split_rows(nrows, E.seg); }
+
+    void set_group_by_column(uint64_t col)
+    {
+        if (col >= current_columns.size()) throw Error(SDB_ERR_INVALID, "group-by column index out of range");
+        group_by_column = current_columns[col];
+        group_by_column_index = col;
+    }
+
+    void ensure_secondary()
+    {
+        if (!flags_secondary) flags_secondary = E.mm.alloc<uint8_t>(nrows);
+    }
+
+    void swap_flag_buffers()
+    {
+        if (flags_secondary) std::swap(flags, flags_secondary);
+    }
+
+    // models/transient_table.hpp:347-381
+    void add_pending_kernels(const std::vector<KernelBundle> &ops)
+    {
+        if (pending_kernels.empty()) {
+            pending_kernels.push_back(ops);
+            return;
+        }
+        auto &last = pending_kernels.back();
+        bool can_merge = last.size() == ops.size();
+        for (size_t i = 0; i < ops.size() && can_merge; i++)
+            if (last[i].on_device != ops[i].on_device || last[i].device_index != ops[i].device_index) can_merge = false;
+        if (can_merge) {
+            for (size_t i = 0; i < ops.size(); i++)
+                for (const auto &k : ops[i].kernels) last[i].add_kernel(k);
+        } else {
+            pending_kernels.push_back(ops);
+        }
+    }
+
+    // models/transient_table.hpp:383-506: segment by segment, phases in order.
+    void execute_pending_kernels()
+    {
+        if (pending_kernels.empty()) return;
+        const size_t nseg = segs().size();
+        for (const auto &ph : pending_kernels)
+            if (ph.size() != nseg) throw Error(SDB_ERR_INVALID, "Pending kernels segment number mismatch.");
+        for (size_t s = 0; s < nseg; s++) {
+            std::vector<const KernelData *> ks;
+            for (const auto &ph : pending_kernels)
+                for (const auto &k : ph[s].kernels) ks.push_back(&k);
+            E.run_kernels(ks);
+        }
+        pending_kernels.clear();
+    }
+
+    Column &new_materialized(uint64_t n)
+    {
+        Column &c = materialized_columns.emplace_back();
+        for (auto [start, cnt] : split_rows(n, E.seg)) {
+            Segment s;
+            s.data = E.mm.alloc<int32_t>(cnt);
+            s.nrows = cnt;
+            c.segments.push_back(s);
+        }
+        return c;
+    }
+
+    Column *col_at(int64_t idx, const char *what)
+    {
+        if (idx < 0 || (uint64_t)idx >= current_columns.size() || current_columns[idx] == nullptr)
+            throw Error(SDB_ERR_INVALID, std::string(what) + ": column index " + std::to_string(idx) + " is not available");
+        Column *c = current_columns[idx];
+        if (c->segments.size() != segs().size())
+            throw Error(SDB_ERR_INVALID, std::string(what) + ": column " + std::to_string(idx) + " is not loaded");
+        return c;
+    }
+
+    // models/transient_table.hpp:750-981
+    void apply_filter(const ExprType &expr, const std::string &parent_op)
+    {
+        if (expr.exprType != EXPR) return;  // the reference logs and returns
+        std::vector<KernelBundle> ops;
+        if (expr.op == "SEARCH") {
+            if (expr.operands.size() < 2) throw Error(SDB_ERR_INVALID, "SEARCH needs a column and a range set");
+            Column *col = col_at(expr.operands[0].input, "SEARCH");
+            const auto &rs = expr.operands[1].literal.rangeSet;
+            ensure_secondary();
+            const int logic = get_logical_op(parent_op);
+            int32_t lo, hi;
+            bool range = rs.size() == 1;
+            // Segment::search_operator: models/models.hpp:604-718
+            if (range) {
+                if (rs[0].size() < 3) throw Error(SDB_ERR_INVALID, "SEARCH range needs [kind, lower, upper]");
+                lo = stoi_ref(rs[0][1]);
+                hi = stoi_ref(rs[0][2]);
+            } else {
+                if (rs.size() < 2 || rs[0].size() < 2 || rs[1].size() < 2)
+                    throw Error(SDB_ERR_INVALID, "SEARCH needs one range or two points");
+                lo = stoi_ref(rs[0][1]);
+                hi = stoi_ref(rs[1][1]);
+            }
+            auto sg = segs();
+            for (size_t s = 0; s < sg.size(); s++) {
+                const uint64_t off = sg[s].first, cnt = sg[s].second;
+                uint8_t *local = E.mm.alloc<uint8_t>(cnt);
+                KernelBundle bundle;
+                KernelData k1;
+                k1.type = KernelType::SelectionKernelLiteral;
+                k1.n = cnt;
+                k1.a = col->segments[s].data;
+                k1.in = local;
+                k1.out = local;
+                k1.cmp = range ? SDB_GE : SDB_EQ;
+                k1.logic = SDB_NONE;
+                k1.lb = lo;
+                KernelData k2 = k1;
+                k2.cmp = range ? SDB_LE : SDB_EQ;
+                k2.logic = range ? SDB_AND : SDB_OR;
+                k2.lb = hi;
+                KernelData k3;
+                k3.type = KernelType::LogicalKernel;
+                k3.n = cnt;
+                k3.logic = logic;
+                k3.in = flags + off;
+                k3.local = local;
+                k3.out = flags_secondary + off;
+                bundle.add_kernel(k1);
+                bundle.add_kernel(k2);
+                bundle.add_kernel(k3);
+                ops.push_back(bundle);
+            }
+            add_pending_kernels(ops);
+            swap_flag_buffers();
+        } else if (is_filter_logical(expr.op)) {
+            bool parent_op_used = false;
+            for (const ExprType &operand : expr.operands) {
+                apply_filter(operand, parent_op_used ? expr.op : parent_op);
+                parent_op_used = true;
+            }
+        } else {
+            if (expr.operands.size() != 2) return;  // the reference logs and returns
+            Column *cols[2] = {nullptr, nullptr};
+            bool literal = false;
+            int32_t literal_value = 0;
+            for (int i = 0; i < 2; i++) {
+                const ExprType &o = expr.operands[i];
+                if (o.exprType == COLUMN) {
+                    cols[i] = col_at(o.input, "filter");
+                } else if (o.exprType == LITERAL) {
+                    literal = true;
+                    literal_value = (int32_t)o.literal.value;
+                } else {
+                    return;  // the reference logs and returns
+                }
+            }
+            if (!cols[0])
+                throw Error(SDB_ERR_UNSUPPORTED, "filter comparison needs a column as its first operand");
+            ensure_secondary();
+            const int cmp = get_comp_op(expr.op), logic = get_logical_op(parent_op);
+            auto sg = segs();
+            for (size_t s = 0; s < sg.size(); s++) {
+                const uint64_t off = sg[s].first, cnt = sg[s].second;
+                KernelBundle bundle;
+                KernelData k;
+                k.type = literal ? KernelType::SelectionKernelLiteral : KernelType::SelectionKernelColumns;
+                k.n = cnt;
+                k.cmp = cmp;
+                k.logic = logic;
+                k.a = cols[0]->segments[s].data;
+                if (literal)
+                    k.lb = literal_value;
+                else
+                    k.b = cols[1]->segments[s].data;
+                k.in = flags + off;
+                k.out = flags_secondary + off;
+                bundle.add_kernel(k);
+                ops.push_back(bundle);
+            }
+            add_pending_kernels(ops);
+            swap_flag_buffers();
+        }
+    }
+
+    // models/transient_table.hpp:983-1224
+    void apply_project(const std::vector<ExprType> &exprs)
+    {
+        std::vector<Column *> new_columns;
+        for (size_t i = 0; i < exprs.size(); i++) {
+            const ExprType &expr = exprs[i];
+            if (expr.exprType == COLUMN) {
+                if (expr.input < 0 || (uint64_t)expr.input >= current_columns.size())
+                    throw Error(SDB_ERR_INVALID, "project: column index out of range");
+                new_columns.push_back(current_columns[expr.input]);
+                if ((uint64_t)expr.input == group_by_column_index) group_by_column_index = i;
+            } else if (expr.exprType == LITERAL) {
+                const int32_t v = (int32_t)expr.literal.value;
+                Column &nc = new_materialized(nrows);
+                std::vector<KernelBundle> ops;
+                for (auto &s : nc.segments) {  // Segment::fill_with_literal: models/models.hpp:293-326
+                    s.min = s.max = v;
+                    KernelBundle b;
+                    KernelData k;
+                    k.type = KernelType::FillKernel;
+                    k.n = s.nrows;
+                    k.res = s.data;
+                    k.la = v;
+                    b.add_kernel(k);
+                    ops.push_back(b);
+                }
+                add_pending_kernels(ops);
+                new_columns.push_back(&nc);
+            } else {
+                if (expr.operands.size() != 2) return;  // the reference logs and returns
+                const int bop = get_op_from_string(expr.op);
+                const ExprType &x = expr.operands[0], &y = expr.operands[1];
+                Column *ca = nullptr, *cb = nullptr;
+                KernelType kt;
+                if (x.exprType == COLUMN && y.exprType == COLUMN) {
+                    ca = col_at(x.input, "project");
+                    cb = col_at(y.input, "project");
+                    kt = KernelType::PerformOperationKernelColumns;
+                } else if (x.exprType == LITERAL && y.exprType == COLUMN) {
+                    cb = col_at(y.input, "project");
+                    kt = KernelType::PerformOperationKernelLiteralFirst;
+                } else if (x.exprType == COLUMN && y.exprType == LITERAL) {
+                    ca = col_at(x.input, "project");
+                    kt = KernelType::PerformOperationKernelLiteralSecond;
+                } else {
+                    return;  // the reference logs and returns
+                }
+                Column &nc = new_materialized(nrows);
+                std::vector<KernelBundle> ops;
+                auto sg = segs();
+                for (size_t s = 0; s < sg.size(); s++) {
+                    Segment &r = nc.segments[s];
+                    // Segment::perform_operator: models/models.hpp:760-845 (min/max of the operands' stats)
+                    if (kt == KernelType::PerformOperationKernelColumns) {
+                        r.min = std::min(ca->segments[s].min, cb->segments[s].min);
+                        r.max = std::max(ca->segments[s].max, cb->segments[s].max);
+                    } else if (kt == KernelType::PerformOperationKernelLiteralSecond) {
+                        r.min = ca->segments[s].min;
+                        r.max = ca->segments[s].max;
+                    } else {
+                        r.min = cb->segments[s].min;
+                        r.max = cb->segments[s].max;
+                    }
+                    KernelBundle b;
+                    KernelData k;
+                    k.type = kt;
+                    k.n = sg[s].second;
+                    k.res = r.data;
+                    k.bin = bop;
+                    k.a = ca ? ca->segments[s].data : nullptr;
+                    k.b = cb ? cb->segments[s].data : nullptr;
+                    k.la = (int32_t)x.literal.value;
+                    k.lb = (int32_t)y.literal.value;
+                    k.in = flags + sg[s].first;
+                    b.add_kernel(k);
+                    ops.push_back(b);
+                }
+                add_pending_kernels(ops);
+                new_columns.push_back(&nc);
+            }
+        }
+        current_columns = new_columns;
+    }
+
+    // models/transient_table.hpp:1226-1647
+    void apply_aggregate(const AggType &agg, const std::vector<int64_t> &group)
+    {
+        if (agg.operands.empty()) throw Error(SDB_ERR_UNSUPPORTED, "aggregate without an operand (COUNT(*) is not supported)");
+        Column *acol = col_at(agg.operands[0], "aggregate");
+        if (acol->is_aggregate_result) throw Error(SDB_ERR_UNSUPPORTED, "aggregate over an aggregate result");
+        auto sg = segs();
+        std::vector<KernelBundle> bundles;
+        if (group.empty()) {
+            uint64_t *final_result = E.mm.alloc_zero<uint64_t>(1);
+            for (size_t s = 0; s < sg.size(); s++) {
+                KernelBundle b;
+                KernelData k;
+                k.type = KernelType::AggregateOperationKernel;
+                k.n = sg[s].second;
+                k.a = acol->segments[s].data;
+                k.in = flags + sg[s].first;
+                k.agg_res = final_result;
+                b.add_kernel(k);
+                bundles.push_back(b);
+            }
+            add_pending_kernels(bundles);
+            execute_pending_kernels();
+            nrows = 1;
+            flags = E.mm.alloc<uint8_t>(1);
+            check(sdb_fill_u8(flags, 1, 1, (sdb_stream_t)E.stream));
+            flags_secondary = nullptr;
+            Column &rc = materialized_columns.emplace_back();
+            rc.is_aggregate_result = true;
+            Segment s;
+            s.agg = final_result;
+            s.nrows = 1;
+            rc.segments.push_back(s);
+            current_columns.clear();
+            current_columns.push_back(&rc);
+            return;
+        }
+        std::vector<Column *> gcols;
+        std::vector<int32_t> mins, maxs;
+        uint64_t P = 1;
+        for (int64_t gi : group) {
+            Column *c = col_at(gi, "group-by");
+            auto mm = c->get_min_max();
+            mins.push_back(mm.first);
+            maxs.push_back(mm.second);
+            P *= (uint64_t)(int64_t)(int32_t)((uint32_t)mm.second - (uint32_t)mm.first + 1u);
+            gcols.push_back(c);
+        }
+        if (P == 0 || P > (1ull << 31)) throw Error(SDB_ERR_NOMEM, "group-by slot array too large: " + std::to_string(P));
+        uint64_t *aggregate_result = E.mm.alloc_zero<uint64_t>(P);
+        uint32_t *temp_flags = E.mm.alloc_zero<uint32_t>(P);
+        std::vector<int32_t *> results;
+        for (size_t i = 0; i < group.size(); i++) results.push_back(E.mm.alloc<int32_t>(P));
+        for (size_t s = 0; s < sg.size(); s++) {
+            KernelBundle b;
+            KernelData k;
+            k.type = KernelType::GroupByAggregateKernel;
+            k.n = sg[s].second;
+            k.a = acol->segments[s].data;
+            k.in = flags + sg[s].first;
+            for (Column *c : gcols) k.keys.push_back(c->segments[s].data);
+            k.mins = mins;
+            k.maxs = maxs;
+            k.out_keys = results;
+            k.P = P;
+            k.agg_res = aggregate_result;
+            k.occ = temp_flags;
+            b.add_kernel(k);
+            bundles.push_back(b);
+        }
+        add_pending_kernels(bundles);
+        execute_pending_kernels();
+        uint8_t *new_flags = E.mm.alloc<uint8_t>(P);
+        {
+            cudaEvent_t a = nullptr;
+            E.prof.begin(E.stream, "occ_to_flags", a);
+            check(sdb_occ_to_flags(temp_flags, new_flags, P, (sdb_stream_t)E.stream));
+            E.prof.end(E.stream);
+        }
+        flags = new_flags;
+        flags_secondary = nullptr;
+        nrows = P;
+        current_columns.clear();
+        auto out_segs = split_rows(P, E.seg);
+        for (size_t i = 0; i < group.size(); i++) {
+            Column &c = materialized_columns.emplace_back();
+            for (auto [start, cnt] : out_segs) {
+                Segment s;
+                s.data = results[i] + start;
+                s.nrows = cnt;
+                c.segments.push_back(s);
+            }
+            current_columns.push_back(&c);
+        }
+        Column &ac = materialized_columns.emplace_back();
+        ac.is_aggregate_result = true;
+        for (auto [start, cnt] : out_segs) {
+            Segment s;
+            s.agg = aggregate_result + start;
+            s.nrows = cnt;
+            ac.segments.push_back(s);
+        }
+        current_columns.push_back(&ac);
+    }
+
+    // models/transient_table.hpp:1649-1927
+    void apply_join(TransientTable &right, const RelNode &rel)
+    {
+        if (rel.condition.operands.size() < 2) throw Error(SDB_ERR_INVALID, "join condition needs two operands");
+        const int64_t left_column = rel.condition.operands[0].input;
+        const int64_t right_column = rel.condition.operands[1].input - (int64_t)current_columns.size();
+        if (left_column < 0 || (uint64_t)left_column >= current_columns.size() || right_column < 0 ||
+            (uint64_t)right_column >= right.current_columns.size())
+            throw Error(SDB_ERR_INVALID, "Invalid column indices in join condition.");
+        Column *probe = col_at(left_column, "join probe");
+        Column *build = right.col_at(right_column, "join build");
+        auto mm = build->get_min_max();
+        const int32_t mn = mm.first, mx = mm.second;
+        const int32_t len = (int32_t)((uint32_t)mx - (uint32_t)mn + 1u);
+        if (len <= 0) throw Error(SDB_ERR_NOMEM, "join key range too large");
+        auto lsg = segs();
+        auto rsg = right.segs();
+        if (rel.joinType == "semi") {
+            // Column::build_keys_hash_table: models/models.hpp:1413-1452
+            uint8_t *ht = E.mm.alloc_zero<uint8_t>((uint64_t)len);
+            std::vector<KernelBundle> hb;
+            for (size_t s = 0; s < rsg.size(); s++) {
+                KernelBundle b;
+                KernelData k;
+                k.type = KernelType::BuildKeysHTKernel;
+                k.n = rsg[s].second;
+                k.a = build->segments[s].data;
+                k.in = right.flags + rsg[s].first;
+                k.ht = ht;
+                k.ht_min = mn;
+                k.ht_len = len;
+                b.add_kernel(k);
+                hb.push_back(b);
+            }
+            right.add_pending_kernels(hb);
+            right.execute_pending_kernels();
+            ensure_secondary();
+            std::vector<KernelBundle> ops;  // Column::semi_join: models/models.hpp:1454-1507
+            for (size_t s = 0; s < lsg.size(); s++) {
+                KernelBundle b;
+                KernelData k;
+                k.type = KernelType::FilterJoinKernel;
+                k.n = lsg[s].second;
+                k.a = probe->segments[s].data;
+                k.in = flags + lsg[s].first;
+                k.out = flags_secondary + lsg[s].first;
+                k.ht = ht;
+                k.ht_min = mn;
+                k.ht_max = mx;
+                b.add_kernel(k);
+                ops.push_back(b);
+            }
+            add_pending_kernels(ops);
+            swap_flag_buffers();
+            for (size_t i = 0; i < right.current_columns.size(); i++) current_columns.push_back(nullptr);
+        } else {
+            Column *gb = right.group_by_column;
+            if (!gb) throw Error(SDB_ERR_UNSUPPORTED, "inner join needs a group-by column on the build side");
+            if (gb->segments.size() != rsg.size()) throw Error(SDB_ERR_INVALID, "build-side group-by column is not loaded");
+            auto gmm = gb->get_min_max();
+            Column &nc = new_materialized(nrows);
+            const uint64_t gidx = current_columns.size() + right.group_by_column_index;
+            for (size_t i = 0; i < right.current_columns.size(); i++) current_columns.push_back(nullptr);
+            current_columns[gidx] = &nc;
+            // Column::build_key_vals_hash_table: models/models.hpp:1509-1548
+            int32_t *ht = E.mm.alloc_zero<int32_t>(2 * (uint64_t)len);
+            std::vector<KernelBundle> hb;
+            for (size_t s = 0; s < rsg.size(); s++) {
+                KernelBundle b;
+                KernelData k;
+                k.type = KernelType::BuildKeyValsHTKernel;
+                k.n = rsg[s].second;
+                k.a = build->segments[s].data;
+                k.b = gb->segments[s].data;
+                k.in = right.flags + rsg[s].first;
+                k.ht = ht;
+                k.ht_min = mn;
+                k.ht_len = len;
+                b.add_kernel(k);
+                hb.push_back(b);
+            }
+            right.add_pending_kernels(hb);
+            right.execute_pending_kernels();
+            ensure_secondary();
+            std::vector<KernelBundle> ops;  // Column::full_join_operation: models/models.hpp:1550-1648
+            for (size_t s = 0; s < lsg.size(); s++) {
+                KernelBundle b;
+                KernelData k;
+                k.type = KernelType::FullJoinKernel;
+                k.n = lsg[s].second;
+                k.a = probe->segments[s].data;
+                k.res = nc.segments[s].data;
+                k.in = flags + lsg[s].first;
+                k.out = flags_secondary + lsg[s].first;
+                k.ht = ht;
+                k.ht_min = mn;
+                k.ht_max = mx;
+                nc.segments[s].min = gmm.first;
+                nc.segments[s].max = gmm.second;
+                b.add_kernel(k);
+                ops.push_back(b);
+            }
+            add_pending_kernels(ops);
+            swap_flag_buffers();
+        }
+    }
+};
+
+// ------------------------------------------------------------------ execution info
+void parse_expression_columns(const ExprType &e, std::set<int64_t> &cols)
+{
+    if (e.exprType == COLUMN)
+        cols.insert(e.input);
+    else if (e.exprType == EXPR)
+        for (const auto &o : e.operands) parse_expression_columns(o, cols);
+}
+
+// operations/preprocessing.cpp:14-102
+std::vector<int> dag_topological_sort(const PlanResult &p)
+{
+    const size_t n = p.rels.size();
+    std::vector<std::vector<char>> dag(n, std::vector<char>(n, 0));
+    std::deque<int> S;
+    for (const RelNode &r : p.rels) {
+        switch (r.relOp) {
+        case TABLE_SCAN: S.push_front((int)r.id); break;
+        case FILTER:
+        case PROJECT:
+        case AGGREGATE:
+        case SORT:
+            if (r.id < 1) return {};
+            dag[r.id - 1][r.id] = 1;
+            break;
+        case JOIN:
+            if (r.inputs.size() != 2) return {};
+            for (auto in : r.inputs)
+                if (in < 0 || (size_t)in >= n) return {};
+            dag[r.inputs[0]][r.id] = 1;
+            dag[r.inputs[1]][r.id] = 1;
+            break;
+        default: return {};
+        }
+    }
+    std::vector<int> sorted;
+    while (!S.empty()) {
+        int node = S.back();
+        S.pop_back();
+        if (!S.empty() && p.rels[node].relOp == TABLE_SCAN && p.rels[node].tables.size() > 1 &&
+            base_name(p.rels[node].tables[1]) == "lineorder") {
+            S.push_front(node);
+            continue;
+        }
+        sorted.push_back(node);
+        for (size_t i = 0; i < n; i++) {
+            if (dag[node][i] == 1) {
+                dag[node][i] = 0;
+                bool inbound = false;
+                for (size_t j = 0; j < n && !inbound; j++) inbound = dag[j][i] == 1;
+                if (!inbound) S.push_front((int)i);
+            }
+        }
+    }
+    if (sorted.size() != n) return {};
+    return sorted;
+}
+
+struct ExecutionInfo {
+    std::map<std::string, std::set<int>> loaded_columns;
+    std::map<std::string, int> group_by_columns;
+    std::vector<int> dag_order;
+};
+
+// operations/preprocessing.cpp:104-275
+ExecutionInfo parse_execution_info(const PlanResult &p)
+{
+    ExecutionInfo info;
+    std::vector<std::vector<std::pair<std::string, int>>> ops_info;
+    auto at = [](const std::vector<std::pair<std::string, int>> &v, int64_t i) -> const std::pair<std::string, int> & {
+        if (i < 0 || (size_t)i >= v.size()) throw Error(SDB_ERR_INVALID, "plan: column index " + std::to_string(i) + " out of range");
+        return v[i];
+    };
+    for (const RelNode &r : p.rels) {
+        switch (r.relOp) {
+        case TABLE_SCAN: {
+            if (r.tables.size() < 2) throw Error(SDB_ERR_INVALID, "TABLE_SCAN needs tables [schema, name]");
+            auto it = table_column_numbers().find(base_name(r.tables[1]));
+            if (it == table_column_numbers().end()) throw Error(SDB_ERR_INVALID, "unknown table " + r.tables[1]);
+            std::vector<std::pair<std::string, int>> t;
+            for (int i = 0; i < it->second; i++) t.emplace_back(r.tables[1], i);
+            ops_info.push_back(t);
+            info.loaded_columns[r.tables[1]];
+            break;
+        }
+        case FILTER: {
+            if (ops_info.empty()) throw Error(SDB_ERR_INVALID, "FILTER without input");
+            auto oi = ops_info.back();
+            std::set<int64_t> cols;
+            parse_expression_columns(r.condition, cols);
+            for (auto c : cols) info.loaded_columns[at(oi, c).first].insert(at(oi, c).second);
+            ops_info.push_back(oi);
+            break;
+        }
+        case PROJECT: {
+            if (ops_info.empty()) throw Error(SDB_ERR_INVALID, "PROJECT without input");
+            auto last = ops_info.back();
+            std::vector<std::pair<std::string, int>> oi;
+            for (const auto &e : r.exprs) {
+                std::set<int64_t> cols;
+                parse_expression_columns(e, cols);
+                for (auto c : cols) info.loaded_columns[at(last, c).first].insert(at(last, c).second);
+                if (!cols.empty()) oi.push_back(at(last, *cols.begin()));
+            }
+            ops_info.push_back(oi);
+            break;
+        }
+        case AGGREGATE: {
+            if (ops_info.empty()) throw Error(SDB_ERR_INVALID, "AGGREGATE without input");
+            auto last = ops_info.back();
+            std::vector<std::pair<std::string, int>> oi;
+            for (auto g : r.group) {
+                const auto &tc = at(last, g);
+                info.loaded_columns[tc.first].insert(tc.second);
+                oi.push_back(tc);
+                info.group_by_columns[tc.first] = tc.second;
+            }
+            for (const auto &a : r.aggs) {
+                for (auto c : a.operands) info.loaded_columns[at(last, c).first].insert(at(last, c).second);
+                if (!a.operands.empty()) oi.push_back(at(last, a.operands[0]));
+            }
+            ops_info.push_back(oi);
+            break;
+        }
+        case JOIN: {
+            if (r.inputs.size() != 2) throw Error(SDB_ERR_INVALID, "JOIN needs two inputs");
+            for (auto in : r.inputs)
+                if (in < 0 || (size_t)in >= ops_info.size()) throw Error(SDB_ERR_INVALID, "JOIN input out of range");
+            const auto &left = ops_info[r.inputs[0]];
+            const auto &right = ops_info[r.inputs[1]];
+            std::set<int64_t> cols;
+            parse_expression_columns(r.condition, cols);
+            for (auto c : cols) {
+                const auto &tc = (size_t)c < left.size() ? at(left, c) : at(right, c - (int64_t)left.size());
+                info.loaded_columns[tc.first].insert(tc.second);
+            }
+            auto oi = left;
+            oi.insert(oi.end(), right.begin(), right.end());
+            ops_info.push_back(oi);
+            break;
+        }
+        case SORT: {
+            if (ops_info.empty()) throw Error(SDB_ERR_INVALID, "SORT without input");
+            auto oi = ops_info.back();
+            for (const auto &c : r.collation)
+                if (c.field >= 0 && (size_t)c.field < oi.size()) info.loaded_columns[oi[c.field].first].insert(oi[c.field].second);
+            ops_info.push_back(oi);
+            break;
+        }
+        default:
+            throw Error(SDB_ERR_UNSUPPORTED, "Unsupported RelNodeType " + std::to_string(r.relOp));
+        }
+    }
+    info.dag_order = dag_topological_sort(p);
+    if (info.dag_order.empty()) throw Error(SDB_ERR_INVALID, "DAG topological sort failed");
+    return info;
+}
+
+}  // namespace sdb
+
+// ====================================================================== results
+struct sdb_result {
+    std::vector<int> types;  // 0 int32, 1 uint64
+    std::vector<std::vector<int32_t>> i32;
+    std::vector<std::vector<uint64_t>> u64;
+    uint64_t nrows = 0;
+};
+
+struct sdb_engine {
+    sdb::Engine E;
+};
+
+namespace sdb {
+
+// execute_ddor_plan (executor/ddor_executor.cpp:22-245) plus the result
+// materialisation of save_result (executor/result_writer.cpp:12-68).
+std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text)
+{
+    PlanResult plan = plan_from_json(plan_text);
+    ExecutionInfo info = parse_execution_info(plan);
+
+    E.mm.reset(E.stream);
+    E.all_true.clear();
+    if (E.cfg.profile) E.prof.stats.clear();
+    SDB_CUDA(cudaEventRecord(E.plan_a, E.stream));
+
+    std::deque<TransientTable> tts;
+    std::vector<int> output_table(plan.rels.size(), -1);
+    for (const RelNode &rel : plan.rels) {
+        if (rel.relOp != TABLE_SCAN) continue;
+        const std::string &name = rel.tables[1];
+        auto it = E.tables.find(name);
+        if (it == E.tables.end()) throw Error(SDB_ERR_INVALID, "Table " + name + " not found among loaded tables.");
+        for (int c : info.loaded_columns[name])
+            if ((size_t)c >= it->second->columns.size() || it->second->columns[c].segments.empty())
+                throw Error(SDB_ERR_INVALID, "column " + std::to_string(c) + " of table " + name + " is not loaded");
+        tts.emplace_back(E, it->second.get());
+        auto g = info.group_by_columns.find(name);
+        if (g != info.group_by_columns.end()) tts.back().set_group_by_column(g->second);
+        output_table[rel.id] = (int)tts.size() - 1;
+    }
+
+    for (int id : info.dag_order) {
+        const RelNode &rel = plan.rels[id];
+        auto prev = [&]() {
+            if (id < 1 || output_table[id - 1] < 0) throw Error(SDB_ERR_INVALID, "node has no input table");
+            return output_table[id - 1];
+        };
+        switch (rel.relOp) {
+        case TABLE_SCAN: break;
+        case FILTER: {
+            int t = prev();
+            tts[t].apply_filter(rel.condition, "");
+            output_table[id] = t;
+            break;
+        }
+        case PROJECT: {
+            int t = prev();
+            tts[t].apply_project(rel.exprs);
+            output_table[id] = t;
+            break;
+        }
+        case AGGREGATE: {
+            int t = prev();
+            if (rel.aggs.empty()) throw Error(SDB_ERR_INVALID, "AGGREGATE without aggs");
+            tts[t].apply_aggregate(rel.aggs[0], rel.group);
+            output_table[id] = t;
+            break;
+        }
+        case JOIN: {
+            int l = output_table[rel.inputs[0]], r = output_table[rel.inputs[1]];
+            if (l < 0 || r < 0) throw Error(SDB_ERR_INVALID, "JOIN input has no table");
+            tts[l].apply_join(tts[r], rel);
+            output_table[id] = l;
+            break;
+        }
+        case SORT: output_table[id] = prev(); break;
+        default: break;
+        }
+    }
+
+    TransientTable &fin = tts[output_table[plan.rels.size() - 1]];
+    fin.execute_pending_kernels();
+
+    // Materialise the flagged rows of the non-null columns, in row order.
+    auto res = std::make_unique<sdb_result>();
+    std::vector<Column *> cols;
+    for (Column *c : fin.current_columns)
+        if (c) {
+            if (c->segments.size() != fin.segs().size()) throw Error(SDB_ERR_INVALID, "result column is not loaded");
+            cols.push_back(c);
+        }
+    for (Column *c : cols) res->types.push_back(c->is_aggregate_result ? 1 : 0);
+    res->i32.resize(cols.size());
+    res->u64.resize(cols.size());
+    auto sg = fin.segs();
+    struct SegOut {
+        uint32_t *count;
+        std::vector<void *> dev;
+        uint64_t cap;
+    };
+    std::vector<SegOut> outs;
+    cudaEvent_t pa = nullptr;
+    E.prof.begin(E.stream, "materialize", pa);
+    for (size_t s = 0; s < sg.size(); s++) {
+        const uint64_t cnt = sg[s].second;
+        SegOut o;
+        o.cap = cnt;
+        int32_t *ids = E.mm.alloc<int32_t>(cnt);
+        o.count = E.mm.alloc<uint32_t>(1);
+        size_t sb = sdb_compact_scratch_bytes(cnt);
+        void *scratch = E.mm.alloc<uint8_t>(sb);
+        check(sdb_compact_row_ids(fin.flags + sg[s].first, cnt, ids, o.count, scratch, sb, (sdb_stream_t)E.stream));
+        for (Column *c : cols) {
+            const Segment &seg = c->segments[s];
+            if (c->is_aggregate_result) {
+                uint64_t *d = E.mm.alloc<uint64_t>(cnt);
+                check(sdb_gather_u64(seg.agg, ids, o.count, d, cnt, (sdb_stream_t)E.stream));
+                o.dev.push_back(d);
+            } else {
+                int32_t *d = E.mm.alloc<int32_t>(cnt);
+                check(sdb_gather_i32(seg.data, ids, o.count, d, cnt, (sdb_stream_t)E.stream));
+                o.dev.push_back(d);
+            }
+        }
+        outs.push_back(o);
+    }
+    E.prof.end(E.stream);
+    std::vector<uint32_t> counts(outs.size());
+    for (size_t s = 0; s < outs.size(); s++)
+        SDB_CUDA(cudaMemcpyAsync(&counts[s], outs[s].count, sizeof(uint32_t), cudaMemcpyDeviceToHost, E.stream));
+    SDB_CUDA(cudaStreamSynchronize(E.stream));
+    uint64_t total = 0;
+    for (auto c : counts) total += c;
+    for (size_t ci = 0; ci < cols.size(); ci++) {
+        if (res->types[ci] == 1)
+            res->u64[ci].resize(total);
+        else
+            res->i32[ci].resize(total);
+    }
+    uint64_t base = 0;
+    for (size_t s = 0; s < outs.size(); s++) {
+        for (size_t ci = 0; ci < cols.size(); ci++) {
+            if (!counts[s]) continue;
+            if (res->types[ci] == 1)
+                SDB_CUDA(cudaMemcpyAsync(res->u64[ci].data() + base, outs[s].dev[ci], counts[s] * sizeof(uint64_t),
+                                         cudaMemcpyDeviceToHost, E.stream));
+            else
+                SDB_CUDA(cudaMemcpyAsync(res->i32[ci].data() + base, outs[s].dev[ci], counts[s] * sizeof(int32_t),
+                                         cudaMemcpyDeviceToHost, E.stream));
+        }
+        base += counts[s];
+    }
+    SDB_CUDA(cudaEventRecord(E.plan_b, E.stream));
+    SDB_CUDA(cudaStreamSynchronize(E.stream));
+    res->nrows = total;
+    float ms = 0;
+    SDB_CUDA(cudaEventElapsedTime(&ms, E.plan_a, E.plan_b));
+    E.last_plan_ms = ms;
+    E.prof.collect();
+    return res;
+}
+
+void load_table(Engine &E, const char *name, int ncols, const int32_t *const *cols, uint64_t nrows, int on_device)
+{
+    if (!name) throw Error(SDB_ERR_INVALID, "table name is NULL");
+    auto it = table_column_numbers().find(base_name(name));
+    if (it == table_column_numbers().end()) throw Error(SDB_ERR_INVALID, std::string("unknown table ") + name);
+    if (ncols != it->second)
+        throw Error(SDB_ERR_INVALID, std::string("table ") + name + " has " + std::to_string(it->second) + " columns");
+    if (!cols) throw Error(SDB_ERR_INVALID, "cols is NULL");
+    if (nrows == 0) throw Error(SDB_ERR_INVALID, "empty table");
+    auto old = E.tables.find(name);
+    std::vector<int32_t *> reuse;
+    if (old != E.tables.end()) {
+        SDB_CUDA(cudaStreamSynchronize(E.stream));
+        if (old->second->nrows == nrows) reuse = old->second->owned;
+        else
+            for (auto p : old->second->owned) cudaFree(p);
+        E.tables.erase(old);
+    }
+    auto t = std::make_unique<Table>();
+    t->name = name;
+    t->nrows = nrows;
+    t->columns.resize(ncols);
+    auto sg = split_rows(nrows, E.seg);
+    std::vector<std::pair<int, int32_t *>> dev_cols;
+    size_t reuse_i = 0;
+    for (int c = 0; c < ncols; c++) {
+        if (!cols[c]) continue;
+        int32_t *d;
+        if (on_device) {
+            d = const_cast<int32_t *>(cols[c]);
+        } else {
+            if (reuse_i < reuse.size()) {
+                d = reuse[reuse_i++];
+            } else {
+                SDB_CUDA(cudaMalloc(&d, nrows * sizeof(int32_t)));
+            }
+            t->owned.push_back(d);
+            SDB_CUDA(cudaMemcpyAsync(d, cols[c], nrows * sizeof(int32_t), cudaMemcpyHostToDevice, E.stream));
+        }
+        dev_cols.emplace_back(c, d);
+    }
+    for (; reuse_i < reuse.size(); reuse_i++) cudaFree(reuse[reuse_i]);
+    // Segment statistics (models/models.hpp:71-77), computed on the device.
+    int32_t *mm = nullptr;
+    const size_t nmm = dev_cols.size() * sg.size() * 2;
+    SDB_CUDA(cudaMalloc(&mm, std::max<size_t>(nmm, 2) * sizeof(int32_t)));
+    size_t q = 0;
+    for (auto &dc : dev_cols)
+        for (auto [start, cnt] : sg) {
+            int st = sdb_min_max_i32(dc.second + start, cnt, mm + 2 * q, (sdb_stream_t)E.stream);
+            if (st != SDB_OK) {
+                cudaFree(mm);
+                check(st);
+            }
+            q++;
+        }
+    std::vector<int32_t> host(nmm);
+    cudaError_t e1 = cudaMemcpyAsync(host.data(), mm, nmm * sizeof(int32_t), cudaMemcpyDeviceToHost, E.stream);
+    cudaError_t e2 = cudaStreamSynchronize(E.stream);
+    cudaFree(mm);
+    if (e1 != cudaSuccess || e2 != cudaSuccess)
+        throw Error(SDB_ERR_CUDA, std::string("load_table: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    q = 0;
+    for (auto &dc : dev_cols) {
+        Column &col = t->columns[dc.first];
+        for (auto [start, cnt] : sg) {
+            Segment s;
+            s.data = dc.second + start;
+            s.nrows = cnt;
+            s.min = host[2 * q];
+            s.max = host[2 * q + 1];
+            col.segments.push_back(s);
+            q++;
+        }
+    }
+    E.tables[name] = std::move(t);
+}
+
+template <class F>
+int guarded(F f)
+{
+    try {
+        f();
+        return SDB_OK;
+    } catch (const Error &e) {
+        return sdb_set_error(e.status, "%s", e.what());
+    } catch (const std::bad_alloc &) {
+        return sdb_set_error(SDB_ERR_NOMEM, "host allocation failed");
+    } catch (const std::exception &e) {
+        return sdb_set_error(SDB_ERR_INVALID, "%s", e.what());
+    }
+}
+
+}  // namespace sdb
+
+// ====================================================================== C ABI
+extern "C" {
+
+int sdb_plan_check(const char *plan_json, int *n_rels, int *order, int order_cap)
+{
+    if (!plan_json) return sdb_set_error(SDB_ERR_INVALID, "sdb_plan_check: NULL plan");
+    return sdb::guarded([&] {
+        sdb::PlanResult p = sdb::plan_from_json(plan_json);
+        sdb::ExecutionInfo info = sdb::parse_execution_info(p);
+        if (n_rels) *n_rels = (int)p.rels.size();
+        if (order)
+            for (size_t i = 0; i < info.dag_order.size() && (int)i < order_cap; i++) order[i] = info.dag_order[i];
+    });
+}
+
+int sdb_engine_create(const sdb_engine_config *cfg, sdb_engine **out)
+{
+    if (!out) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_create: out is NULL");
+    *out = nullptr;
+    auto eng = std::make_unique<sdb_engine>();
+    int st = sdb::guarded([&] {
+        sdb::Engine &E = eng->E;
+        if (cfg) E.cfg = *cfg;
+        if (E.cfg.segment_rows) {
+            if (E.cfg.segment_rows % 256 != 0) throw sdb::Error(SDB_ERR_INVALID, "segment_rows must be a multiple of 256");
+            E.seg = E.cfg.segment_rows;
+        }
+        if (E.cfg.stream) {
+            E.stream = (cudaStream_t)E.cfg.stream;
+        } else {
+            SDB_CUDA(cudaStreamCreateWithFlags(&E.stream, cudaStreamNonBlocking));
+            E.own_stream = true;
+        }
+        uint64_t budget = E.cfg.arena_bytes;
+        if (budget == 0) {
+            // runtime/runtime.cpp:278-285: min(max(8 GB, mem/2), 10.5 GB)
+            size_t fr = 0, tot = 0;
+            SDB_CUDA(cudaMemGetInfo(&fr, &tot));
+            budget = std::min<uint64_t>(std::max<uint64_t>(8ull << 30, tot / 2), (10ull << 30) + (512ull << 20));
+        }
+        E.mm.init(budget, E.stream);
+        E.prof.on = E.cfg.profile != 0;
+        SDB_CUDA(cudaEventCreate(&E.plan_a));
+        SDB_CUDA(cudaEventCreate(&E.plan_b));
+        SDB_CUDA(cudaStreamSynchronize(E.stream));
+    });
+    if (st == SDB_OK) *out = eng.release();
+    return st;
+}
+
+int sdb_engine_destroy(sdb_engine *eng)
+{
+    if (!eng) return SDB_OK;
+    sdb::Engine &E = eng->E;
+    cudaStreamSynchronize(E.stream);
+    for (auto &t : E.tables)
+        for (auto p : t.second->owned) cudaFree(p);
+    E.tables.clear();
+    E.mm.release();
+    if (E.plan_a) cudaEventDestroy(E.plan_a);
+    if (E.plan_b) cudaEventDestroy(E.plan_b);
+    if (E.own_stream) cudaStreamDestroy(E.stream);
+    delete eng;
+    return SDB_OK;
+}
+
+int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const int32_t *const *cols, uint64_t nrows,
+                          int on_device)
+{
+    if (!eng) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_load_table: engine is NULL");
+    return sdb::guarded([&] { sdb::load_table(eng->E, name, ncols, cols, nrows, on_device); });
+}
+
+int sdb_engine_execute(sdb_engine *eng, const char *plan_json, sdb_result **out)
+{
+    if (!eng || !plan_json || !out) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_execute: NULL argument");
+    *out = nullptr;
+    return sdb::guarded([&] {
+        auto r = sdb::execute_plan(eng->E, plan_json);
+        *out = r.release();
+    });
+}
+
+int sdb_result_shape(const sdb_result *r, int *ncols, uint64_t *nrows)
+{
+    if (!r) return sdb_set_error(SDB_ERR_INVALID, "sdb_result_shape: NULL result");
+    if (ncols) *ncols = (int)r->types.size();
+    if (nrows) *nrows = r->nrows;
+    return SDB_OK;
+}
+
+int sdb_result_column(const sdb_result *r, int c, int *type, const void **data)
+{
+    if (!r || c < 0 || (size_t)c >= r->types.size()) return sdb_set_error(SDB_ERR_INVALID, "sdb_result_column: bad column");
+    if (type) *type = r->types[c];
+    if (data) *data = r->types[c] == 1 ? (const void *)r->u64[c].data() : (const void *)r->i32[c].data();
+    return SDB_OK;
+}
+
+int sdb_result_write_res(const sdb_result *r, const char *path)
+{
+    if (!r || !path) return sdb_set_error(SDB_ERR_INVALID, "sdb_result_write_res: NULL argument");
+    std::ofstream f(path);
+    if (!f.is_open()) return sdb_set_error(SDB_ERR_INVALID, "Could not open result file for writing: %s", path);
+    for (uint64_t row = 0; row < r->nrows; row++) {
+        for (size_t c = 0; c < r->types.size(); c++) {
+            if (c) f << ' ';
+            if (r->types[c] == 1)
+                f << r->u64[c][row];
+            else
+                f << r->i32[c][row];
+        }
+        f << '\n';
+    }
+    return f.good() ? SDB_OK : sdb_set_error(SDB_ERR_INVALID, "write failed: %s", path);
+}
+
+void sdb_result_free(sdb_result *r) { delete r; }
+
+int sdb_engine_kernel_stats(const sdb_engine *eng, int k, const char **name, uint64_t *launches, double *total_ms)
+{
+    if (!eng) return 0;
+    const auto &st = eng->E.prof.stats;
+    if (k < 0 || (size_t)k >= st.size()) return (int)st.size();
+    auto it = st.begin();
+    std::advance(it, k);
+    if (name) *name = it->first.c_str();
+    if (launches) *launches = it->second.first;
+    if (total_ms) *total_ms = it->second.second;
+    return (int)st.size();
+}
+
+int sdb_engine_last_plan_ms(const sdb_engine *eng, double *ms)
+{
+    if (!eng || !ms) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_last_plan_ms: NULL argument");
+    *ms = eng->E.last_plan_ms;
+    return SDB_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,158 @@
+"""Python front end of the host executor (``sdb_engine_*`` in the C ABI).
+
+``Engine`` owns one native engine: base tables are registered with
+``load_table`` (numpy arrays = host memory, copied to the device; torch CUDA
+tensors = device memory, used in place) and plans in the Thrift PlanResult
+JSON shape run with ``execute``, which returns the result rows as numpy
+columns (int32 keys, uint64 sums), in row order.
+"""
+from __future__ import annotations
+
+import ctypes
+import json
+from typing import Dict, List, Mapping, Optional
+
+import numpy as np
+
+from . import capi
+
+TABLE_COLUMN_NUMBERS = {"lineorder": 17, "part": 9, "supplier": 7, "customer": 8, "ddate": 17}
+
+
+def _ptr_and_loc(a):
+    """(pointer, on_device, nrows) of a numpy array or torch tensor."""
+    if isinstance(a, np.ndarray):
+        if a.dtype != np.int32 or not a.flags["C_CONTIGUOUS"]:
+            raise TypeError("host columns must be contiguous int32 numpy arrays")
+        return a.ctypes.data, 0, a.size
+    try:
+        import torch
+    except ImportError:  # pragma: no cover
+        torch = None
+    if torch is not None and isinstance(a, torch.Tensor):
+        if a.dtype != torch.int32 or not a.is_contiguous():
+            raise TypeError("columns must be contiguous int32 tensors")
+        return a.data_ptr(), 1 if a.is_cuda else 0, a.numel()
+    raise TypeError("unsupported column type %r" % type(a))
+
+
+class Result:
+    """Result rows: ``columns`` is a list of numpy arrays (int32 or uint64)."""
+
+    def __init__(self, columns: List[np.ndarray]):
+        self.columns = columns
+
+    @property
+    def nrows(self) -> int:
+        return int(self.columns[0].size) if self.columns else 0
+
+    def rows(self):
+        return list(zip(*[c.tolist() for c in self.columns])) if self.columns else []
+
+    def canonical(self):
+        r = self.rows()
+        r.sort()
+        return r
+
+
+class Engine:
+    def __init__(self, arena_bytes: int = 0, segment_rows: int = 0, fuse: bool = True, profile: bool = False,
+                 stream: Optional[int] = None):
+        L = capi.lib()
+        cfg = capi.EngineConfig(arena_bytes, segment_rows, 1 if fuse else 0, 1 if profile else 0, stream or None)
+        h = ctypes.c_void_p()
+        capi.check(L.sdb_engine_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._keep: Dict[str, list] = {}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().sdb_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def load_table(self, name: str, columns: Mapping[int, object]):
+        """Registers base table ``name``; ``columns`` maps column index to an
+        int32 array (all host or all device)."""
+        ncols = TABLE_COLUMN_NUMBERS[name.split("@", 1)[0]]
+        ptrs = (ctypes.c_void_p * ncols)()
+        loc = None
+        nrows = None
+        keep = []
+        for c, a in columns.items():
+            if not 0 <= c < ncols:
+                raise ValueError("column %d out of range for %s" % (c, name))
+            p, on_dev, n = _ptr_and_loc(a)
+            if loc is None:
+                loc, nrows = on_dev, n
+            if on_dev != loc:
+                raise ValueError("all columns of a table must be on the same side (host or device)")
+            if n != nrows:
+                raise ValueError("column length mismatch in %s%d" % (name, c))
+            ptrs[c] = p
+            keep.append(a)
+        capi.check(capi.lib().sdb_engine_load_table(self._h, name.encode(), ncols, ptrs, nrows or 0, loc or 0))
+        if loc:
+            self._keep[name] = keep  # device columns are used in place
+        else:
+            self._keep.pop(name, None)
+
+    def execute(self, plan) -> Result:
+        text = plan if isinstance(plan, str) else json.dumps(plan)
+        L = capi.lib()
+        r = ctypes.c_void_p()
+        capi.check(L.sdb_engine_execute(self._h, text.encode(), ctypes.byref(r)))
+        try:
+            ncols, nrows = ctypes.c_int(), ctypes.c_uint64()
+            L.sdb_result_shape(r, ctypes.byref(ncols), ctypes.byref(nrows))
+            cols = []
+            for c in range(ncols.value):
+                t, d = ctypes.c_int(), ctypes.c_void_p()
+                capi.check(L.sdb_result_column(r, c, ctypes.byref(t), ctypes.byref(d)))
+                dt = np.uint64 if t.value == 1 else np.int32
+                n = nrows.value
+                if n == 0:
+                    cols.append(np.empty(0, dtype=dt))
+                else:
+                    buf = (ctypes.c_char * (n * np.dtype(dt).itemsize)).from_address(d.value)
+                    cols.append(np.frombuffer(buf, dtype=dt).copy())
+            return Result(cols)
+        finally:
+            L.sdb_result_free(r)
+
+    def execute_to_res(self, plan, path: str):
+        """Runs ``plan`` and writes the rows as the reference's ``.res`` file."""
+        text = plan if isinstance(plan, str) else json.dumps(plan)
+        L = capi.lib()
+        r = ctypes.c_void_p()
+        capi.check(L.sdb_engine_execute(self._h, text.encode(), ctypes.byref(r)))
+        try:
+            capi.check(L.sdb_result_write_res(r, path.encode()))
+        finally:
+            L.sdb_result_free(r)
+
+    def last_plan_ms(self) -> float:
+        v = ctypes.c_double()
+        capi.check(capi.lib().sdb_engine_last_plan_ms(self._h, ctypes.byref(v)))
+        return v.value
+
+    def kernel_stats(self) -> Dict[str, tuple]:
+        L = capi.lib()
+        n = L.sdb_engine_kernel_stats(self._h, -1, None, None, None)
+        out = {}
+        for k in range(n):
+            name, cnt, ms = ctypes.c_char_p(), ctypes.c_uint64(), ctypes.c_double()
+            L.sdb_engine_kernel_stats(self._h, k, ctypes.byref(name), ctypes.byref(cnt), ctypes.byref(ms))
+            out[name.value.decode()] = (cnt.value, ms.value)
+        return out

@@ -1,0 +1,144 @@
+"""The C-ABI library without a GPU: it loads, exports every entry point that
+include/sycldb_gpu.h declares, its struct layouts match the bindings, its host
+paths (generator, plan ingestion, argument checks) behave."""
+import ctypes
+import json
+import os
+import re
+
+import numpy as np
+import pytest
+
+from sycldb_gb300 import capi, plans, ssb
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "sycldb_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sdb_\w+)\s*\(", text)))
+
+
+def test_header_declares_the_kernel_entries():
+    names = declared_functions()
+    for k in ["sdb_fill_u8", "sdb_select_lit", "sdb_select_cols", "sdb_logical", "sdb_fill_i32", "sdb_binop_cc",
+              "sdb_binop_lc", "sdb_binop_cl", "sdb_sum_i32_u64", "sdb_groupby_sum", "sdb_occ_to_flags",
+              "sdb_ht_build_keys", "sdb_probe_semi", "sdb_ht_build_kv", "sdb_probe_full", "sdb_compact_row_ids",
+              "sdb_gather_i32", "sdb_count_flags", "sdb_fused_chain", "sdb_engine_execute", "sdb_last_error"]:
+        assert k in names
+
+
+def test_library_exports_every_declared_symbol():
+    L = capi.lib()
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+    # and the bindings cover every declaration
+    assert set(declared_functions()) <= set(capi.exported_symbols())
+
+
+def test_abi_struct_sizes():
+    L = capi.lib()  # lib() itself raises on a mismatch
+    assert L.sdb_abi_sizeof(b"sdb_chain_desc") == ctypes.sizeof(capi.ChainDesc)
+    assert L.sdb_abi_sizeof(b"nope") == 0
+    assert L.sdb_version().startswith(b"sycldb-gb300")
+
+
+def test_generator_is_deterministic_and_in_range():
+    L = capi.lib()
+    a = np.empty(100_003, np.int32)
+    b = np.empty(100_003, np.int32)
+    capi.check(L.sdb_gen_uniform_cpu(a.ctypes.data, a.size, 0, 7, 3, 90_000, 10_494_950))
+    capi.check(L.sdb_gen_uniform_cpu(b.ctypes.data, 50, 100_003 - 50, 7, 3, 90_000, 10_494_950))
+    assert np.array_equal(a[-50:], b[:50])  # any row range gives the same values
+    assert a.min() >= 90_000 and a.max() <= 10_494_950
+    assert L.sdb_gen_uniform_host(7, 3, 12345, 90_000, 10_494_950) == a[12345]
+    # roughly uniform
+    assert abs(a.mean() - (90_000 + 10_494_950) / 2) < 0.01 * 10_494_950
+
+
+def test_dates_cover_the_calendar():
+    d = ssb.gen_ddate()
+    assert d[0][0] == 19920101 and d[0][-1] == 19981230 and d[0].size == 2556
+    assert d[4].min() == 1992 and d[4].max() == 1998
+    assert d[10].min() == 1 and d[10].max() == 12 and d[11].max() == 53
+    f = ssb.gen_lineorder_host(200_000, [5], 1.0)[5]
+    assert set(np.unique(f)) <= set(d[0].tolist())
+
+
+def test_plan_check_orders_and_rejects():
+    L = capi.lib()
+    p = json.dumps(plans.plan_star(1, 1))
+    n = ctypes.c_int()
+    order = (ctypes.c_int * 32)()
+    capi.check(L.sdb_plan_check(p.encode(), ctypes.byref(n), order, 32))
+    assert n.value == 12
+    assert list(order[:n.value]) == [1, 4, 7, 2, 5, 0, 3, 6, 8, 9, 10, 11]
+    for bad in ['{"rels": [', '{"nope": []}', '{"rels": [{"id": 0, "relOp": "SCAN"}]}',
+                '{"rels": [{"id": 0, "relOp": "TABLE_SCAN", "tables": ["ssb", "nosuch"]}]}',
+                '{"rels": [{"id": 1, "relOp": "TABLE_SCAN", "tables": ["ssb", "part"]}]}']:
+        assert L.sdb_plan_check(bad.encode(), None, None, 0) == capi.SDB_ERR_INVALID
+        assert capi.last_error()
+
+
+def test_plan_check_numeric_enums():
+    """Enums may be given by IDL number (TABLE_SCAN=0, FILTER=1, ..., COLUMN=1)."""
+    p = {"rels": [{"id": 0, "relOp": 0, "tables": ["ssb", "lineorder"]},
+                  {"id": 1, "relOp": 1, "condition": {"exprType": 2, "op": "<", "operands": [
+                      {"exprType": 1, "input": 8}, {"exprType": 0, "literal": {"literalOption": 0, "value": 25}}]}},
+                  {"id": 2, "relOp": 4, "group": [], "aggs": [{"agg": "SUM", "operands": [9]}]}]}
+    n = ctypes.c_int()
+    capi.check(capi.lib().sdb_plan_check(json.dumps(p).encode(), ctypes.byref(n), None, 0))
+    assert n.value == 3
+
+
+def test_argument_errors_need_no_device():
+    L = capi.lib()
+    assert L.sdb_fused_chain(None, None) == capi.SDB_ERR_INVALID
+    d = capi.ChainDesc()
+    d.n_ops = capi.CHAIN_MAX_OPS + 1
+    assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID
+    d.n_ops = 1
+    d.ops[0].kind = 99
+    assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID
+    assert "unknown op" in capi.last_error()
+    d.ops[0].kind = capi.OP_FULL_PROBE
+    d.ops[0].a.kind = capi.SRC_LIT
+    d.ops[0].ht = None
+    assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID
+    assert L.sdb_groupby_sum(None, None, None, 0, None, None, 10, 5, None, None, None, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_select_lit(None, 1, 0, 0, None, None, 10, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_binop_cc(None, None, None, 9, None, 10, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_compact_row_ids(None, 10, None, None, None, 0, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_gen_uniform_cpu(None, 0, 0, 1, 1, 5, 4) == capi.SDB_ERR_INVALID
+    assert L.sdb_compact_scratch_bytes(0) == 0
+    assert L.sdb_compact_scratch_bytes(1) == 256
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    monkeypatch.setattr(capi, "_LIB", None)
+    monkeypatch.setattr(capi, "LIB_PATH", str(tmp_path / "absent.so"))
+    with pytest.raises(RuntimeError, match="not built"):
+        capi.lib()
+
+
+def test_misaligned_typed_pointers_are_rejected_on_the_host():
+    """A typed device access at a misaligned address would fault the GPU, so
+    the entry points refuse such pointers before launching anything."""
+    L = capi.lib()
+    odd = 0x1001  # never dereferenced: the check comes first
+    assert L.sdb_select_lit(odd, 1, 0, 0, 0x2000, 0x3000, 10, None) == capi.SDB_ERR_INVALID
+    assert "aligned" in capi.last_error()
+    assert L.sdb_sum_i32_u64(0x2000, 0x3000, 10, 0x4004, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_probe_full(0x2000, 0x3002, 0x1, 0x2, 10, 0x4000, 0, 5, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_gather_u64(0x2004, 0x3000, 0x4000, 0x5000, 10, None) == capi.SDB_ERR_INVALID
+    d = capi.ChainDesc()
+    d.n = 10
+    d.n_ops = 1
+    d.ops[0].kind = capi.OP_SELECT
+    d.ops[0].a.kind = capi.SRC_COL
+    d.ops[0].a.col = odd
+    d.ops[0].b.kind = capi.SRC_LIT
+    d.terminal = capi.TERM_FLAGS
+    d.flags_out = 0x2000
+    assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID

@@ -1,0 +1,132 @@
+"""The host executor on the GPU: plans of the benchmark shapes against the
+committed golden results and the oracle, operator-at-a-time and fused, with
+one and several segments; the SF20 star join at full size."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from sycldb_gb300 import capi, plans, ssb
+from sycldb_gb300.engine import Engine
+from tests import datasets, naive
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+PLANS = json.load(open(os.path.join(HERE, "plans.json")))
+
+
+def load(eng, ds, device=False):
+    import torch
+
+    for name, cols in ds.items():
+        if device:
+            eng.load_table(name, {c: torch.from_numpy(a).cuda() for c, a in cols.items()})
+        else:
+            eng.load_table(name, cols)
+
+
+@pytest.mark.parametrize("fuse", [False, True])
+@pytest.mark.parametrize("seg", [0, 4096])
+@pytest.mark.parametrize("case", PLANS, ids=[c["name"] for c in PLANS])
+def test_plan_matches_golden(case, fuse, seg):
+    ds = datasets.dataset(case["sf"], case["seed"])
+    with Engine(arena_bytes=1 << 30, segment_rows=seg, fuse=fuse) as eng:
+        load(eng, ds, device=bool(seg))
+        got = eng.execute(case["plan"]).canonical()
+    assert [list(r) for r in got] == case["rows"]
+
+
+@pytest.mark.parametrize("fuse", [False, True])
+def test_quirk_plans_match_oracle(fuse):
+    """Filters with OR / parent-op quirk, SEARCH points, column-column
+    comparisons, literal projections, every binary operator."""
+    ds = datasets.dataset(0.01)
+    P = plans
+    cases = []
+    b = P.PlanBuilder()
+    b.scan("lineorder")
+    b.filter(P.AND(P.expr("<=", P.col(8), P.lit(30)),
+                   P.OR(P.search_points(11, 2, 7), P.expr(">", P.col(9), P.col(12)))))
+    b.project([P.expr("-", P.col(9), P.col(13)), P.lit(3)])
+    b.aggregate([], 0)
+    cases.append(b.plan())
+    for op in ["*", "/", "+", "-"]:
+        b = P.PlanBuilder()
+        b.scan("lineorder")
+        b.filter(P.expr("<>", P.col(11), P.lit(0)))
+        b.project([P.col(8), P.expr(op, P.col(9), P.col(11)), P.expr(op, P.lit(1000), P.col(11))])
+        b.aggregate([0], 1)
+        cases.append(b.plan())
+        b = P.PlanBuilder()
+        b.scan("lineorder")
+        b.project([P.col(11), P.expr(op, P.col(12), P.lit(7))])
+        b.aggregate([0], 1)
+        cases.append(b.plan())
+    b = P.PlanBuilder()  # a plan that ends in a filter (no aggregate)
+    b.scan("lineorder")
+    b.filter(P.AND(P.expr("==", P.col(11), P.lit(10)), P.expr("<", P.col(8), P.lit(3))))
+    b.project([P.col(5), P.col(9)])
+    cases.append(b.plan())
+    with Engine(arena_bytes=1 << 30, segment_rows=8192, fuse=fuse) as eng:
+        load(eng, ds)
+        for plan in cases:
+            assert eng.execute(plan).canonical() == datasets.oracle_run(ds, plan, 8192), json.dumps(plan)
+
+
+def test_res_writer(tmp_path):
+    ds = datasets.dataset(0.01)
+    with Engine(arena_bytes=1 << 30) as eng:
+        load(eng, ds)
+        plan = plans.plan_date_join(1994)
+        p = str(tmp_path / "q.res")
+        eng.execute_to_res(plan, p)
+        rows = [tuple(int(x) for x in line.split()) for line in open(p).read().splitlines()]
+    assert sorted(rows) == datasets.oracle_run(ds, plan)
+
+
+def test_errors_are_statuses_not_crashes():
+    ds = datasets.dataset(0.01)
+    with Engine(arena_bytes=1 << 28) as eng:
+        load(eng, ds)
+        with pytest.raises(capi.SdbError) as e:
+            eng.execute('{"rels": [{"id": 0, "relOp": "TABLE_SCAN", "tables": ["ssb", "customerz"]}]}')
+        assert e.value.status == capi.SDB_ERR_INVALID
+        bad = plans.plan_star(1, 1)
+        bad["rels"][3]["condition"]["operands"][1]["input"] = 999
+        with pytest.raises(capi.SdbError):
+            eng.execute(bad)
+        # the engine stays usable
+        assert eng.execute(plans.plan_filter_sum(1993)).canonical() == datasets.oracle_run(ds, plans.plan_filter_sum(1993))
+    with Engine(arena_bytes=1 << 16) as small:  # budget exceeded -> SDB_ERR_NOMEM
+        small.load_table("lineorder", ds["lineorder"])
+        with pytest.raises(capi.SdbError) as e:
+            small.execute(plans.plan_filter_sum(1993))
+        assert e.value.status == capi.SDB_ERR_NOMEM
+
+
+def test_star_sf20_full_size():
+    """The benchmark configuration at full size (120 M fact rows): fused and
+    operator-at-a-time results agree and equal the naive evaluator's."""
+    import torch
+
+    sf = 20.0
+    n = ssb.fact_rows(sf)
+    fact = ssb.gen_lineorder_device(n, ssb.QUERY_COLUMNS["star"], sf)
+    dims = ssb.gen_dims(sf)
+    plan = plans.plan_star(2, 11)
+    res = {}
+    for fuse in (True, False):
+        with Engine(fuse=fuse) as eng:
+            eng.load_table("lineorder", fact)
+            for t in ("supplier", "part", "ddate"):
+                eng.load_table(t, dims[t])
+            res[fuse] = eng.execute(plan).canonical()
+    assert res[True] == res[False]
+    host_fact = {c: t.cpu().numpy() for c, t in fact.items()}
+    want = naive.star(host_fact, dims["supplier"], dims["part"], dims["ddate"], 2, 11)
+    assert res[True] == want
+    assert 200 <= len(want) <= 280
+    del fact
+    torch.cuda.empty_cache()

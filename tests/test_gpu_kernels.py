@@ -1,0 +1,235 @@
+"""Operator kernels (K1-K16) through the C ABI on the GPU, against the golden
+vectors of the reference functors and against the oracle."""
+import ctypes
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from sycldb_gb300 import capi
+from tests import kernel_cases as kc
+from tests.gpu_util import dev, host, stream, zeros
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+CASES = json.load(open(os.path.join(HERE, "kernels.json")))
+ARR = np.load(os.path.join(HERE, "kernels.npz"))
+
+
+def L():
+    return capi.lib()
+
+
+def inp(case, k):
+    return ARR["%s/in/%s" % (case["name"], k)].copy()
+
+
+def run_gpu(case, pad=0):
+    """The C-ABI kernel of a golden case; pad=1 offsets every device pointer
+    off the 16-byte boundary (keeping each type's natural alignment)."""
+    k, p = case["kernel"], case["params"]
+    s = stream()
+    keep = []
+
+    def D(a):
+        # misaligned for the vector paths, naturally aligned for the type
+        off = {1: 3, 4: 4, 8: 8}[a.dtype.itemsize] if pad else 0
+        b, q = dev(a, off)
+        keep.append(b)
+        return b, q
+
+    if k in ("select_lit", "select_cols"):
+        n = inp(case, "in").size
+        _, fin = D(inp(case, "in"))
+        ob, out = D(np.zeros(n, np.uint8))
+        if k == "select_lit":
+            _, col = D(inp(case, "col"))
+            capi.check(L().sdb_select_lit(col, p["v"], p["cmp"], p["logic"], fin, out, n, s))
+        else:
+            _, a = D(inp(case, "a"))
+            _, b = D(inp(case, "b"))
+            capi.check(L().sdb_select_cols(a, b, p["cmp"], p["logic"], fin, out, n, s))
+        return {"out": host(ob, out, n, np.uint8)}
+    if k == "logical":
+        n = inp(case, "in").size
+        _, fin = D(inp(case, "in"))
+        _, loc = D(inp(case, "local"))
+        ob, out = D(np.zeros(n, np.uint8))
+        capi.check(L().sdb_logical(p["logic"], fin, loc, out, n, s))
+        return {"out": host(ob, out, n, np.uint8)}
+    if k == "fill_i32":
+        n = ARR["%s/out/out" % case["name"]].size
+        ob, out = D(np.zeros(n, np.int32))
+        capi.check(L().sdb_fill_i32(out, p["v"], n, s))
+        return {"out": host(ob, out, n, np.int32)}
+    if k.startswith("binop_"):
+        mode = k.split("_")[1]
+        res0 = inp(case, "res0")
+        n = res0.size
+        rb, res = D(res0)
+        _, a = D(inp(case, "a"))
+        _, b = D(inp(case, "b"))
+        _, fl = D(inp(case, "flags"))
+        if mode == "cc":
+            capi.check(L().sdb_binop_cc(res, a, b, p["op"], fl, n, s))
+        elif mode == "lc":
+            capi.check(L().sdb_binop_lc(res, p["la"], b, p["op"], fl, n, s))
+        else:
+            capi.check(L().sdb_binop_cl(res, a, p["lb"], p["op"], fl, n, s))
+        return {"res": host(rb, res, n, np.int32)}
+    if k == "sum":
+        col = inp(case, "col")
+        _, c = D(col)
+        _, fl = D(inp(case, "flags"))
+        ab, acc = D(np.array([p["acc0"]], np.uint64))
+        capi.check(L().sdb_sum_i32_u64(c, fl, col.size, acc, s))
+        return {"acc": host(ab, acc, 1, np.uint64)}
+    if k == "groupby":
+        g, P = p["g"], p["P"]
+        val = inp(case, "val")
+        n = val.size
+        keys = [D(inp(case, "key%d" % j))[1] for j in range(g)]
+        okb = [D(np.zeros(P, np.int32)) for _ in range(g)]
+        sb, sm = D(np.zeros(P, np.uint64))
+        cb, oc = D(np.zeros(P, np.uint32))
+        _, v = D(val)
+        _, fl = D(inp(case, "flags"))
+        mins = (ctypes.c_int32 * g)(*inp(case, "mins").tolist())
+        maxs = (ctypes.c_int32 * g)(*inp(case, "maxs").tolist())
+        kp = (ctypes.c_void_p * g)(*keys)
+        op = (ctypes.c_void_p * g)(*[q for _, q in okb])
+        capi.check(L().sdb_groupby_sum(kp, mins, maxs, g, v, fl, n, P, op, sm, oc, s))
+        occ = host(cb, oc, P, np.uint32) != 0
+        out = {"sum": host(sb, sm, P, np.uint64), "occ": occ.astype(np.uint8)}
+        for j in range(g):
+            out["okey%d" % j] = np.where(occ, host(okb[j][0], okb[j][1], P, np.int32), 0).astype(np.int32)
+        return out
+    if k in ("semi", "full"):
+        keys = inp(case, "keys")
+        nb = keys.size
+        probe = inp(case, "probe")
+        m = probe.size
+        _, kk = D(keys)
+        _, bf = D(inp(case, "bflags"))
+        _, pr = D(probe)
+        _, fin = D(inp(case, "in"))
+        ob, out = D(np.zeros(m, np.uint8))
+        lo, hi = p["lo"], p["lo"] + p["len"] - 1
+        if k == "semi":
+            hb, ht = D(np.zeros(nb, np.uint8))
+            capi.check(L().sdb_ht_build_keys(kk, bf, nb, ht, lo, p["len"], s))
+            capi.check(L().sdb_probe_semi(pr, fin, out, m, ht, lo, hi, s))
+            return {"ht": host(hb, ht, nb, np.uint8), "out": host(ob, out, m, np.uint8)}
+        hb, ht = D(np.zeros(2 * nb, np.int32))
+        _, vv = D(inp(case, "vals"))
+        vb, vo = D(np.full(m, -7, np.int32))
+        capi.check(L().sdb_ht_build_kv(kk, vv, bf, nb, ht, lo, p["len"], s))
+        capi.check(L().sdb_probe_full(pr, vo, fin, out, m, ht, lo, hi, s))
+        return {"ht2": host(hb, ht, 2 * nb, np.int32), "out": host(ob, out, m, np.uint8),
+                "val_out": host(vb, vo, m, np.int32)}
+    if k == "count":
+        f = inp(case, "flags")
+        _, fl = D(f)
+        cb, c = D(np.zeros(1, np.uint64))
+        capi.check(L().sdb_count_flags(fl, f.size, c, s))
+        return {"count": host(cb, c, 1, np.uint64)}
+    raise KeyError(k)
+
+
+@pytest.mark.parametrize("pad", [0, 1])
+@pytest.mark.parametrize("case", CASES, ids=[c["name"] for c in CASES])
+def test_kernel_matches_reference_golden(case, pad):
+    got = run_gpu(case, pad)
+    for k in case["outputs"]:
+        want = ARR["%s/out/%s" % (case["name"], k)]
+        assert np.array_equal(got[k], want), (case["name"], k, pad)
+
+
+@pytest.mark.parametrize("n", [0] + kc.SIZES + [1 << 20, (1 << 20) + 5])
+def test_select_and_sum_vs_oracle(n):
+    rng = np.random.default_rng(n + 99)
+    col = kc.col_small(rng, n, -50, 50)
+    fin = kc.flags(rng, n, 0.6, canonical=False)
+    want = np.empty(n, np.uint8)
+    O.select_lit(col, 3, O.GT, O.AND, fin, want)
+    cb, c = dev(col)
+    fb, f = dev(fin)
+    ob, o = zeros(n, np.uint8)
+    capi.check(capi.lib().sdb_select_lit(c, 3, O.GT, O.AND, f, o, n, stream()))
+    assert np.array_equal(host(ob, o, n, np.uint8), want)
+    acc = np.zeros(1, np.uint64)
+    O.sum_i32_u64(col, fin, acc)
+    ab, a = zeros(1, np.uint64)
+    capi.check(capi.lib().sdb_sum_i32_u64(c, f, n, a, stream()))
+    assert host(ab, a, 1, np.uint64)[0] == acc[0]
+
+
+def test_division_edge_cases_defined():
+    """x/0 -> 0 and INT_MIN/-1 -> INT_MIN (undefined in the reference)."""
+    a = np.array([5, -7, kc.I32_MIN, kc.I32_MIN, 9, 0, 12, -12], np.int32)
+    b = np.array([0, 0, -1, 1, 2, 0, -5, 5], np.int32)
+    fl = np.ones(8, np.uint8)
+    want = np.zeros(8, np.int32)
+    O.binop_cc(want, a, b, O.DIV, fl)
+    assert want.tolist() == [0, 0, kc.I32_MIN, kc.I32_MIN, 4, 0, -2, -2]
+    _, pa = dev(a)
+    _, pb = dev(b)
+    _, pf = dev(fl)
+    rb, r = zeros(8, np.int32)
+    capi.check(capi.lib().sdb_binop_cc(r, pa, pb, O.DIV, pf, 8, stream()))
+    assert np.array_equal(host(rb, r, 8, np.int32), want)
+
+
+def test_out_of_range_slots_are_counted_not_written():
+    L = capi.lib()
+    cnt = ctypes.c_uint64()
+    capi.check(L.sdb_device_errors(ctypes.byref(cnt), stream()))  # clear
+    keys = np.array([1, 2, 9, 3], np.int32)  # 9 is outside [1, 4)
+    fl = np.ones(4, np.uint8)
+    _, k = dev(keys)
+    _, f = dev(fl)
+    hb, ht = zeros(3, np.uint8)
+    capi.check(L.sdb_ht_build_keys(k, f, 4, ht, 1, 3, stream()))
+    assert host(hb, ht, 3, np.uint8).tolist() == [1, 1, 1]
+    capi.check(L.sdb_device_errors(ctypes.byref(cnt), stream()))
+    assert cnt.value == 1
+
+
+@pytest.mark.parametrize("n", [0, 1, 15, 16, 17, 4095, 4096, 4097, 100_000, 3 * 4096 * 257 + 11])
+@pytest.mark.parametrize("p", [0.0, 0.01, 0.5, 1.0])
+def test_compaction_and_gather(n, p):
+    rng = np.random.default_rng(n)
+    fl = kc.flags(rng, n, p, canonical=False)
+    src = rng.integers(-1000, 1000, n).astype(np.int32)
+    want = O.compact_row_ids(fl) if n else np.empty(0, np.int32)
+    L = capi.lib()
+    _, f = dev(fl)
+    ib, ids = zeros(max(n, 1), np.int32)
+    cb, cnt = zeros(1, np.uint32)
+    sbytes = L.sdb_compact_scratch_bytes(n)
+    scb, scr = zeros(max(sbytes, 1), np.uint8)
+    capi.check(L.sdb_compact_row_ids(f, n, ids, cnt, scr, sbytes, stream()))
+    c = int(host(cb, cnt, 1, np.uint32)[0])
+    assert c == want.size
+    assert np.array_equal(host(ib, ids, c, np.int32), want)
+    _, s = dev(src)
+    db, d = zeros(max(n, 1), np.int32)
+    capi.check(L.sdb_gather_i32(s, ids, cnt, d, n, stream()))
+    assert np.array_equal(host(db, d, c, np.int32), src[want])
+
+
+def test_min_max_and_generator_agree_with_host():
+    from sycldb_gb300 import ssb
+
+    L = capi.lib()
+    n = 1_000_003
+    host_cols = ssb.gen_lineorder_host(n, [5, 9], 20.0, row0=17)
+    dev_cols = ssb.gen_lineorder_device(n, [5, 9], 20.0, row0=17)
+    for c in (5, 9):
+        assert np.array_equal(dev_cols[c].cpu().numpy(), host_cols[c])
+        mb, mm = zeros(2, np.int32)
+        capi.check(L.sdb_min_max_i32(dev_cols[c].data_ptr(), n, mm, stream()))
+        assert host(mb, mm, 2, np.int32).tolist() == list(O.min_max(host_cols[c]))
