@@ -37,3 +37,12 @@ def pytest_collection_modifyitems(config, items):
     for it in items:
         if "gpu" in it.keywords:
             it.add_marker(skip)
+
+
+@pytest.fixture(autouse=True)
+def _release_device_buffers(request):
+    yield
+    if "gpu" in request.keywords:
+        from tests import gpu_util
+
+        gpu_util.release()

@@ -12,6 +12,16 @@ def torch():
     return t
 
 
+# Every buffer handed out stays referenced until release(): a raw pointer
+# whose tensor was dropped would be recycled by torch's caching allocator and
+# alias the next buffer.
+_LIVE = []
+
+
+def release():
+    _LIVE.clear()
+
+
 def dev(a: np.ndarray, pad: int = 0):
     """Copies a numpy array to a fresh device buffer (optionally with `pad`
     leading bytes so the data pointer is misaligned); returns (tensor, ptr)."""
@@ -20,6 +30,7 @@ def dev(a: np.ndarray, pad: int = 0):
     buf = t.empty(raw.size + pad + 16, dtype=t.uint8, device="cuda")
     if raw.size:
         buf[pad:pad + raw.size].copy_(t.from_numpy(raw.copy()))
+    _LIVE.append(buf)
     return buf, buf.data_ptr() + pad
 
 

@@ -187,7 +187,9 @@ def test_out_of_range_slots_are_counted_not_written():
     L = capi.lib()
     cnt = ctypes.c_uint64()
     capi.check(L.sdb_device_errors(ctypes.byref(cnt), stream()))  # clear
-    keys = np.array([1, 2, 9, 3], np.int32)  # 9 is outside [1, 4)
+    # HASH = (x - min) % len wraps keys above the range (9 -> slot 2, as in the
+    # reference); a key below min gives a negative slot: -4 -> (-5) % 3 = -2.
+    keys = np.array([1, 2, -4, 3], np.int32)
     fl = np.ones(4, np.uint8)
     _, k = dev(keys)
     _, f = dev(fl)
