@@ -253,8 +253,27 @@ typedef struct sdb_chain_desc {
 } sdb_chain_desc;
 
 /* Launch one fused pass.  The descriptor is read on the host (copied into
- * the launch); its pointers are device pointers. */
+ * the launch); its pointers are device pointers.  The kernel variant comes
+ * from the tuning table (below), else a default. */
 int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream);
+/* Same, forcing a kernel variant.  0, 1, 2: the general pass with 4, 8 or
+ * 16 rows per thread (chains needing more than 2 registers cap it: 4
+ * registers at 8 rows, 8 at 4); each row loads a column only while its flag
+ * can still change, so later columns cost only the sectors that hold live
+ * rows.  3: a shape-specialised pass (straight-line code for the common
+ * chain shapes; every chain column of the next tiles is staged in shared
+ * memory by asynchronous copies while the current tile is probed).  4: as 3,
+ * and after the first op each warp compacts its surviving rows so that the
+ * remaining ops run one row per lane.  Shapes without a specialised pass fall
+ * back to the general pass.  Default (and an unset tuning entry): 4. */
+int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream);
+/* Tuning table used by sdb_fused_chain: variant for chains with this
+ * terminal (sdb_chain_terminal), register count and row count (bucketed by
+ * log2).  variant -1 restores the default.  _get returns the variant used. */
+int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant);
+int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows);
+/* Registers (1..8) a chain needs, or a negative status if it is invalid. */
+int sdb_chain_registers(const sdb_chain_desc *chain);
 
 /* ------------------------------------------------------ synthetic SSB data */
 

@@ -90,6 +90,10 @@ _SIGS = {
     "sdb_count_flags": (c_int, [_P, c_uint64, _P, _P]),
     "sdb_min_max_i32": (c_int, [_P, c_uint64, _P, _P]),
     "sdb_fused_chain": (c_int, [POINTER(ChainDesc), _P]),
+    "sdb_fused_chain_variant": (c_int, [POINTER(ChainDesc), c_int, _P]),
+    "sdb_chain_tune_set": (c_int, [c_int, c_int, c_uint64, c_int]),
+    "sdb_chain_tune_get": (c_int, [c_int, c_int, c_uint64]),
+    "sdb_chain_registers": (c_int, [POINTER(ChainDesc)]),
     "sdb_gen_uniform_host": (c_int32, [c_uint64, c_uint64, c_uint64, c_int32, c_int32]),
     "sdb_gen_uniform": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32, c_int32, _P]),
     "sdb_gen_uniform_cpu": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32, c_int32]),
@@ -145,3 +149,12 @@ def check(status: int):
     if status != SDB_OK:
         raise SdbError(status, last_error())
     return status
+
+
+def force_chain_variant(variant: int):
+    """Sets every tuning-table entry to `variant` (-1 restores the defaults)."""
+    L = lib()
+    for term in range(3):
+        for nregs in (1, 4, 8):
+            for b in range(40):
+                check(L.sdb_chain_tune_set(term, nregs, 1 << b, variant))

@@ -88,7 +88,7 @@ __host__ __device__ __forceinline__ uint64_t widen(int32_t v)
     return (uint64_t)(int64_t)v;
 }
 
-inline bool aligned(const void *p, uintptr_t a)
+__host__ __device__ inline bool aligned(const void *p, uintptr_t a)
 {
     return p == nullptr || (reinterpret_cast<uintptr_t>(p) % a) == 0;
 }

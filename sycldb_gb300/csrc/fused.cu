@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <utility>
 
 #include "common.cuh"
 
@@ -41,7 +42,7 @@ const int g_reader_registered = (sdb_errors_add_reader(&read_errors), 0);
 
 constexpr int kThreads = 256;
 
-enum Term { T_FLAGS = 0, T_SUM = 1, T_GROUP_SMEM = 2, T_GROUP_GLOBAL = 3 };
+enum Term { T_FLAGS = 0, T_SUM = 1, T_GROUP = 2 };
 
 struct ChainLaunch {
     sdb_chain_desc d;
@@ -50,258 +51,310 @@ struct ChainLaunch {
     uint32_t mults[SDB_CHAIN_MAX_KEYS];
 };
 
-template <int NREGS>
-struct Regs {
-    int32_t v[NREGS][4];
+// Block tile: kThreads x ITEMS consecutive rows.  Thread t owns rows
+// tile + t + k * kThreads (k < ITEMS), so each per-item load of a warp is one
+// coalesced 128-byte request, and every op issues the loads of all its items
+// before it consumes any (ITEMS independent loads in flight per thread).  A
+// thread's flags are an ITEMS-bit mask; values the ops produce (join values,
+// projections) stay in registers, NREGS per row.
+template <int NREGS, int ITEMS>
+struct Tile {
+    uint64_t base;       // row of item 0
+    uint32_t valid;      // bit k: row base + k * kThreads exists
+    uint32_t live;       // bit k: that row's flag
+    int32_t reg[NREGS][ITEMS];
 };
 
-template <int NREGS>
-__device__ __forceinline__ void reg_get(const Regs<NREGS> &R, int idx, int32_t (&out)[4])
+template <int NREGS, int ITEMS>
+__device__ __forceinline__ void reg_get(const Tile<NREGS, ITEMS> &T, int idx, int32_t (&out)[ITEMS])
 {
 #pragma unroll
-    for (int j = 0; j < 4; j++) out[j] = R.v[0][j];
+    for (int k = 0; k < ITEMS; k++) out[k] = T.reg[0][k];
 #pragma unroll
     for (int r = 1; r < NREGS; r++)
         if (idx == r) {
 #pragma unroll
-            for (int j = 0; j < 4; j++) out[j] = R.v[r][j];
+            for (int k = 0; k < ITEMS; k++) out[k] = T.reg[r][k];
         }
 }
 
-template <int NREGS>
-__device__ __forceinline__ void reg_set(Regs<NREGS> &R, int idx, const int32_t (&in)[4], uint32_t mask)
+template <int NREGS, int ITEMS>
+__device__ __forceinline__ void reg_set(Tile<NREGS, ITEMS> &T, int idx, const int32_t (&in)[ITEMS], uint32_t mask)
 {
 #pragma unroll
     for (int r = 0; r < NREGS; r++)
         if (idx == r) {
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-                if (mask & (1u << j)) R.v[r][j] = in[j];
+            for (int k = 0; k < ITEMS; k++)
+                if ((mask >> k) & 1u) T.reg[r][k] = in[k];
         }
 }
 
-// Loads operand `o` for the rows of `need` (other rows are left unspecified).
-template <int NREGS>
-__device__ __forceinline__ void fetch(const sdb_operand &o, uint64_t r0, uint32_t need, bool full, bool vec,
-                                      const Regs<NREGS> &R, int32_t (&v)[4])
+__device__ __forceinline__ uint64_t row_of(uint64_t base, int k) { return base + (uint64_t)k * kThreads; }
+
+// Operand values for the items of `need` (other items unspecified).
+template <int NREGS, int ITEMS>
+__device__ __forceinline__ void fetch(const sdb_operand &o, const Tile<NREGS, ITEMS> &T, uint32_t need,
+                                      int32_t (&v)[ITEMS])
 {
     if (o.kind == SDB_SRC_COL) {
-        if (need == 0) return;
-        if (full && vec) {
-            int4 q = __ldcs(reinterpret_cast<const int4 *>(o.col + r0));
-            v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
-        } else {
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-                if (need & (1u << j)) v[j] = __ldcs(o.col + r0 + j);
-        }
+        for (int k = 0; k < ITEMS; k++)
+            if ((need >> k) & 1u) v[k] = __ldcs(o.col + row_of(T.base, k));
     } else if (o.kind == SDB_SRC_REG) {
-        reg_get(R, o.reg, v);
+        reg_get(T, o.reg, v);
     } else {
 #pragma unroll
-        for (int j = 0; j < 4; j++) v[j] = o.lit;
+        for (int k = 0; k < ITEMS; k++) v[k] = o.lit;
     }
 }
 
-__device__ __forceinline__ void store_masked(int32_t *col, uint64_t r0, const int32_t (&v)[4], uint32_t mask)
+// One item's operand value (the rare first-writer path).
+template <int NREGS, int ITEMS>
+__device__ __forceinline__ int32_t operand_item(const sdb_operand &o, const Tile<NREGS, ITEMS> &T, int k)
 {
+    if (o.kind == SDB_SRC_COL) return __ldg(o.col + row_of(T.base, k));
+    if (o.kind == SDB_SRC_LIT) return o.lit;
+    int32_t v = T.reg[0][k];
 #pragma unroll
-    for (int j = 0; j < 4; j++)
-        if (mask & (1u << j)) col[r0 + j] = v[j];
+    for (int r = 1; r < NREGS; r++)
+        if (o.reg == r) v = T.reg[r][k];
+    return v;
 }
 
-__device__ __forceinline__ uint32_t load_flags4(const uint8_t *f, uint64_t r0, uint32_t valid, bool full, bool vec)
+template <int ITEMS>
+__device__ __forceinline__ void store_masked(int32_t *col, uint64_t base, const int32_t (&v)[ITEMS], uint32_t mask)
 {
-    if (full && vec) {
-        uint32_t w = __ldcs(reinterpret_cast<const unsigned int *>(f + r0));
-        uint32_t x = __vcmpne4(w, 0u);
-        return ((x >> 7) & 1u) | ((x >> 14) & 2u) | ((x >> 21) & 4u) | ((x >> 28) & 8u);
-    }
-    uint32_t m = 0;
 #pragma unroll
-    for (int j = 0; j < 4; j++)
-        if ((valid >> j) & 1u) m |= (uint32_t)(f[r0 + j] != 0) << j;
-    return m;
+    for (int k = 0; k < ITEMS; k++)
+        if ((mask >> k) & 1u) col[row_of(base, k)] = v[k];
 }
 
-__device__ __forceinline__ void store_flags4(uint8_t *f, uint64_t r0, uint32_t live, uint32_t valid, bool full, bool vec)
-{
-    if (full && vec) {
-        uint32_t w = (live & 1u) | ((live & 2u) << 7) | ((live & 4u) << 14) | ((live & 8u) << 21);
-        *reinterpret_cast<unsigned int *>(f + r0) = w;
-        return;
-    }
-#pragma unroll
-    for (int j = 0; j < 4; j++)
-        if ((valid >> j) & 1u) f[r0 + j] = (uint8_t)((live >> j) & 1u);
-}
-
-// Evaluates the op list on one 4-row group.  Returns the live mask; the
-// registers hold the values the ops produced for live rows.
-template <int NREGS, class L>
-__device__ __forceinline__ uint32_t run_ops(const L &Lc, uint64_t r0, uint32_t valid, bool full, Regs<NREGS> &R)
+// Evaluates the op list on a thread's items; on return T.live holds the flags.
+template <int NREGS, int ITEMS, class LC>
+__device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
 {
     const sdb_chain_desc &d = Lc.d;
-    const bool vec = Lc.vec != 0;
-    uint32_t live = d.flags_in ? load_flags4(d.flags_in, r0, valid, full, vec) : valid;
+    if (d.flags_in) {
+        uint8_t f[ITEMS];
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++)
+            if ((T.valid >> k) & 1u) f[k] = __ldcs(d.flags_in + row_of(T.base, k));
+        T.live = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++)
+            if ((T.valid >> k) & 1u) T.live |= (uint32_t)(f[k] != 0) << k;
+    } else {
+        T.live = T.valid;
+    }
 
 #pragma unroll 1
-    for (int k = 0; k < d.n_ops; k++) {
-        if (live == 0 && k >= Lc.dead_from) break;
-        const sdb_chain_op &op = d.ops[k];
-        int32_t a[4], b[4];
+    for (int i = 0; i < d.n_ops; i++) {
+        if (T.live == 0 && i >= Lc.dead_from) break;
+        const sdb_chain_op &op = d.ops[i];
+        int32_t a[ITEMS], c[ITEMS];
         switch (op.kind) {
         case SDB_OP_SELECT: {
-            const uint32_t need = op.logic_op == SDB_AND ? live : valid;
-            fetch(op.a, r0, need, full, vec, R, a);
-            fetch(op.b, r0, need, full, vec, R, b);
+            const uint32_t need = op.logic_op == SDB_AND ? T.live : T.valid;
+            fetch(op.a, T, need, a);
+            fetch(op.b, T, need, c);
             uint32_t m = 0;
 #pragma unroll
-            for (int j = 0; j < 4; j++) m |= (uint32_t)sdb::compare(op.cmp_op, a[j], b[j]) << j;
-            live = sdb::logical4(op.logic_op, live, m & need) & valid;
+            for (int k = 0; k < ITEMS; k++) m |= (uint32_t)sdb::compare(op.cmp_op, a[k], c[k]) << k;
+            T.live = sdb::logical4(op.logic_op, T.live, m & need) & T.valid;
             break;
         }
         case SDB_OP_SEARCH_RANGE:
         case SDB_OP_SEARCH_POINTS: {
-            const uint32_t need = op.logic_op == SDB_AND ? live : valid;
-            fetch(op.a, r0, need, full, vec, R, a);
+            const uint32_t need = op.logic_op == SDB_AND ? T.live : T.valid;
+            fetch(op.a, T, need, a);
             uint32_t m = 0;
             if (op.kind == SDB_OP_SEARCH_RANGE) {
 #pragma unroll
-                for (int j = 0; j < 4; j++) m |= (uint32_t)(a[j] >= op.lo && a[j] <= op.hi) << j;
+                for (int k = 0; k < ITEMS; k++) m |= (uint32_t)(a[k] >= op.lo && a[k] <= op.hi) << k;
             } else {
 #pragma unroll
-                for (int j = 0; j < 4; j++) m |= (uint32_t)(a[j] == op.lo || a[j] == op.hi) << j;
+                for (int k = 0; k < ITEMS; k++) m |= (uint32_t)(a[k] == op.lo || a[k] == op.hi) << k;
             }
-            live = sdb::logical4(op.logic_op, live, m & need) & valid;
+            T.live = sdb::logical4(op.logic_op, T.live, m & need) & T.valid;
             break;
         }
         case SDB_OP_SEMI_PROBE: {
-            fetch(op.a, r0, live, full, vec, R, a);
+            const uint32_t need = T.live;
+            fetch(op.a, T, need, a);
             const uint8_t *ht = static_cast<const uint8_t *>(op.ht);
+            uint8_t h[ITEMS];
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                h[k] = 0;
+                if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) h[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+            }
             uint32_t m = 0;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-                if ((live >> j) & 1u) {
-                    const int32_t key = a[j];
-                    if (key >= op.lo && key <= op.hi && __ldg(ht + ((uint32_t)key - (uint32_t)op.lo)) != 0)
-                        m |= 1u << j;
-                }
-            live = m;
+            for (int k = 0; k < ITEMS; k++) m |= (uint32_t)(h[k] != 0) << k;
+            T.live = m & need;
             break;
         }
         case SDB_OP_FULL_PROBE: {
-            fetch(op.a, r0, live, full, vec, R, a);
+            const uint32_t need = T.live;
+            fetch(op.a, T, need, a);
             const int2 *ht = static_cast<const int2 *>(op.ht);
-            uint32_t m = 0;
-            int32_t val[4] = {0, 0, 0, 0};
+            int2 e[ITEMS];
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-                if ((live >> j) & 1u) {
-                    const int32_t key = a[j];
-                    if (key >= op.lo && key <= op.hi) {
-                        const int2 e = __ldg(ht + ((uint32_t)key - (uint32_t)op.lo));
-                        if (e.x == 1) {
-                            m |= 1u << j;
-                            val[j] = e.y;
-                        }
-                    }
-                }
-            live = m;
-            reg_set(R, op.out_reg, val, m);
-            if (op.out_col && m) store_masked(op.out_col, r0, val, m);
+            for (int k = 0; k < ITEMS; k++) {
+                e[k] = make_int2(0, 0);
+                if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) e[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+            }
+            uint32_t m = 0;
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                m |= (uint32_t)(e[k].x == 1) << k;
+                c[k] = e[k].y;
+            }
+            m &= need;
+            T.live = m;
+            reg_set(T, op.out_reg, c, m);
+            if (op.out_col && m) store_masked(op.out_col, T.base, c, m);
             break;
         }
         case SDB_OP_BINOP: {
-            fetch(op.a, r0, live, full, vec, R, a);
-            fetch(op.b, r0, live, full, vec, R, b);
-            int32_t c[4];
+            const uint32_t need = T.live;
+            fetch(op.a, T, need, a);
+            fetch(op.b, T, need, c);
 #pragma unroll
-            for (int j = 0; j < 4; j++) c[j] = sdb::binop(a[j], b[j], op.bin_op);
-            reg_set(R, op.out_reg, c, live);
-            if (op.out_col && live) store_masked(op.out_col, r0, c, live);
+            for (int k = 0; k < ITEMS; k++) a[k] = sdb::binop(a[k], c[k], op.bin_op);
+            reg_set(T, op.out_reg, a, need);
+            if (op.out_col && need) store_masked(op.out_col, T.base, a, need);
             break;
         }
         case SDB_OP_FILL: {
-            int32_t c[4] = {op.a.lit, op.a.lit, op.a.lit, op.a.lit};
-            reg_set(R, op.out_reg, c, valid);
-            if (op.out_col) store_masked(op.out_col, r0, c, valid);
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) a[k] = op.a.lit;
+            reg_set(T, op.out_reg, a, T.valid);
+            if (op.out_col && T.valid) store_masked(op.out_col, T.base, a, T.valid);
             break;
         }
         default:
             break;
         }
     }
-    return live;
 }
 
-template <int TERM, int NREGS>
-__global__ void __launch_bounds__(kThreads) k_chain(const __grid_constant__ ChainLaunch L)
+// Block-private group-by partials: a shared-memory table of kCap entries
+// (slot id + 64-bit sum, 24 KB).  Slots index it directly when P <= kCap;
+// otherwise it is an open-addressing table (bounded linear probing) and a
+// row that finds no entry goes straight to the global arrays.
+constexpr uint32_t kCap = 2048;
+constexpr uint32_t kEmpty = 0xFFFFFFFFu;
+constexpr int kMaxProbe = 16;
+
+template <uint32_t CAP = kCap>
+__device__ __forceinline__ bool smem_group_add(uint32_t *s_key, unsigned long long *s_sum, uint32_t slot,
+                                               unsigned long long v, bool direct, bool &first)
+{
+    static_assert((CAP & (CAP - 1)) == 0, "table size must be a power of two");
+    uint32_t h = direct ? slot : ((slot * 2654435761u) >> (32 - __builtin_ctz(CAP)));
+#pragma unroll 1
+    for (int p = 0; p < (direct ? 1 : kMaxProbe); p++) {
+        uint32_t k = s_key[h];
+        if (k == kEmpty) {
+            k = atomicCAS(&s_key[h], kEmpty, slot);
+            if (k == kEmpty) {
+                first = true;
+                atomicAdd(&s_sum[h], v);
+                return true;
+            }
+        }
+        if (k == slot) {
+            first = false;
+            atomicAdd(&s_sum[h], v);
+            return true;
+        }
+        h = (h + 1) & (CAP - 1);
+    }
+    return false;
+}
+
+// Resident blocks per SM a tile size targets (register cap 64 / 85 / 128
+// per thread at 256 threads per block).
+__host__ __device__ constexpr int min_blocks_of(int ITEMS) { return ITEMS <= 4 ? 4 : (ITEMS <= 8 ? 3 : 2); }
+
+template <int TERM, int NREGS, int ITEMS>
+__global__ void __launch_bounds__(kThreads, min_blocks_of(ITEMS)) k_chain(const __grid_constant__ ChainLaunch L)
 {
     const sdb_chain_desc &d = L.d;
-    extern __shared__ uint64_t s_sum[];
-    uint32_t *s_occ = reinterpret_cast<uint32_t *>(s_sum + (TERM == T_GROUP_SMEM ? d.P : 0));
-    if (TERM == T_GROUP_SMEM) {
-        for (uint64_t i = threadIdx.x; i < d.P; i += blockDim.x) { s_sum[i] = 0; s_occ[i] = 0; }
+    __shared__ uint32_t s_key[TERM == T_GROUP ? kCap : 1];
+    __shared__ unsigned long long s_sum[TERM == T_GROUP ? kCap : 1];
+    const bool direct = d.P <= kCap;
+    if (TERM == T_GROUP) {
+        for (uint32_t i = threadIdx.x; i < kCap; i += blockDim.x) {
+            s_key[i] = kEmpty;
+            s_sum[i] = 0;
+        }
         __syncthreads();
     }
 
-    const uint64_t groups = (d.n + 3) >> 2;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    constexpr uint64_t kTile = (uint64_t)kThreads * ITEMS;
     uint64_t acc = 0;
-    Regs<NREGS> R;
+    Tile<NREGS, ITEMS> T;
 #pragma unroll
     for (int r = 0; r < NREGS; r++)
 #pragma unroll
-        for (int j = 0; j < 4; j++) R.v[r][j] = 0;
+        for (int k = 0; k < ITEMS; k++) T.reg[r][k] = 0;
 
-    for (uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; g < groups; g += stride) {
-        const uint64_t r0 = g << 2;
-        const uint64_t left = d.n - r0;
-        const bool full = left >= 4;
-        const uint32_t valid = full ? 0xFu : ((1u << left) - 1u);
-        uint32_t live = run_ops<NREGS>(L, r0, valid, full, R);
-
-        if (TERM == T_FLAGS || d.flags_out) store_flags4(d.flags_out, r0, live, valid, full, L.vec != 0);
-        if (live == 0) continue;
-
-        if (TERM == T_SUM) {
-            int32_t v[4];
-            fetch(d.value, r0, live, full, L.vec != 0, R, v);
+    for (uint64_t tile = (uint64_t)blockIdx.x * kTile; tile < d.n; tile += (uint64_t)gridDim.x * kTile) {
+        T.base = tile + threadIdx.x;
+        T.valid = 0;
 #pragma unroll
-            for (int j = 0; j < 4; j++)
-                if ((live >> j) & 1u) acc += sdb::widen(v[j]);
-        } else if (TERM == T_GROUP_SMEM || TERM == T_GROUP_GLOBAL) {
-            int32_t v[4];
-            int32_t key[SDB_CHAIN_MAX_KEYS][4];
-            fetch(d.value, r0, live, full, L.vec != 0, R, v);
-            uint32_t h[4] = {0, 0, 0, 0};
+        for (int k = 0; k < ITEMS; k++) T.valid |= (uint32_t)(row_of(T.base, k) < d.n) << k;
+        run_ops(L, T);
+
+        if (TERM == T_FLAGS || d.flags_out) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++)
+                if ((T.valid >> k) & 1u) d.flags_out[row_of(T.base, k)] = (uint8_t)((T.live >> k) & 1u);
+        }
+        if (T.live == 0) continue;
+        if (TERM == T_SUM) {
+            int32_t v[ITEMS];
+            fetch(d.value, T, T.live, v);
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++)
+                if ((T.live >> k) & 1u) acc += sdb::widen(v[k]);
+        } else if (TERM == T_GROUP) {
+            int32_t v[ITEMS], kv[ITEMS];
+            uint32_t h[ITEMS];
+            fetch(d.value, T, T.live, v);
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) h[k] = 0;
 #pragma unroll
             for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++) {
-                if (kk >= d.n_keys) break;
-                fetch(d.keys[kk], r0, live, full, L.vec != 0, R, key[kk]);
+                if (kk < d.n_keys) {
+                    fetch(d.keys[kk], T, T.live, kv);
 #pragma unroll
-                for (int j = 0; j < 4; j++)
-                    h[j] += ((uint32_t)key[kk][j] - (uint32_t)d.key_min[kk]) * L.mults[kk];
+                    for (int k = 0; k < ITEMS; k++) h[k] += ((uint32_t)kv[k] - (uint32_t)d.key_min[kk]) * L.mults[kk];
+                }
             }
 #pragma unroll
-            for (int j = 0; j < 4; j++) {
-                if (!((live >> j) & 1u)) continue;
-                const int64_t s = sdb::group_slot(h[j], d.P);
-                if (s < 0 || (uint64_t)s >= d.P) { atomicAdd(&g_errors, 1ull); continue; }
-                bool first;
-                if (TERM == T_GROUP_SMEM) {
-                    first = atomicExch(&s_occ[s], 1u) == 0u;
+            for (int k = 0; k < ITEMS; k++) {
+                if (!((T.live >> k) & 1u)) continue;
+                const int64_t s = sdb::group_slot(h[k], d.P);
+                if (s < 0 || (uint64_t)s >= d.P) {
+                    atomicAdd(&g_errors, 1ull);
+                    continue;
+                }
+                const unsigned long long val = (unsigned long long)sdb::widen(v[k]);
+                bool first = false;
+                if (smem_group_add(s_key, s_sum, (uint32_t)s, val, direct, first)) {
                     if (first) first = atomicExch(&d.occ[s], 1u) == 0u;
-                    atomicAdd(reinterpret_cast<unsigned long long *>(&s_sum[s]), (unsigned long long)sdb::widen(v[j]));
                 } else {
                     first = d.occ[s] == 0u && atomicExch(&d.occ[s], 1u) == 0u;
-                    atomicAdd(reinterpret_cast<unsigned long long *>(&d.out_sum[s]), (unsigned long long)sdb::widen(v[j]));
+                    atomicAdd(reinterpret_cast<unsigned long long *>(&d.out_sum[s]), val);
                 }
                 if (first) {
 #pragma unroll
                     for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-                        if (kk < d.n_keys) d.out_keys[kk][s] = key[kk][j];
+                        if (kk < d.n_keys) d.out_keys[kk][s] = operand_item(d.keys[kk], T, k);
                 }
             }
         }
@@ -318,14 +371,14 @@ __global__ void __launch_bounds__(kThreads) k_chain(const __grid_constant__ Chai
             for (int w = 0; w < kThreads / 32; w++) t += part[w];
             if (t) atomicAdd(reinterpret_cast<unsigned long long *>(d.sum_out), (unsigned long long)t);
         }
-    } else if (TERM == T_GROUP_SMEM) {
+    } else if (TERM == T_GROUP) {
         __syncthreads();
-        for (uint64_t i = threadIdx.x; i < d.P; i += blockDim.x)
-            if (s_occ[i]) atomicAdd(reinterpret_cast<unsigned long long *>(&d.out_sum[i]), (unsigned long long)s_sum[i]);
+        for (uint32_t i = threadIdx.x; i < kCap; i += blockDim.x) {
+            const uint32_t k = s_key[i];
+            if (k != kEmpty) atomicAdd(reinterpret_cast<unsigned long long *>(&d.out_sum[k]), s_sum[i]);
+        }
     }
 }
-
-constexpr uint64_t kSmemSlotsMax = 16384;  // 16 K slots x 12 B = 192 KB of shared memory
 
 int num_sms()
 {
@@ -338,37 +391,705 @@ int num_sms()
     return sms;
 }
 
-template <int TERM, int NREGS>
+template <int TERM, int NREGS, int ITEMS>
 int launch_term(const ChainLaunch &L, cudaStream_t s)
 {
-    auto kern = k_chain<TERM, NREGS>;
-    size_t smem = 0;
-    if (TERM == T_GROUP_SMEM) {
-        smem = (size_t)L.d.P * (sizeof(uint64_t) + sizeof(uint32_t));
-        static bool attr = false;
-        if (!attr) {
-            cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(kSmemSlotsMax * 12));
-            attr = true;
+    auto kern = k_chain<TERM, NREGS, ITEMS>;
+    static int per_sm = 0;
+    if (per_sm == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0) != cudaSuccess || per_sm < 1))
+        per_sm = 1;
+    const uint64_t tile = (uint64_t)kThreads * ITEMS;
+    uint64_t blocks = (L.d.n + tile - 1) / tile;
+    const uint64_t cap = (uint64_t)num_sms() * per_sm;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    kern<<<(unsigned)blocks, kThreads, 0, s>>>(L);
+    return sdb_check_launch("sdb_fused_chain");
+}
+
+// Variants: 0, 1, 2 = 4, 8, 16 rows per thread.  Chains needing up to 2
+// registers take all three; up to 4 registers, 4 or 8 rows; up to 8, 4 rows.
+template <int TERM>
+int launch_regs(const ChainLaunch &L, int nregs, int variant, cudaStream_t s)
+{
+    if (nregs <= 2) {
+        if (variant <= 0) return launch_term<TERM, 2, 4>(L, s);
+        if (variant == 1) return launch_term<TERM, 2, 8>(L, s);
+        return launch_term<TERM, 2, 16>(L, s);
+    }
+    if (nregs <= 4) {
+        if (variant <= 0) return launch_term<TERM, 4, 4>(L, s);
+        return launch_term<TERM, 4, 8>(L, s);
+    }
+    return launch_term<TERM, 8, 4>(L, s);
+}
+
+// ------------------------------------------------------------------ dense
+// Shape-specialised pass for the common chains.  The op sequence is a
+// compile-time pack, so each op is straight-line code (no dispatch), and the
+// columns the chain reads (up to kSlots distinct ones) are loaded for the
+// NEXT tile while the current tile is probed: DRAM latency overlaps the
+// hash-table probes instead of sitting in each row's dependency chain.  Every
+// chain column is read in full (dense), so the pass is bound by HBM
+// bandwidth at 4 B per column per row.
+namespace dense {
+
+constexpr int kItems = 4;
+constexpr int kSlots = 4;
+constexpr int kMaxOps = 8;
+
+struct Src {
+    int32_t src;  // 0 prefetched column slot, 1 register, 2 literal
+    int32_t idx;
+    int32_t lit;
+    int32_t pad;
+};
+
+struct Op {
+    int32_t kind, cmp, logic, bin;
+    Src a, b;
+    int32_t lo, hi, out_reg;
+    int32_t smem_bits;  // SEMI: probe the shared-memory bitmap copy of ht
+    const void *ht;
+    int32_t *out_col;
+};
+
+struct Launch {
+    uint64_t n;
+    const uint8_t *flags_in;
+    uint8_t *flags_out;
+    const int32_t *slot[kSlots];
+    int32_t nslot, n_ops;
+    Op ops[kMaxOps];
+    Src value;
+    uint64_t *sum_out;
+    int32_t n_keys, pad;
+    Src keys[SDB_CHAIN_MAX_KEYS];
+    int32_t key_min[SDB_CHAIN_MAX_KEYS];
+    uint32_t mults[SDB_CHAIN_MAX_KEYS];
+    uint64_t P;
+    int32_t *out_keys[SDB_CHAIN_MAX_KEYS];
+    uint64_t *out_sum;
+    uint32_t *occ;
+    const uint8_t *bitmap_ht;  // semi-join table staged as a bitmap (NULL: none)
+    uint32_t bitmap_len;       // its entries
+};
+
+// Largest semi-join table staged as a shared-memory bitmap (32 KB of bits).
+constexpr uint32_t kBitmapMax = 1u << 18;
+// Block-private group-by table of the specialised pass (12 KB).
+constexpr uint32_t kDenseCap = 1024;
+
+// Tile rows are staged in shared memory by cp.async: thread t's four rows
+// (tile + 4t .. 4t + 3) of every chain column arrive as one 16-byte copy per
+// column into a kStages-deep ring, issued kStages - 1 tiles ahead.  Each
+// thread reads back only what it copied, so no block barrier is needed.
+constexpr int kStages = 3;
+
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint32_t src_bytes)
+{
+    const uint32_t d = (uint32_t)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(d), "l"(gmem), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+template <int NREGS>
+struct State {
+    int32_t reg[NREGS][kItems];
+    const uint32_t *bits;  // shared-memory bitmap of the staged semi-join table
+    const int4 *stage;  // this thread's copies of the current tile: stage[slot * kThreads]
+    uint64_t base;      // row of item 0 (items are base .. base + 3)
+    uint32_t valid, live;
+};
+
+template <int NREGS>
+__device__ __forceinline__ void fetch4(const Src &s, const State<NREGS> &S, int32_t (&v)[kItems])
+{
+    if (s.src == 0) {
+        const int4 q = S.stage[s.idx * kThreads];
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if (s.src == 1) {
+#pragma unroll
+        for (int k = 0; k < kItems; k++) v[k] = S.reg[0][k];
+#pragma unroll
+        for (int i = 1; i < NREGS; i++)
+            if (s.idx == i) {
+#pragma unroll
+                for (int k = 0; k < kItems; k++) v[k] = S.reg[i][k];
+            }
+    } else {
+#pragma unroll
+        for (int k = 0; k < kItems; k++) v[k] = s.lit;
+    }
+}
+
+template <int NREGS>
+__device__ __forceinline__ void set_regs(State<NREGS> &S, int r, const int32_t (&v)[kItems], uint32_t mask)
+{
+#pragma unroll
+    for (int i = 0; i < NREGS; i++)
+        if (r == i) {
+#pragma unroll
+            for (int k = 0; k < kItems; k++)
+                if ((mask >> k) & 1u) S.reg[i][k] = v[k];
+        }
+}
+
+__device__ __forceinline__ void store4(int32_t *col, uint64_t base, const int32_t (&v)[kItems], uint32_t mask)
+{
+#pragma unroll
+    for (int k = 0; k < kItems; k++)
+        if ((mask >> k) & 1u) col[base + k] = v[k];
+}
+
+template <int K, int NREGS>
+__device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
+{
+    int32_t a[kItems], b[kItems];
+    if (K == SDB_OP_SELECT || K == SDB_OP_SEARCH_RANGE || K == SDB_OP_SEARCH_POINTS) {
+        const bool and_op = op.logic == SDB_AND;
+        if (and_op && S.live == 0) return;
+        const uint32_t need = and_op ? S.live : S.valid;
+        fetch4(op.a, S, a);
+        if (K == SDB_OP_SELECT) fetch4(op.b, S, b);
+        uint32_t m = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+            bool c;
+            if (K == SDB_OP_SELECT) c = sdb::compare(op.cmp, a[k], b[k]);
+            else if (K == SDB_OP_SEARCH_RANGE) c = a[k] >= op.lo && a[k] <= op.hi;
+            else c = a[k] == op.lo || a[k] == op.hi;
+            m |= (uint32_t)c << k;
+        }
+        S.live = sdb::logical4(op.logic, S.live, m & need) & S.valid;
+    } else if (K == SDB_OP_SEMI_PROBE) {
+        if (S.live == 0) return;
+        fetch4(op.a, S, a);
+        const uint8_t *ht = static_cast<const uint8_t *>(op.ht);
+        uint32_t m = 0;
+        if (op.smem_bits) {
+#pragma unroll
+            for (int k = 0; k < kItems; k++)
+                if (((S.live >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) {
+                    const uint32_t h = (uint32_t)a[k] - (uint32_t)op.lo;
+                    m |= ((S.bits[h >> 5] >> (h & 31u)) & 1u) << k;
+                }
+        } else {
+            uint8_t h[kItems];
+#pragma unroll
+            for (int k = 0; k < kItems; k++) {
+                h[k] = 0;
+                if (((S.live >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi)
+                    h[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+            }
+#pragma unroll
+            for (int k = 0; k < kItems; k++) m |= (uint32_t)(h[k] != 0) << k;
+        }
+        S.live &= m;
+    } else if (K == SDB_OP_FULL_PROBE) {
+        if (S.live == 0) return;
+        fetch4(op.a, S, a);
+        const int2 *ht = static_cast<const int2 *>(op.ht);
+        int2 e[kItems];
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+            e[k] = make_int2(0, 0);
+            if (((S.live >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi)
+                e[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+        }
+        uint32_t m = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; k++) {
+            m |= (uint32_t)(e[k].x == 1) << k;
+            b[k] = e[k].y;
+        }
+        m &= S.live;
+        S.live = m;
+        set_regs(S, op.out_reg, b, m);
+        if (op.out_col && m) store4(op.out_col, S.base, b, m);
+    } else if (K == SDB_OP_BINOP) {
+        if (S.live == 0) return;
+        fetch4(op.a, S, a);
+        fetch4(op.b, S, b);
+#pragma unroll
+        for (int k = 0; k < kItems; k++) a[k] = sdb::binop(a[k], b[k], op.bin);
+        set_regs(S, op.out_reg, a, S.live);
+        if (op.out_col) store4(op.out_col, S.base, a, S.live);
+    } else if (K == SDB_OP_FILL) {
+#pragma unroll
+        for (int k = 0; k < kItems; k++) a[k] = op.a.lit;
+        set_regs(S, op.out_reg, a, S.valid);
+        if (op.out_col) store4(op.out_col, S.base, a, S.valid);
+    }
+}
+
+template <int NREGS, int BEGIN, int... KS, int... IS>
+__device__ __forceinline__ void run_steps(const Launch &L, State<NREGS> &S, std::integer_sequence<int, IS...>)
+{
+    constexpr int kinds[] = {KS...};
+    (step<kinds[BEGIN + IS], NREGS>(L.ops[BEGIN + IS], S), ...);
+}
+
+// Sparse phase: after op SPLIT - 1 each warp compacts its surviving rows
+// (ballot-free: a warp prefix sum of the lanes' live-bit counts) into a
+// shared-memory list, and the remaining ops run one row per lane over that
+// dense list instead of over mostly-dead 4-row groups.
+template <int NREGS>
+struct Row {
+    int32_t reg[NREGS];
+    const int32_t *wstage;  // the warp's 128 staged rows of slot 0 (slot s at + s * 4 * kThreads)
+    uint32_t r;             // row within the warp's 128
+    uint64_t grow;          // global row
+    bool live;
+};
+
+template <int NREGS>
+__device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
+{
+    if (s.src == 0) return R.wstage[s.idx * 4 * kThreads + R.r];
+    if (s.src == 1) {
+        int32_t v = R.reg[0];
+#pragma unroll
+        for (int i = 1; i < NREGS; i++) v = s.idx == i ? R.reg[i] : v;
+        return v;
+    }
+    return s.lit;
+}
+
+template <int K, int NREGS>
+__device__ __forceinline__ void step1(const Op &op, Row<NREGS> &R, const uint32_t *bits)
+{
+    if (!R.live) return;
+    if (K == SDB_OP_SELECT) {
+        R.live = sdb::compare(op.cmp, fetch1(op.a, R), fetch1(op.b, R));
+    } else if (K == SDB_OP_SEARCH_RANGE) {
+        const int32_t a = fetch1(op.a, R);
+        R.live = a >= op.lo && a <= op.hi;
+    } else if (K == SDB_OP_SEARCH_POINTS) {
+        const int32_t a = fetch1(op.a, R);
+        R.live = a == op.lo || a == op.hi;
+    } else if (K == SDB_OP_SEMI_PROBE) {
+        const int32_t a = fetch1(op.a, R);
+        if (a < op.lo || a > op.hi) {
+            R.live = false;
+        } else {
+            const uint32_t h = (uint32_t)a - (uint32_t)op.lo;
+            R.live = op.smem_bits ? ((bits[h >> 5] >> (h & 31u)) & 1u) != 0
+                                  : __ldg(static_cast<const uint8_t *>(op.ht) + h) != 0;
+        }
+    } else if (K == SDB_OP_FULL_PROBE) {
+        const int32_t a = fetch1(op.a, R);
+        if (a < op.lo || a > op.hi) {
+            R.live = false;
+        } else {
+            const int2 e = __ldg(static_cast<const int2 *>(op.ht) + ((uint32_t)a - (uint32_t)op.lo));
+            R.live = e.x == 1;
+#pragma unroll
+            for (int i = 0; i < NREGS; i++) R.reg[i] = (R.live && op.out_reg == i) ? e.y : R.reg[i];
+            if (R.live && op.out_col) op.out_col[R.grow] = e.y;
+        }
+    } else if (K == SDB_OP_BINOP) {
+        const int32_t v = sdb::binop(fetch1(op.a, R), fetch1(op.b, R), op.bin);
+#pragma unroll
+        for (int i = 0; i < NREGS; i++) R.reg[i] = op.out_reg == i ? v : R.reg[i];
+        if (op.out_col) op.out_col[R.grow] = v;
+    }
+}
+
+template <int NREGS, int BEGIN, int... KS, int... IS>
+__device__ __forceinline__ void run_steps1(const Launch &L, Row<NREGS> &R, const uint32_t *bits,
+                                           std::integer_sequence<int, IS...>)
+{
+    constexpr int kinds[] = {KS...};
+    (step1<kinds[BEGIN + IS], NREGS>(L.ops[BEGIN + IS], R, bits), ...);
+}
+
+// Adds one row to the group-by (block table first, global on overflow) and
+// runs the first-writer exchange; key(kk) gives the row's key values.
+template <class KeyFn>
+__device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsigned long long *s_sum, bool direct,
+                                          uint32_t h, int32_t value, KeyFn key)
+{
+    const int64_t sl = sdb::group_slot(h, L.P);
+    if (sl < 0 || (uint64_t)sl >= L.P) {
+        atomicAdd(&g_errors, 1ull);
+        return;
+    }
+    const unsigned long long val = (unsigned long long)sdb::widen(value);
+    bool first = false;
+    if (smem_group_add<kDenseCap>(s_key, s_sum, (uint32_t)sl, val, direct, first)) {
+        if (first) first = atomicExch(&L.occ[sl], 1u) == 0u;
+    } else {
+        first = L.occ[sl] == 0u && atomicExch(&L.occ[sl], 1u) == 0u;
+        atomicAdd(reinterpret_cast<unsigned long long *>(&L.out_sum[sl]), val);
+    }
+    if (first) {
+#pragma unroll
+        for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+            if (kk < L.n_keys) L.out_keys[kk][sl] = key(kk);
+    }
+}
+
+// SPLIT = number of ops run on 4-row groups; the rest run on the compacted
+// rows.  SPLIT == sizeof...(KS) + 1 means no compaction (all ops dense, which
+// also serves SDB_TERM_FLAGS).
+template <int TERM, int NREGS, int SPLIT, int... KS>
+__global__ void __launch_bounds__(kThreads, 3) k_dense(const __grid_constant__ Launch L)
+{
+    constexpr int N = sizeof...(KS);
+    constexpr bool kCompact = SPLIT <= N;
+    constexpr int kDenseOps = kCompact ? SPLIT : N;
+    extern __shared__ int4 s_buf[];  // [kStages][kSlots][kThreads], then the semi-join bitmap
+    __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
+    const bool direct = L.P <= kDenseCap;
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
+    if (TERM == T_GROUP) {
+        for (uint32_t i = threadIdx.x; i < kDenseCap; i += blockDim.x) {
+            s_key[i] = kEmpty;
+            s_sum[i] = 0;
         }
     }
+    if (L.bitmap_ht) {
+        // Pack the bool table into bits: word w holds entries 32w .. 32w + 31.
+        const uint32_t words = (L.bitmap_len + 31) / 32;
+        for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
+            uint32_t bits = 0;
+            const uint32_t e0 = w * 32;
+            if (e0 + 32 <= L.bitmap_len && sdb::aligned(L.bitmap_ht, 4)) {
+                const uint32_t *q = reinterpret_cast<const uint32_t *>(L.bitmap_ht + e0);
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const uint32_t x = __vcmpne4(__ldg(q + j), 0u);
+                    bits |= (((x >> 7) & 1u) | ((x >> 14) & 2u) | ((x >> 21) & 4u) | ((x >> 28) & 8u)) << (4 * j);
+                }
+            } else {
+                for (uint32_t j = 0; j < 32 && e0 + j < L.bitmap_len; j++) bits |= (uint32_t)(L.bitmap_ht[e0 + j] != 0) << j;
+            }
+            s_bits[w] = bits;
+        }
+    }
+    if (TERM == T_GROUP || L.bitmap_ht) __syncthreads();
+    constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
+    const uint64_t stride = (uint64_t)gridDim.x * kTile;
+    const int nslot = L.nslot;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+
+    // Copies this thread's 4 rows of every slot column for `tile` into ring
+    // stage `st` (rows past the end are zero-filled or skipped), then commits
+    // one group (possibly empty, so every thread counts groups the same way).
+    auto issue = [&](int st, uint64_t tile) {
+        const uint64_t r0 = tile + (uint64_t)kItems * threadIdx.x;
+        if (r0 < L.n) {
+            const uint64_t left = L.n - r0;
+            const uint32_t bytes = left >= kItems ? 16u : (uint32_t)(left * 4);
+#pragma unroll
+            for (int sl = 0; sl < kSlots; sl++)
+                if (sl < nslot)
+                    cp_async16(&s_buf[(st * kSlots + sl) * kThreads + threadIdx.x], L.slot[sl] + r0, bytes);
+        }
+        cp_async_commit();
+    };
+
+    State<NREGS> S;
+    S.bits = s_bits;
+#pragma unroll
+    for (int r = 0; r < NREGS; r++)
+#pragma unroll
+        for (int k = 0; k < kItems; k++) S.reg[r][k] = 0;
+    uint64_t acc = 0;
+
+    uint64_t tile = (uint64_t)blockIdx.x * kTile;
+#pragma unroll
+    for (int p = 0; p < kStages - 1; p++) issue(p, tile + p * stride);
+    int st = 0;
+    for (; tile < L.n; tile += stride) {
+        issue((st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
+        cp_async_wait<kStages - 1>();
+        S.stage = &s_buf[st * kSlots * kThreads + threadIdx.x];
+        S.base = tile + (uint64_t)kItems * threadIdx.x;
+        S.valid = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; k++) S.valid |= (uint32_t)(S.base + k < L.n) << k;
+        if (L.flags_in && S.valid) {
+            uint32_t m = 0;
+#pragma unroll
+            for (int k = 0; k < kItems; k++)
+                if ((S.valid >> k) & 1u) m |= (uint32_t)(L.flags_in[S.base + k] != 0) << k;
+            S.live = m;
+        } else {
+            S.live = S.valid;
+        }
+        run_steps<NREGS, 0, KS...>(L, S, std::make_integer_sequence<int, kDenseOps>{});
+
+        if constexpr (kCompact) {
+            // warp prefix sum of the live-row counts
+            const uint32_t cnt = __popc(S.live);
+            uint32_t incl = cnt;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+                if (lane >= (uint32_t)o) incl += y;
+            }
+            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+            uint8_t *list = s_list + warp * 32 * kItems;
+            uint32_t pos = incl - cnt;
+#pragma unroll
+            for (int k = 0; k < kItems; k++)
+                if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
+            __syncwarp();
+            Row<NREGS> R;
+            R.wstage = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
+            for (uint32_t b = 0; b < total; b += 32) {
+                const uint32_t idx = b + lane;
+                R.live = idx < total;
+                R.r = R.live ? list[idx] : 0;
+                R.grow = tile + (uint64_t)warp * 32 * kItems + R.r;
+#pragma unroll
+                for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
+                run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
+                if (R.live) {
+                    if (TERM == T_SUM) {
+                        acc += sdb::widen(fetch1(L.value, R));
+                    } else if (TERM == T_GROUP) {
+                        uint32_t h = 0;
+#pragma unroll
+                        for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+                            if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
+                        group_row(L, s_key, s_sum, direct, h, fetch1(L.value, R),
+                                  [R, &L](int kk) { return fetch1(L.keys[kk], R); });
+                    }
+                }
+            }
+            __syncwarp();
+        } else {
+            if (TERM == T_FLAGS || L.flags_out) {
+#pragma unroll
+                for (int k = 0; k < kItems; k++)
+                    if ((S.valid >> k) & 1u) L.flags_out[S.base + k] = (uint8_t)((S.live >> k) & 1u);
+            }
+            if (S.live) {
+                int32_t v[kItems];
+                if (TERM == T_SUM) {
+                    fetch4(L.value, S, v);
+#pragma unroll
+                    for (int k = 0; k < kItems; k++)
+                        if ((S.live >> k) & 1u) acc += sdb::widen(v[k]);
+                } else if (TERM == T_GROUP) {
+                    fetch4(L.value, S, v);
+                    uint32_t h[kItems] = {0, 0, 0, 0};
+#pragma unroll
+                    for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+                        if (kk < L.n_keys) {
+                            int32_t kv[kItems];
+                            fetch4(L.keys[kk], S, kv);
+#pragma unroll
+                            for (int k = 0; k < kItems; k++) h[k] += ((uint32_t)kv[k] - (uint32_t)L.key_min[kk]) * L.mults[kk];
+                        }
+#pragma unroll
+                    for (int k = 0; k < kItems; k++)
+                        if ((S.live >> k) & 1u)
+                            group_row(L, s_key, s_sum, direct, h[k], v[k], [&](int kk) {
+                                int32_t kv[kItems];
+                                fetch4(L.keys[kk], S, kv);
+                                return kv[k];
+                            });
+                }
+            }
+        }
+        st = (st + 1) % kStages;
+    }
+    cp_async_wait<0>();
+
+    if (TERM == T_SUM) {
+        __shared__ uint64_t part[kThreads / 32];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t t = 0;
+            for (int w = 0; w < kThreads / 32; w++) t += part[w];
+            if (t) atomicAdd(reinterpret_cast<unsigned long long *>(L.sum_out), (unsigned long long)t);
+        }
+    } else if (TERM == T_GROUP) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < kDenseCap; i += blockDim.x) {
+            const uint32_t k = s_key[i];
+            if (k != kEmpty) atomicAdd(reinterpret_cast<unsigned long long *>(&L.out_sum[k]), s_sum[i]);
+        }
+    }
+}
+
+template <int TERM, int NREGS, int SPLIT, int... KS>
+int launch(const Launch &L, cudaStream_t s)
+{
+    auto kern = k_dense<TERM, NREGS, SPLIT, KS...>;
+    const int ring = kStages * kSlots * kThreads * (int)sizeof(int4);
+    const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
+        attr = true;
+    }
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1) per_sm = 1;
-    const uint64_t groups = (L.d.n + 3) / 4;
-    uint64_t blocks = (groups + kThreads - 1) / kThreads;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const uint64_t tile = (uint64_t)kThreads * kItems;
+    uint64_t blocks = (L.n + tile - 1) / tile;
     const uint64_t cap = (uint64_t)num_sms() * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(L);
-    return sdb_check_launch("sdb_fused_chain");
+    return sdb_check_launch("sdb_fused_chain (dense)");
 }
 
-template <int TERM>
-int launch_regs(const ChainLaunch &L, int nregs, cudaStream_t s)
+// Converts a checked chain into a dense launch.  Returns false when the chain
+// reads more than kSlots distinct columns, has too many ops or registers.
+bool convert(const ChainLaunch &C, int nregs, Launch &D)
 {
-    if (nregs <= 2) return launch_term<TERM, 2>(L, s);
-    if (nregs <= 4) return launch_term<TERM, 4>(L, s);
-    return launch_term<TERM, 8>(L, s);
+    const sdb_chain_desc &c = C.d;
+    if (c.n_ops > kMaxOps || nregs > 2) return false;
+    std::memset(&D, 0, sizeof D);
+    D.n = c.n;
+    D.flags_in = c.flags_in;
+    D.flags_out = c.flags_out;
+    D.n_ops = c.n_ops;
+    auto map = [&](const sdb_operand &o, Src &out) -> bool {
+        out.src = o.kind == SDB_SRC_COL ? 0 : (o.kind == SDB_SRC_REG ? 1 : 2);
+        out.lit = o.lit;
+        out.idx = o.reg;
+        if (o.kind == SDB_SRC_COL) {
+            int i = 0;
+            while (i < D.nslot && D.slot[i] != o.col) i++;
+            if (i == D.nslot) {
+                if (D.nslot == kSlots || !sdb::aligned(o.col, 16)) return false;
+                D.slot[D.nslot++] = o.col;
+            }
+            out.idx = i;
+        }
+        return true;
+    };
+    for (int k = 0; k < c.n_ops; k++) {
+        const sdb_chain_op &o = c.ops[k];
+        Op &d = D.ops[k];
+        d.kind = o.kind;
+        d.cmp = o.cmp_op;
+        d.logic = o.logic_op;
+        d.bin = o.bin_op;
+        d.lo = o.lo;
+        d.hi = o.hi;
+        d.out_reg = o.out_reg;
+        d.ht = o.ht;
+        d.out_col = o.out_col;
+        if (o.kind == SDB_OP_SEMI_PROBE && !D.bitmap_ht) {
+            const uint64_t len = (uint64_t)((int64_t)o.hi - (int64_t)o.lo + 1);
+            if (len >= 1 && len <= kBitmapMax) {
+                D.bitmap_ht = static_cast<const uint8_t *>(o.ht);
+                D.bitmap_len = (uint32_t)len;
+                d.smem_bits = 1;
+            }
+        }
+        const bool uses_b = o.kind == SDB_OP_SELECT || o.kind == SDB_OP_BINOP;
+        if (o.kind != SDB_OP_FILL && !map(o.a, d.a)) return false;
+        if (o.kind == SDB_OP_FILL) { d.a.src = 2; d.a.lit = o.a.lit; }
+        if (uses_b && !map(o.b, d.b)) return false;
+    }
+    if (c.terminal != SDB_TERM_FLAGS && !map(c.value, D.value)) return false;
+    D.sum_out = c.sum_out;
+    if (c.terminal == SDB_TERM_GROUPBY) {
+        D.n_keys = c.n_keys;
+        for (int j = 0; j < c.n_keys; j++) {
+            if (!map(c.keys[j], D.keys[j])) return false;
+            D.key_min[j] = c.key_min[j];
+            D.mults[j] = C.mults[j];
+            D.out_keys[j] = c.out_keys[j];
+        }
+    }
+    D.P = c.P;
+    D.out_sum = c.out_sum;
+    D.occ = c.occ;
+    return true;
 }
+
+// Instantiated shapes.  Returns SDB_ERR_UNSUPPORTED (without launching) for
+// any other chain.
+// Whether the ops from index `split` on can run on compacted rows: no flags
+// output, and every later op only keeps or clears a row's flag (no NONE/OR
+// selection, no literal fill); ops before the split produce no register.
+bool can_compact(const Launch &D, int term, int split)
+{
+    if (term == T_FLAGS || D.flags_out || split < 1 || split > D.n_ops) return false;
+    for (int i = 0; i < D.n_ops; i++) {
+        const Op &o = D.ops[i];
+        const bool makes_reg = o.kind == SDB_OP_FULL_PROBE || o.kind == SDB_OP_BINOP || o.kind == SDB_OP_FILL;
+        if (i < split && makes_reg) return false;
+        if (i >= split) {
+            if (o.kind == SDB_OP_FILL) return false;
+            if ((o.kind == SDB_OP_SELECT || o.kind == SDB_OP_SEARCH_RANGE || o.kind == SDB_OP_SEARCH_POINTS) &&
+                o.logic != SDB_AND)
+                return false;
+        }
+    }
+    return true;
+}
+
+// Instantiated shapes.  Returns SDB_ERR_UNSUPPORTED (without launching) for
+// any other chain.  `compact`: 1 = compact after the first op when allowed.
+int dispatch(const ChainLaunch &C, int nregs, int term, int compact, cudaStream_t s)
+{
+    Launch D;
+    if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
+    int k[kMaxOps];
+    for (int i = 0; i < D.n_ops; i++) k[i] = D.ops[i].kind;
+    const int n = D.n_ops;
+    const bool c1 = compact && can_compact(D, term, 1);
+    // star join: semi + full + full -> group-by (SSB flight 2)
+    if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_FULL_PROBE)
+        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, s)
+                  : launch<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, s);
+    // full + full -> group-by
+    if (term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
+        return launch<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, s);
+    // range filter + one join + projection -> group-by
+    if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_BINOP)
+        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, s)
+                  : launch<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, s);
+    // filter-project-sum (SSB flight 1)
+    if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE && k[2] == SDB_OP_SELECT &&
+        k[3] == SDB_OP_BINOP)
+        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, s)
+                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, s);
+    if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
+        k[2] == SDB_OP_SEARCH_RANGE && k[3] == SDB_OP_BINOP)
+        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, s)
+                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, s);
+    return SDB_ERR_UNSUPPORTED;
+}
+
+}  // namespace dense
+
+// Tuning table: variant per (terminal, register class, log2 rows bucket);
+// -1 = default.  Set by sdb_chain_tune_set (the autotuner persists its
+// choices and loads them at start-up).
+int g_tune[3][3][40];
+bool g_tune_init = false;
+
+int reg_class(int nregs) { return nregs <= 2 ? 0 : (nregs <= 4 ? 1 : 2); }
+int rows_bucket(uint64_t n)
+{
+    int b = 0;
+    while (b < 39 && (1ull << (b + 1)) <= n) b++;
+    return b;
+}
+
+int default_variant(int nregs) { return nregs <= 4 ? 1 : 0; }
+
+constexpr int kDenseVariant = 3;
+constexpr int kCompactVariant = 4;
 
 bool operand_ok(const sdb_operand &o, int &nregs, bool &vec, const char **why)
 {
@@ -471,7 +1192,7 @@ int sdb_chain_prepare(const sdb_chain_desc *c, void *launch_out, size_t launch_b
             L.mults[j] = mult;
             mult *= (uint32_t)c->key_max[j] - (uint32_t)c->key_min[j] + 1u;
         }
-        *term_out = c->P <= kSmemSlotsMax ? T_GROUP_SMEM : T_GROUP_GLOBAL;
+        *term_out = T_GROUP;
         break;
     }
     default:
@@ -488,7 +1209,7 @@ bad:
 
 size_t sdb_chain_launch_bytes() { return sizeof(ChainLaunch); }
 
-extern "C" int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream)
+static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream_t stream)
 {
     ChainLaunch L;
     int nregs = 1, term = 0;
@@ -496,10 +1217,62 @@ extern "C" int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream)
     if (st != SDB_OK) return st;
     if (L.d.n == 0) return SDB_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    if (variant < 0) {
+        if (!g_tune_init) {
+            memset(g_tune, 0xff, sizeof g_tune);
+            g_tune_init = true;
+        }
+        variant = g_tune[term][reg_class(nregs)][rows_bucket(L.d.n)];
+        if (variant < 0) variant = kCompactVariant;  // shape-specialised pass when one exists
+    }
+    if (variant == kDenseVariant || variant == kCompactVariant) {
+        const int st2 = dense::dispatch(L, nregs, term, variant == kCompactVariant, s);
+        if (st2 != SDB_ERR_UNSUPPORTED) return st2;
+        variant = default_variant(nregs);
+    }
     switch (term) {
-    case T_FLAGS: return launch_regs<T_FLAGS>(L, nregs, s);
-    case T_SUM: return launch_regs<T_SUM>(L, nregs, s);
-    case T_GROUP_SMEM: return launch_regs<T_GROUP_SMEM>(L, nregs, s);
-    default: return launch_regs<T_GROUP_GLOBAL>(L, nregs, s);
+    case T_FLAGS: return launch_regs<T_FLAGS>(L, nregs, variant, s);
+    case T_SUM: return launch_regs<T_SUM>(L, nregs, variant, s);
+    default: return launch_regs<T_GROUP>(L, nregs, variant, s);
     }
 }
+
+extern "C" {
+
+int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream) { return fused_chain_impl(chain, -1, stream); }
+
+int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream)
+{
+    if (variant < 0 || variant > 4) return sdb_set_error(SDB_ERR_INVALID, "sdb_fused_chain_variant: variant %d", variant);
+    return fused_chain_impl(chain, variant, stream);
+}
+
+int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant)
+{
+    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS || variant < -1 || variant > 4)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_tune_set: bad argument");
+    if (!g_tune_init) {
+        memset(g_tune, 0xff, sizeof g_tune);
+        g_tune_init = true;
+    }
+    g_tune[terminal][reg_class(nregs)][rows_bucket(rows)] = variant;
+    return SDB_OK;
+}
+
+int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows)
+{
+    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS) return -1;
+    if (!g_tune_init) return kCompactVariant;
+    int v = g_tune[terminal][reg_class(nregs)][rows_bucket(rows)];
+    return v < 0 ? kCompactVariant : v;
+}
+
+int sdb_chain_registers(const sdb_chain_desc *chain)
+{
+    ChainLaunch L;
+    int nregs = 1, term = 0;
+    int st = sdb_chain_prepare(chain, &L, sizeof L, &nregs, &term);
+    return st != SDB_OK ? st : nregs;
+}
+
+}  // extern "C"

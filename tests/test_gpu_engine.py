@@ -130,3 +130,19 @@ def test_star_sf20_full_size():
     assert 200 <= len(want) <= 280
     del fact
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4])
+def test_every_kernel_variant_matches_golden(variant):
+    """The general pass at 4/8/16 rows per thread and the shape-specialised
+    pass give the same rows."""
+    try:
+        capi.force_chain_variant(variant)
+        for case in PLANS:
+            ds = datasets.dataset(case["sf"], case["seed"])
+            with Engine(arena_bytes=1 << 30, fuse=True) as eng:
+                load(eng, ds)
+                got = eng.execute(case["plan"]).canonical()
+            assert [list(r) for r in got] == case["rows"], (variant, case["name"])
+    finally:
+        capi.force_chain_variant(-1)
