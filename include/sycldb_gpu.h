@@ -264,8 +264,9 @@ int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream);
  * chain shapes; every chain column of the next tiles is staged in shared
  * memory by asynchronous copies while the current tile is probed).  4: as 3,
  * and after the first op each warp compacts its surviving rows so that the
- * remaining ops run one row per lane.  Shapes without a specialised pass fall
- * back to the general pass.  Default (and an unset tuning entry): 4. */
+ * remaining ops run one row per lane.  5: as 4 with a 2-stage copy ring (less
+ * shared memory, more resident blocks).  Shapes without a specialised pass
+ * fall back to the general pass.  Default (and an unset tuning entry): 5. */
 int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream);
 /* Tuning table used by sdb_fused_chain: variant for chains with this
  * terminal (sdb_chain_terminal), register count and row count (bucketed by

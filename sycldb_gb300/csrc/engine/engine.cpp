@@ -613,26 +613,53 @@ struct Engine {
     Profiler prof;
     double last_plan_ms = 0;
     cudaEvent_t plan_a = nullptr, plan_b = nullptr;
-    // flag buffers known to hold all-true (filled at TransientTable creation
-    // and not written since)
+    // Segment flag buffers that hold all-true: a TransientTable's initial
+    // flags (transient_table.hpp:86,105), not written since.  The fill itself
+    // is deferred until some kernel reads the buffer (`unfilled`), so a fused
+    // pass that treats the buffer as all-true never pays for it.
     std::set<const uint8_t *> all_true;
+    std::map<const uint8_t *, uint64_t> unfilled;
+
+    void ensure_filled(const uint8_t *p)
+    {
+        auto it = unfilled.find(p);
+        if (it == unfilled.end()) return;
+        cudaEvent_t a = nullptr;
+        prof.begin(stream, "fill_flags", a);
+        check(sdb_fill_u8(const_cast<uint8_t *>(p), it->second, 1, (sdb_stream_t)stream));
+        prof.end(stream);
+        unfilled.erase(it);
+    }
+
+    void written(const uint8_t *p)
+    {
+        all_true.erase(p);
+        unfilled.erase(p);
+    }
 
     void run_kernel(const KernelData &k)
     {
+        // A selection or logical combine with logic NONE overwrites its
+        // input (selection.hpp:83-96), so it does not need the fill.
+        const bool ignores_in = (k.type == KernelType::SelectionKernelLiteral ||
+                                 k.type == KernelType::SelectionKernelColumns || k.type == KernelType::LogicalKernel) &&
+                                k.logic == SDB_NONE;
+        if (k.in && !ignores_in) ensure_filled(k.in);
         cudaEvent_t a = nullptr;
         prof.begin(stream, kernel_name(k.type), a);
         check(k.execute(stream));
         prof.end(stream);
-        if (k.out) all_true.erase(k.out);
+        if (k.out) written(k.out);
     }
 
     void run_chain(const sdb_chain_desc &c)
     {
+        if (c.flags_in) ensure_filled(c.flags_in);
         cudaEvent_t a = nullptr;
         prof.begin(stream, "fused_chain", a);
         check(sdb_fused_chain(&c, (sdb_stream_t)stream));
         prof.end(stream);
-        if (c.flags_out) all_true.erase(c.flags_out);
+        if (c.flags_out) written(c.flags_out);
     }
 
     // KernelBundle::execute for one segment, fusing runs when enabled.
@@ -672,8 +699,10 @@ public:
     TransientTable(Engine &e, Table *base) : E(e), nrows(base->nrows)
     {
         flags = E.mm.alloc<uint8_t>(nrows);
-        check(sdb_fill_u8(flags, nrows, 1, (sdb_stream_t)E.stream));
-        E.all_true.insert(flags);
+        for (auto [start, cnt] : split_rows(nrows, E.seg)) {
+            E.all_true.insert(flags + start);
+            E.unfilled[flags + start] = cnt;
+        }
         for (Column &c : base->columns) current_columns.push_back(&c);
     }
 
@@ -1340,6 +1369,7 @@ std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text
 
     E.mm.reset(E.stream);
     E.all_true.clear();
+    E.unfilled.clear();
     if (E.cfg.profile) E.prof.stats.clear();
     SDB_CUDA(cudaEventRecord(E.plan_a, E.stream));
 
@@ -1429,6 +1459,7 @@ std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text
         o.count = E.mm.alloc<uint32_t>(1);
         size_t sb = sdb_compact_scratch_bytes(cnt);
         void *scratch = E.mm.alloc<uint8_t>(sb);
+        E.ensure_filled(fin.flags + sg[s].first);
         check(sdb_compact_row_ids(fin.flags + sg[s].first, cnt, ids, o.count, scratch, sb, (sdb_stream_t)E.stream));
         for (Column *c : cols) {
             const Segment &seg = c->segments[s];

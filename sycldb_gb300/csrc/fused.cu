@@ -434,6 +434,12 @@ int launch_regs(const ChainLaunch &L, int nregs, int variant, cudaStream_t s)
 // bandwidth at 4 B per column per row.
 namespace dense {
 
+// lo <= a <= hi as one unsigned compare (lo <= hi).
+__device__ __forceinline__ bool in_range(int32_t a, int32_t lo, int32_t hi)
+{
+    return (uint32_t)a - (uint32_t)lo <= (uint32_t)hi - (uint32_t)lo;
+}
+
 constexpr int kItems = 4;
 constexpr int kSlots = 4;
 constexpr int kMaxOps = 8;
@@ -477,14 +483,15 @@ struct Launch {
 
 // Largest semi-join table staged as a shared-memory bitmap (32 KB of bits).
 constexpr uint32_t kBitmapMax = 1u << 18;
-// Block-private group-by table of the specialised pass (12 KB).
-constexpr uint32_t kDenseCap = 1024;
+// Block-private group-by table of the specialised pass (6 KB): small enough
+// for five resident blocks per SM; a group-by has few live slots per block.
+constexpr uint32_t kDenseCap = 512;
 
 // Tile rows are staged in shared memory by cp.async: thread t's four rows
 // (tile + 4t .. 4t + 3) of every chain column arrive as one 16-byte copy per
 // column into a kStages-deep ring, issued kStages - 1 tiles ahead.  Each
 // thread reads back only what it copied, so no block barrier is needed.
-constexpr int kStages = 3;
+constexpr int kMaxStages = 3;
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint32_t src_bytes)
 {
@@ -559,7 +566,7 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         for (int k = 0; k < kItems; k++) {
             bool c;
             if (K == SDB_OP_SELECT) c = sdb::compare(op.cmp, a[k], b[k]);
-            else if (K == SDB_OP_SEARCH_RANGE) c = a[k] >= op.lo && a[k] <= op.hi;
+            else if (K == SDB_OP_SEARCH_RANGE) c = in_range(a[k], op.lo, op.hi);
             else c = a[k] == op.lo || a[k] == op.hi;
             m |= (uint32_t)c << k;
         }
@@ -572,7 +579,7 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         if (op.smem_bits) {
 #pragma unroll
             for (int k = 0; k < kItems; k++)
-                if (((S.live >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) {
+                if (((S.live >> k) & 1u) && in_range(a[k], op.lo, op.hi)) {
                     const uint32_t h = (uint32_t)a[k] - (uint32_t)op.lo;
                     m |= ((S.bits[h >> 5] >> (h & 31u)) & 1u) << k;
                 }
@@ -581,7 +588,7 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
 #pragma unroll
             for (int k = 0; k < kItems; k++) {
                 h[k] = 0;
-                if (((S.live >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi)
+                if (((S.live >> k) & 1u) && in_range(a[k], op.lo, op.hi))
                     h[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
             }
 #pragma unroll
@@ -596,7 +603,7 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
 #pragma unroll
         for (int k = 0; k < kItems; k++) {
             e[k] = make_int2(0, 0);
-            if (((S.live >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi)
+            if (((S.live >> k) & 1u) && in_range(a[k], op.lo, op.hi))
                 e[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
         }
         uint32_t m = 0;
@@ -665,14 +672,13 @@ __device__ __forceinline__ void step1(const Op &op, Row<NREGS> &R, const uint32_
     if (K == SDB_OP_SELECT) {
         R.live = sdb::compare(op.cmp, fetch1(op.a, R), fetch1(op.b, R));
     } else if (K == SDB_OP_SEARCH_RANGE) {
-        const int32_t a = fetch1(op.a, R);
-        R.live = a >= op.lo && a <= op.hi;
+        R.live = in_range(fetch1(op.a, R), op.lo, op.hi);
     } else if (K == SDB_OP_SEARCH_POINTS) {
         const int32_t a = fetch1(op.a, R);
         R.live = a == op.lo || a == op.hi;
     } else if (K == SDB_OP_SEMI_PROBE) {
         const int32_t a = fetch1(op.a, R);
-        if (a < op.lo || a > op.hi) {
+        if (!in_range(a, op.lo, op.hi)) {
             R.live = false;
         } else {
             const uint32_t h = (uint32_t)a - (uint32_t)op.lo;
@@ -681,7 +687,7 @@ __device__ __forceinline__ void step1(const Op &op, Row<NREGS> &R, const uint32_
         }
     } else if (K == SDB_OP_FULL_PROBE) {
         const int32_t a = fetch1(op.a, R);
-        if (a < op.lo || a > op.hi) {
+        if (!in_range(a, op.lo, op.hi)) {
             R.live = false;
         } else {
             const int2 e = __ldg(static_cast<const int2 *>(op.ht) + ((uint32_t)a - (uint32_t)op.lo));
@@ -735,9 +741,13 @@ __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsi
 // SPLIT = number of ops run on 4-row groups; the rest run on the compacted
 // rows.  SPLIT == sizeof...(KS) + 1 means no compaction (all ops dense, which
 // also serves SDB_TERM_FLAGS).
-template <int TERM, int NREGS, int SPLIT, int... KS>
-__global__ void __launch_bounds__(kThreads, 3) k_dense(const __grid_constant__ Launch L)
+template <int STAGES>
+__host__ __device__ constexpr int dense_min_blocks() { return STAGES >= 3 ? 3 : 5; }
+
+template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(const __grid_constant__ Launch L)
 {
+    constexpr int kStages = STAGES;
     constexpr int N = sizeof...(KS);
     constexpr bool kCompact = SPLIT <= N;
     constexpr int kDenseOps = kCompact ? SPLIT : N;
@@ -924,11 +934,11 @@ __global__ void __launch_bounds__(kThreads, 3) k_dense(const __grid_constant__ L
     }
 }
 
-template <int TERM, int NREGS, int SPLIT, int... KS>
-int launch(const Launch &L, cudaStream_t s)
+template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+int launch_stages(const Launch &L, cudaStream_t s)
 {
-    auto kern = k_dense<TERM, NREGS, SPLIT, KS...>;
-    const int ring = kStages * kSlots * kThreads * (int)sizeof(int4);
+    auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, KS...>;
+    const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
     static bool attr = false;
     if (!attr) {
@@ -945,6 +955,12 @@ int launch(const Launch &L, cudaStream_t s)
     if (blocks == 0) blocks = 1;
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(L);
     return sdb_check_launch("sdb_fused_chain (dense)");
+}
+
+template <int TERM, int NREGS, int SPLIT, int... KS>
+int launch(const Launch &L, int stages, cudaStream_t s)
+{
+    return stages >= 3 ? launch_stages<TERM, NREGS, 3, SPLIT, KS...>(L, s) : launch_stages<TERM, NREGS, 2, SPLIT, KS...>(L, s);
 }
 
 // Converts a checked chain into a dense launch.  Returns false when the chain
@@ -1039,7 +1055,7 @@ bool can_compact(const Launch &D, int term, int split)
 
 // Instantiated shapes.  Returns SDB_ERR_UNSUPPORTED (without launching) for
 // any other chain.  `compact`: 1 = compact after the first op when allowed.
-int dispatch(const ChainLaunch &C, int nregs, int term, int compact, cudaStream_t s)
+int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, cudaStream_t s)
 {
     Launch D;
     if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
@@ -1049,24 +1065,24 @@ int dispatch(const ChainLaunch &C, int nregs, int term, int compact, cudaStream_
     const bool c1 = compact && can_compact(D, term, 1);
     // star join: semi + full + full -> group-by (SSB flight 2)
     if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_FULL_PROBE)
-        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, s)
-                  : launch<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, s);
+        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, stages, s)
+                  : launch<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, stages, s);
     // full + full -> group-by
     if (term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
-        return launch<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, s);
+        return launch<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, stages, s);
     // range filter + one join + projection -> group-by
     if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_BINOP)
-        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, s)
-                  : launch<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, s);
+        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, stages, s)
+                  : launch<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, stages, s);
     // filter-project-sum (SSB flight 1)
     if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE && k[2] == SDB_OP_SELECT &&
         k[3] == SDB_OP_BINOP)
-        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, s)
-                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, s);
+        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, stages, s)
+                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, stages, s);
     if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
         k[2] == SDB_OP_SEARCH_RANGE && k[3] == SDB_OP_BINOP)
-        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, s)
-                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, s);
+        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, stages, s)
+                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, stages, s);
     return SDB_ERR_UNSUPPORTED;
 }
 
@@ -1090,6 +1106,7 @@ int default_variant(int nregs) { return nregs <= 4 ? 1 : 0; }
 
 constexpr int kDenseVariant = 3;
 constexpr int kCompactVariant = 4;
+constexpr int kCompact2Variant = 5;  // as 4 with a 2-stage copy ring
 
 bool operand_ok(const sdb_operand &o, int &nregs, bool &vec, const char **why)
 {
@@ -1223,10 +1240,10 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
             g_tune_init = true;
         }
         variant = g_tune[term][reg_class(nregs)][rows_bucket(L.d.n)];
-        if (variant < 0) variant = kCompactVariant;  // shape-specialised pass when one exists
+        if (variant < 0) variant = kCompact2Variant;  // shape-specialised pass when one exists
     }
-    if (variant == kDenseVariant || variant == kCompactVariant) {
-        const int st2 = dense::dispatch(L, nregs, term, variant == kCompactVariant, s);
+    if (variant >= kDenseVariant) {
+        const int st2 = dense::dispatch(L, nregs, term, variant != kDenseVariant, variant == kCompact2Variant ? 2 : 3, s);
         if (st2 != SDB_ERR_UNSUPPORTED) return st2;
         variant = default_variant(nregs);
     }
@@ -1243,13 +1260,13 @@ int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream) { return f
 
 int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream)
 {
-    if (variant < 0 || variant > 4) return sdb_set_error(SDB_ERR_INVALID, "sdb_fused_chain_variant: variant %d", variant);
+    if (variant < 0 || variant > 5) return sdb_set_error(SDB_ERR_INVALID, "sdb_fused_chain_variant: variant %d", variant);
     return fused_chain_impl(chain, variant, stream);
 }
 
 int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant)
 {
-    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS || variant < -1 || variant > 4)
+    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS || variant < -1 || variant > 5)
         return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_tune_set: bad argument");
     if (!g_tune_init) {
         memset(g_tune, 0xff, sizeof g_tune);
@@ -1262,9 +1279,9 @@ int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant)
 int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows)
 {
     if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS) return -1;
-    if (!g_tune_init) return kCompactVariant;
+    if (!g_tune_init) return kCompact2Variant;
     int v = g_tune[terminal][reg_class(nregs)][rows_bucket(rows)];
-    return v < 0 ? kCompactVariant : v;
+    return v < 0 ? kCompact2Variant : v;
 }
 
 int sdb_chain_registers(const sdb_chain_desc *chain)
