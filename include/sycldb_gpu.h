@@ -164,6 +164,26 @@ size_t sdb_compact_scratch_bytes(uint64_t n);
 int sdb_compact_row_ids(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t *count,
                         void *scratch, size_t scratch_bytes, sdb_stream_t stream);
 
+/* K14 without any allocation -- no counterpart in the reference.
+ * Some callers cannot allocate device memory for scratch: executors whose
+ * device memory all belongs to a pool they manage themselves (as the
+ * reference's memory_manager reserves every byte up front), serving loops that
+ * must not call cudaMalloc/cudaFree because those calls can synchronise the
+ * whole device, or callers already at their memory budget.  This entry takes
+ * the same arguments as sdb_compact_row_ids minus the scratch and returns the
+ * same ids and count; its scratch is a fixed 256 KB array inside the library
+ * (resident on every device that loads the library until the process
+ * exits), so n is limited to SDB_COMPACT_NOALLOC_MAX_ROWS (one 2^28-row
+ * segment); larger n is refused with SDB_ERR_INVALID.  The first call on a
+ * device looks up that array's device address (a one-time set-up per device,
+ * done with the device current); make that first call before any stream
+ * capture.  All calls on a device share the array, so calls that overlap on
+ * the GPU (different streams, no ordering between them) race and must not be
+ * issued.  It calls no allocator. */
+#define SDB_COMPACT_NOALLOC_MAX_ROWS 268435456ull
+int sdb_compact_row_ids_noalloc(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t *count,
+                                sdb_stream_t stream);
+
 /* K15: dst[i] = src[ids[i]] for i < *count (count is a device word, cap
  * bounds it).  Replaces the gather of Segment::compress_sync
  * (models/models.hpp:1019-1063). */

@@ -85,6 +85,7 @@ _SIGS = {
     "sdb_probe_full": (c_int, [_P, _P, _P, _P, c_uint64, _P, c_int32, c_int32, _P]),
     "sdb_compact_scratch_bytes": (c_size_t, [c_uint64]),
     "sdb_compact_row_ids": (c_int, [_P, c_uint64, _P, _P, _P, c_size_t, _P]),
+    "sdb_compact_row_ids_noalloc": (c_int, [_P, c_uint64, _P, _P, _P]),
     "sdb_gather_i32": (c_int, [_P, _P, _P, _P, c_uint64, _P]),
     "sdb_gather_u64": (c_int, [_P, _P, _P, _P, c_uint64, _P]),
     "sdb_count_flags": (c_int, [_P, c_uint64, _P, _P]),

@@ -8,6 +8,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <initializer_list>
+#include <mutex>
 #include <thread>
 #include <vector>
 
@@ -852,6 +853,56 @@ int sdb_compact_row_ids(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t
     k_compact_write<<<grid, kThreads, 0, s>>>(flags, n, bc, nchunks, ids);
     sdb_count_launches(2);
     return sdb_check_launch("sdb_compact_row_ids");
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- no-allocation compaction
+// Scratch of sdb_compact_row_ids_noalloc: the per-chunk counts for one
+// segment of up to SDB_COMPACT_NOALLOC_MAX_ROWS rows (256 KB).  It lives in
+// the library's own device image, so every device that loads the library
+// holds it until the process exits, and every call on that device shares it.
+static __device__ __align__(256) uint32_t g_noalloc_compact_scratch[SDB_COMPACT_NOALLOC_MAX_ROWS / kCompactChunk];
+
+namespace {
+constexpr int kNoAllocMaxDevices = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_scratch_ptr[kNoAllocMaxDevices];  // device address of the array, per device (set up once)
+}  // namespace
+
+extern "C" {
+
+int sdb_compact_row_ids_noalloc(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t *count, sdb_stream_t stream)
+{
+    if (n > SDB_COMPACT_NOALLOC_MAX_ROWS)
+        return sdb_set_error(SDB_ERR_INVALID,
+                             "sdb_compact_row_ids_noalloc: %llu rows exceed the fixed scratch (at most %llu rows per call)",
+                             (unsigned long long)n, (unsigned long long)SDB_COMPACT_NOALLOC_MAX_ROWS);
+    if (n == 0) return sdb_compact_row_ids(flags, 0, ids, count, nullptr, 0, stream);
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return sdb_set_error(SDB_ERR_CUDA, "sdb_compact_row_ids_noalloc: cudaGetDevice: %s", cudaGetErrorString(e));
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_row_ids_noalloc: device %d beyond the supported %d", dev,
+                             kNoAllocMaxDevices);
+    void *scratch = nullptr;
+    {
+        // Set-up, once per device, with that device current: the host-side
+        // name of the array is not a device address, so ask the runtime for it.
+        std::lock_guard<std::mutex> lk(g_noalloc_mu);
+        if (!g_noalloc_scratch_ptr[dev]) {
+            void *p = nullptr;
+            e = cudaGetSymbolAddress(&p, g_noalloc_compact_scratch);
+            if (e != cudaSuccess || !p)
+                return sdb_set_error(SDB_ERR_CUDA, "sdb_compact_row_ids_noalloc: cudaGetSymbolAddress: %s",
+                                     cudaGetErrorString(e));
+            g_noalloc_scratch_ptr[dev] = p;
+        }
+        scratch = g_noalloc_scratch_ptr[dev];
+    }
+    // Every count the passes read is written first by k_compact_count, so the
+    // array needs no clearing between calls.
+    return sdb_compact_row_ids(flags, n, ids, count, scratch, sizeof(g_noalloc_compact_scratch), stream);
 }
 
 int sdb_gather_i32(const int32_t *src, const int32_t *ids, const uint32_t *count, int32_t *dst, uint64_t cap,
