@@ -296,6 +296,31 @@ int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows);
 /* Registers (1..8) a chain needs, or a negative status if it is invalid. */
 int sdb_chain_registers(const sdb_chain_desc *chain);
 
+/* ------------------------------------------------------------ chain batches
+ * Many fused chains in one persistent launch per chain shape.  No counterpart
+ * in the reference, which runs one plan at a time (executor/ddor_executor.cpp:
+ * 22-245); the results are those of calling sdb_fused_chain on each chain in
+ * turn.  Chains are grouped by the kernel instantiation they map to; each
+ * group's (chain, tile range) spans go to one launch whose blocks pull spans
+ * from a device work queue.  Chains without a batched instantiation are
+ * launched one by one by sdb_chain_batch_launch.
+ *
+ * sdb_chain_batch_create checks every chain, writes the batch's tables into
+ * `dev_scratch` (sdb_chain_batch_scratch_bytes(chains, n) bytes, 256-byte
+ * aligned) and waits for that copy on `stream`, so it must not run under
+ * stream capture.  sdb_chain_batch_launch issues one memset and the kernels,
+ * nothing else; the chains' buffers must stay valid and their outputs be
+ * zeroed (group-by slots, sums) before each launch.  Launches of one batch
+ * must not overlap: they share the work-queue heads in `dev_scratch`. */
+typedef struct sdb_chain_batch sdb_chain_batch;
+size_t sdb_chain_batch_scratch_bytes(const sdb_chain_desc *chains, int n_chains);
+int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
+                           sdb_stream_t stream, sdb_chain_batch **out);
+int sdb_chain_batch_launch(const sdb_chain_batch *batch, sdb_stream_t stream);
+/* Kernel launches one sdb_chain_batch_launch makes (the memset excluded). */
+int sdb_chain_batch_kernels(const sdb_chain_batch *batch);
+void sdb_chain_batch_destroy(sdb_chain_batch *batch);
+
 /* ------------------------------------------------------ synthetic SSB data */
 
 /* Counter-based generator shared by host and device: value of row `row` of
@@ -371,6 +396,51 @@ int sdb_engine_kernel_stats(const sdb_engine *eng, int k, const char **name, uin
                             double *total_ms);
 /* Device milliseconds of the last execute (CUDA events around the plan). */
 int sdb_engine_last_plan_ms(const sdb_engine *eng, double *ms);
+
+/* ---------------------------------------------------------------- batches
+ * Many plans prepared once and run together.  No counterpart in the
+ * reference, whose executor runs one plan at a time
+ * (executor/ddor_executor.cpp:22-245); each plan's result is the one
+ * sdb_engine_execute gives for it alone.
+ *
+ * Prepare records every plan's device work without running it (a sizing pass,
+ * then a pass against an arena of exactly the size needed, owned by the
+ * batch), splits each plan at its aggregating fused chain and gathers those
+ * chains into one sdb_chain_batch.  A run replays: the zeroed region is
+ * cleared, the plans' work before their chains runs spread over up to 8
+ * streams, then the chain batch (one persistent launch per chain shape), then
+ * the plans' remaining work and the copies of their results at full capacity
+ * into pinned host staging.  Unless SDB_BATCH_EAGER, the replay is captured
+ * once as a CUDA graph and each run is one graph launch.  The base tables the
+ * plans read must stay loaded, unchanged, while the batch lives.  Runs of one
+ * batch must not overlap; different batches and plain executes may alternate
+ * freely (each batch has its own arena). */
+typedef struct sdb_batch sdb_batch;
+
+#define SDB_BATCH_EAGER 1           /* replay the recorded launches on every run, no graph */
+#define SDB_BATCH_NO_CHAIN_BATCH 2  /* launch every fused chain on its own */
+
+typedef struct sdb_batch_stats {
+    int32_t n_plans;
+    int32_t kernels_per_run;  /* library kernel launches one run makes */
+    int32_t graph;            /* 1: runs are CUDA graph launches */
+    int32_t chain_launches;   /* launches of the chain batch (one per chain shape) */
+    int32_t batched_chains;   /* chains that went into the chain batch */
+    int32_t pad;
+    uint64_t arena_bytes;     /* the batch's device arena */
+    uint64_t zero_bytes;      /* of it, the region cleared on each run */
+    uint64_t host_bytes;      /* pinned staging */
+    double last_run_ms;       /* device milliseconds of the last run */
+} sdb_batch_stats;
+
+int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int n_plans, int flags,
+                             sdb_batch **out);
+/* Runs the batch once and waits for it; results[i] (n_plans entries, may be
+ * NULL to skip the unpacking) receives plan i's result, freed with
+ * sdb_result_free. */
+int sdb_batch_run(sdb_batch *batch, sdb_result **results);
+int sdb_batch_info(const sdb_batch *batch, sdb_batch_stats *info);
+void sdb_batch_free(sdb_batch *batch);
 
 #ifdef __cplusplus
 }

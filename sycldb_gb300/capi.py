@@ -60,6 +60,15 @@ class EngineConfig(ctypes.Structure):
                 ("stream", c_void_p)]
 
 
+class BatchStats(ctypes.Structure):
+    _fields_ = [("n_plans", c_int32), ("kernels_per_run", c_int32), ("graph", c_int32), ("chain_launches", c_int32),
+                ("batched_chains", c_int32), ("pad", c_int32), ("arena_bytes", c_uint64), ("zero_bytes", c_uint64),
+                ("host_bytes", c_uint64), ("last_run_ms", c_double)]
+
+
+SDB_BATCH_EAGER = 1
+SDB_BATCH_NO_CHAIN_BATCH = 2
+
 _P = c_void_p  # device pointers travel as integers
 _SIGS = {
     "sdb_last_error": (c_char_p, []),
@@ -95,6 +104,11 @@ _SIGS = {
     "sdb_chain_tune_set": (c_int, [c_int, c_int, c_uint64, c_int]),
     "sdb_chain_tune_get": (c_int, [c_int, c_int, c_uint64]),
     "sdb_chain_registers": (c_int, [POINTER(ChainDesc)]),
+    "sdb_chain_batch_scratch_bytes": (c_size_t, [POINTER(ChainDesc), c_int]),
+    "sdb_chain_batch_create": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
+    "sdb_chain_batch_launch": (c_int, [c_void_p, _P]),
+    "sdb_chain_batch_kernels": (c_int, [c_void_p]),
+    "sdb_chain_batch_destroy": (None, [c_void_p]),
     "sdb_gen_uniform_host": (c_int32, [c_uint64, c_uint64, c_uint64, c_int32, c_int32]),
     "sdb_gen_uniform": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32, c_int32, _P]),
     "sdb_gen_uniform_cpu": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32, c_int32]),
@@ -112,6 +126,10 @@ _SIGS = {
     "sdb_result_free": (None, [c_void_p]),
     "sdb_engine_kernel_stats": (c_int, [c_void_p, c_int, POINTER(c_char_p), POINTER(c_uint64), POINTER(c_double)]),
     "sdb_engine_last_plan_ms": (c_int, [c_void_p, POINTER(c_double)]),
+    "sdb_engine_batch_prepare": (c_int, [c_void_p, POINTER(c_char_p), c_int, c_int, POINTER(c_void_p)]),
+    "sdb_batch_run": (c_int, [c_void_p, POINTER(c_void_p)]),
+    "sdb_batch_info": (c_int, [c_void_p, POINTER(BatchStats)]),
+    "sdb_batch_free": (None, [c_void_p]),
 }
 
 _LIB = None
@@ -130,7 +148,7 @@ def lib():
             fn.restype = res
             fn.argtypes = args
         for cls, name in ((Operand, "sdb_operand"), (ChainOp, "sdb_chain_op"), (ChainDesc, "sdb_chain_desc"),
-                          (EngineConfig, "sdb_engine_config")):
+                          (EngineConfig, "sdb_engine_config"), (BatchStats, "sdb_batch_stats")):
             n = L.sdb_abi_sizeof(name.encode())
             if n != ctypes.sizeof(cls):
                 raise RuntimeError("ABI mismatch for %s: C %d, ctypes %d" % (name, n, ctypes.sizeof(cls)))

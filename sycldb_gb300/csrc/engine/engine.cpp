@@ -24,6 +24,7 @@
 #include <cstring>
 #include <deque>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <new>
@@ -143,23 +144,59 @@ public:
     MemoryManager() = default;
     ~MemoryManager() { release(); }
 
-    void init(uint64_t budget, cudaStream_t s)
+    void init(uint64_t budget, cudaStream_t s) { init_sized(budget, std::max<uint64_t>(budget >> 6, 1u << 20), s); }
+
+    void init_sized(uint64_t size, uint64_t zsize, cudaStream_t s)
     {
         release();
-        size_ = budget;
-        zsize_ = std::max<uint64_t>(budget >> 6, 1u << 20);
+        size_ = std::max<uint64_t>(size, 256);
+        zsize_ = std::max<uint64_t>(zsize, 256);
         SDB_CUDA(cudaMalloc(&base_, size_));
         SDB_CUDA(cudaMalloc(&zbase_, zsize_));
         SDB_CUDA(cudaMemsetAsync(zbase_, 0, zsize_, s));
-        used_ = zused_ = zdirty_ = 0;
+        used_ = zused_ = zdirty_ = peak_ = 0;
+    }
+
+    // Hands out addresses that are never dereferenced: a sizing pass records
+    // a batch's work without running it, to learn how much memory it needs.
+    void init_virtual()
+    {
+        release();
+        virtual_ = true;
+        base_ = reinterpret_cast<char *>(uintptr_t(1) << 44);
+        zbase_ = reinterpret_cast<char *>(uintptr_t(3) << 44);
+        size_ = zsize_ = uint64_t(1) << 43;
+        used_ = zused_ = zdirty_ = peak_ = 0;
     }
 
     void release()
     {
-        if (base_) cudaFree(base_);
-        if (zbase_) cudaFree(zbase_);
+        if (!virtual_) {
+            if (base_) cudaFree(base_);
+            if (zbase_) cudaFree(zbase_);
+        }
+        virtual_ = false;
         base_ = zbase_ = nullptr;
     }
+
+    void swap(MemoryManager &o)
+    {
+        std::swap(base_, o.base_);
+        std::swap(zbase_, o.zbase_);
+        std::swap(size_, o.size_);
+        std::swap(used_, o.used_);
+        std::swap(peak_, o.peak_);
+        std::swap(zsize_, o.zsize_);
+        std::swap(zused_, o.zused_);
+        std::swap(zdirty_, o.zdirty_);
+        std::swap(virtual_, o.virtual_);
+    }
+
+    uint64_t used() const { return used_; }
+    uint64_t zused() const { return zused_; }
+    uint64_t size() const { return size_; }
+    uint64_t zsize() const { return zsize_; }
+    char *zero_base() const { return zbase_; }
 
     template <typename T>
     T *alloc(uint64_t count)
@@ -204,6 +241,7 @@ private:
     char *base_ = nullptr, *zbase_ = nullptr;
     uint64_t size_ = 0, used_ = 0, peak_ = 0;
     uint64_t zsize_ = 0, zused_ = 0, zdirty_ = 0;
+    bool virtual_ = false;
 };
 
 // ------------------------------------------------------------------ storage
@@ -603,8 +641,28 @@ struct Fuser {
 };
 
 // ------------------------------------------------------------------ engine state
+// Device work recorded instead of run: a batch records every plan's launches,
+// split at the plan's batched chain into the work before it (`pre`) and after
+// it (`post`), and replays them later (eagerly or inside a CUDA graph).
+struct DevOp {
+    const char *name;
+    std::function<int(cudaStream_t)> fn;
+};
+
+struct PlanRecord {
+    std::vector<DevOp> pre, post;
+    bool after = false;  // the plan's batched chain has been recorded
+};
+
+struct Recorder {
+    std::vector<PlanRecord> plans;
+    std::vector<sdb_chain_desc> chains;  // chains for sdb_chain_batch
+    bool batch_chains = true;
+};
+
 struct Engine {
     sdb_engine_config cfg{};
+    Recorder *rec = nullptr;  // non-null: record device work, don't run it
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     uint64_t seg = kDefaultSegment;
@@ -620,14 +678,28 @@ struct Engine {
     std::set<const uint8_t *> all_true;
     std::map<const uint8_t *, uint64_t> unfilled;
 
+    // Every device operation of a plan goes through here: run now on the
+    // engine's stream, or recorded for a batch.
+    void dev(const char *name, std::function<int(cudaStream_t)> fn)
+    {
+        if (rec) {
+            PlanRecord &pr = rec->plans.back();
+            (pr.after ? pr.post : pr.pre).push_back({name, std::move(fn)});
+            return;
+        }
+        cudaEvent_t a = nullptr;
+        prof.begin(stream, name, a);
+        check(fn(stream));
+        prof.end(stream);
+    }
+
     void ensure_filled(const uint8_t *p)
     {
         auto it = unfilled.find(p);
         if (it == unfilled.end()) return;
-        cudaEvent_t a = nullptr;
-        prof.begin(stream, "fill_flags", a);
-        check(sdb_fill_u8(const_cast<uint8_t *>(p), it->second, 1, (sdb_stream_t)stream));
-        prof.end(stream);
+        uint8_t *q = const_cast<uint8_t *>(p);
+        const uint64_t n = it->second;
+        dev("fill_flags", [q, n](cudaStream_t s) { return sdb_fill_u8(q, n, 1, (sdb_stream_t)s); });
         unfilled.erase(it);
     }
 
@@ -645,20 +717,22 @@ struct Engine {
                                  k.type == KernelType::SelectionKernelColumns || k.type == KernelType::LogicalKernel) &&
                                 k.logic == SDB_NONE;
         if (k.in && !ignores_in) ensure_filled(k.in);
-        cudaEvent_t a = nullptr;
-        prof.begin(stream, kernel_name(k.type), a);
-        check(k.execute(stream));
-        prof.end(stream);
+        dev(kernel_name(k.type), [k](cudaStream_t s) { return k.execute(s); });
         if (k.out) written(k.out);
     }
 
     void run_chain(const sdb_chain_desc &c)
     {
         if (c.flags_in) ensure_filled(c.flags_in);
-        cudaEvent_t a = nullptr;
-        prof.begin(stream, "fused_chain", a);
-        check(sdb_fused_chain(&c, (sdb_stream_t)stream));
-        prof.end(stream);
+        PlanRecord *pr = rec ? &rec->plans.back() : nullptr;
+        if (pr && rec->batch_chains && c.terminal != SDB_TERM_FLAGS && pr->post.empty()) {
+            // an aggregating chain goes into the batch's shared launch; the
+            // plan's later work waits for it
+            rec->chains.push_back(c);
+            pr->after = true;
+        } else {
+            dev("fused_chain", [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); });
+        }
         if (c.flags_out) written(c.flags_out);
     }
 
@@ -998,7 +1072,8 @@ public:
             execute_pending_kernels();
             nrows = 1;
             flags = E.mm.alloc<uint8_t>(1);
-            check(sdb_fill_u8(flags, 1, 1, (sdb_stream_t)E.stream));
+            uint8_t *f = flags;
+            E.dev("fill_flags", [f](cudaStream_t s) { return sdb_fill_u8(f, 1, 1, (sdb_stream_t)s); });
             flags_secondary = nullptr;
             Column &rc = materialized_columns.emplace_back();
             rc.is_aggregate_result = true;
@@ -1046,12 +1121,8 @@ public:
         add_pending_kernels(bundles);
         execute_pending_kernels();
         uint8_t *new_flags = E.mm.alloc<uint8_t>(P);
-        {
-            cudaEvent_t a = nullptr;
-            E.prof.begin(E.stream, "occ_to_flags", a);
-            check(sdb_occ_to_flags(temp_flags, new_flags, P, (sdb_stream_t)E.stream));
-            E.prof.end(E.stream);
-        }
+        E.dev("occ_to_flags",
+              [temp_flags, new_flags, P](cudaStream_t s) { return sdb_occ_to_flags(temp_flags, new_flags, P, (sdb_stream_t)s); });
         flags = new_flags;
         flags_secondary = nullptr;
         nrows = P;
@@ -1344,6 +1415,20 @@ ExecutionInfo parse_execution_info(const PlanResult &p)
     return info;
 }
 
+// A plan's result after its last kernel, before it reaches the host: per
+// segment of the final table the device count of qualifying rows and the
+// gathered columns (capacity `cap` rows each).
+struct PendingSeg {
+    uint32_t *count;
+    std::vector<void *> dev;
+    uint64_t cap;
+};
+
+struct PendingResult {
+    std::vector<int> types;  // 0 int32, 1 uint64
+    std::vector<PendingSeg> segs;
+};
+
 }  // namespace sdb
 
 // ====================================================================== results
@@ -1358,20 +1443,58 @@ struct sdb_engine {
     sdb::Engine E;
 };
 
+// A prepared batch: every plan's device work recorded once against the
+// batch's own arena, replayed per run (as one CUDA graph unless eager).
+struct sdb_batch {
+    sdb_engine *eng = nullptr;
+    int flags = 0;
+    sdb::MemoryManager mm;
+    sdb::Recorder rec;
+    std::vector<sdb::PendingResult> pend;
+    sdb_chain_batch *cb = nullptr;
+    char *host = nullptr;  // pinned staging of counts and result columns
+    size_t host_bytes = 0;
+    struct Stage {
+        size_t count_off;
+        std::vector<size_t> col_off;
+    };
+    std::vector<std::vector<Stage>> stage;  // [plan][segment]
+    cudaStream_t bs = nullptr;              // the stream a run goes on
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> join;
+    cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr, ev_in = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int kernels = 0;
+    int chain_groups = 0;
+    double last_ms = 0;
+
+    ~sdb_batch()
+    {
+        if (bs) cudaStreamSynchronize(bs);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (cb) sdb_chain_batch_destroy(cb);
+        for (auto s : side) cudaStreamDestroy(s);
+        for (auto e : join) cudaEventDestroy(e);
+        for (auto e : {fork, ev_a, ev_b, ev_in})
+            if (e) cudaEventDestroy(e);
+        if (bs) cudaStreamDestroy(bs);
+        if (host) cudaFreeHost(host);
+    }
+};
+
 namespace sdb {
 
-// execute_ddor_plan (executor/ddor_executor.cpp:22-245) plus the result
-// materialisation of save_result (executor/result_writer.cpp:12-68).
-std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text)
+// execute_ddor_plan (executor/ddor_executor.cpp:22-245) up to the result
+// materialisation of save_result (executor/result_writer.cpp:12-68): every
+// device operation goes through Engine::dev.  The caller resets the arena.
+PendingResult run_plan(Engine &E, const std::string &plan_text)
 {
     PlanResult plan = plan_from_json(plan_text);
     ExecutionInfo info = parse_execution_info(plan);
-
-    E.mm.reset(E.stream);
     E.all_true.clear();
     E.unfilled.clear();
-    if (E.cfg.profile) E.prof.stats.clear();
-    SDB_CUDA(cudaEventRecord(E.plan_a, E.stream));
 
     std::deque<TransientTable> tts;
     std::vector<int> output_table(plan.rels.size(), -1);
@@ -1431,72 +1554,86 @@ std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text
     TransientTable &fin = tts[output_table[plan.rels.size() - 1]];
     fin.execute_pending_kernels();
 
-    // Materialise the flagged rows of the non-null columns, in row order.
-    auto res = std::make_unique<sdb_result>();
+    // Compact the flagged rows of the non-null columns, in row order.
+    PendingResult pr;
     std::vector<Column *> cols;
     for (Column *c : fin.current_columns)
         if (c) {
             if (c->segments.size() != fin.segs().size()) throw Error(SDB_ERR_INVALID, "result column is not loaded");
             cols.push_back(c);
         }
-    for (Column *c : cols) res->types.push_back(c->is_aggregate_result ? 1 : 0);
-    res->i32.resize(cols.size());
-    res->u64.resize(cols.size());
+    for (Column *c : cols) pr.types.push_back(c->is_aggregate_result ? 1 : 0);
     auto sg = fin.segs();
-    struct SegOut {
-        uint32_t *count;
-        std::vector<void *> dev;
-        uint64_t cap;
-    };
-    std::vector<SegOut> outs;
-    cudaEvent_t pa = nullptr;
-    E.prof.begin(E.stream, "materialize", pa);
     for (size_t s = 0; s < sg.size(); s++) {
         const uint64_t cnt = sg[s].second;
-        SegOut o;
+        PendingSeg o;
         o.cap = cnt;
         int32_t *ids = E.mm.alloc<int32_t>(cnt);
-        o.count = E.mm.alloc<uint32_t>(1);
+        uint32_t *count = E.mm.alloc<uint32_t>(1);
+        o.count = count;
         size_t sb = sdb_compact_scratch_bytes(cnt);
         void *scratch = E.mm.alloc<uint8_t>(sb);
-        E.ensure_filled(fin.flags + sg[s].first);
-        check(sdb_compact_row_ids(fin.flags + sg[s].first, cnt, ids, o.count, scratch, sb, (sdb_stream_t)E.stream));
+        const uint8_t *fl = fin.flags + sg[s].first;
+        E.ensure_filled(fl);
+        E.dev("compact_row_ids", [fl, cnt, ids, count, scratch, sb](cudaStream_t st) {
+            return sdb_compact_row_ids(fl, cnt, ids, count, scratch, sb, (sdb_stream_t)st);
+        });
         for (Column *c : cols) {
             const Segment &seg = c->segments[s];
             if (c->is_aggregate_result) {
                 uint64_t *d = E.mm.alloc<uint64_t>(cnt);
-                check(sdb_gather_u64(seg.agg, ids, o.count, d, cnt, (sdb_stream_t)E.stream));
+                const uint64_t *src = seg.agg;
+                E.dev("gather", [src, ids, count, d, cnt](cudaStream_t st) {
+                    return sdb_gather_u64(src, ids, count, d, cnt, (sdb_stream_t)st);
+                });
                 o.dev.push_back(d);
             } else {
                 int32_t *d = E.mm.alloc<int32_t>(cnt);
-                check(sdb_gather_i32(seg.data, ids, o.count, d, cnt, (sdb_stream_t)E.stream));
+                const int32_t *src = seg.data;
+                E.dev("gather", [src, ids, count, d, cnt](cudaStream_t st) {
+                    return sdb_gather_i32(src, ids, count, d, cnt, (sdb_stream_t)st);
+                });
                 o.dev.push_back(d);
             }
         }
-        outs.push_back(o);
+        pr.segs.push_back(o);
     }
-    E.prof.end(E.stream);
-    std::vector<uint32_t> counts(outs.size());
-    for (size_t s = 0; s < outs.size(); s++)
-        SDB_CUDA(cudaMemcpyAsync(&counts[s], outs[s].count, sizeof(uint32_t), cudaMemcpyDeviceToHost, E.stream));
+    return pr;
+}
+
+std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text)
+{
+    E.mm.reset(E.stream);
+    if (E.cfg.profile) E.prof.stats.clear();
+    SDB_CUDA(cudaEventRecord(E.plan_a, E.stream));
+    PendingResult pr = run_plan(E, plan_text);
+
+    auto res = std::make_unique<sdb_result>();
+    res->types = pr.types;
+    const size_t ncols = pr.types.size();
+    res->i32.resize(ncols);
+    res->u64.resize(ncols);
+    std::vector<uint32_t> counts(pr.segs.size());
+    for (size_t s = 0; s < pr.segs.size(); s++)
+        SDB_CUDA(cudaMemcpyAsync(&counts[s], pr.segs[s].count, sizeof(uint32_t), cudaMemcpyDeviceToHost, E.stream));
     SDB_CUDA(cudaStreamSynchronize(E.stream));
     uint64_t total = 0;
     for (auto c : counts) total += c;
-    for (size_t ci = 0; ci < cols.size(); ci++) {
+    for (size_t ci = 0; ci < ncols; ci++) {
         if (res->types[ci] == 1)
             res->u64[ci].resize(total);
         else
             res->i32[ci].resize(total);
     }
     uint64_t base = 0;
-    for (size_t s = 0; s < outs.size(); s++) {
-        for (size_t ci = 0; ci < cols.size(); ci++) {
+    for (size_t s = 0; s < pr.segs.size(); s++) {
+        for (size_t ci = 0; ci < ncols; ci++) {
             if (!counts[s]) continue;
             if (res->types[ci] == 1)
-                SDB_CUDA(cudaMemcpyAsync(res->u64[ci].data() + base, outs[s].dev[ci], counts[s] * sizeof(uint64_t),
+                SDB_CUDA(cudaMemcpyAsync(res->u64[ci].data() + base, pr.segs[s].dev[ci], counts[s] * sizeof(uint64_t),
                                          cudaMemcpyDeviceToHost, E.stream));
             else
-                SDB_CUDA(cudaMemcpyAsync(res->i32[ci].data() + base, outs[s].dev[ci], counts[s] * sizeof(int32_t),
+                SDB_CUDA(cudaMemcpyAsync(res->i32[ci].data() + base, pr.segs[s].dev[ci], counts[s] * sizeof(int32_t),
                                          cudaMemcpyDeviceToHost, E.stream));
         }
         base += counts[s];
@@ -1587,6 +1724,214 @@ void load_table(Engine &E, const char *name, int ncols, const int32_t *const *co
         }
     }
     E.tables[name] = std::move(t);
+}
+
+// ------------------------------------------------------------------ batches
+// Records `plans` into B.rec against arena `mm` (swapped into the engine for
+// the duration).
+void record_plans(Engine &E, sdb_batch &B, MemoryManager &mm, const std::vector<std::string> &plans)
+{
+    struct Swap {  // the engine records into B against mm until scope exit
+        Engine &E;
+        MemoryManager &mm;
+        Swap(Engine &e, MemoryManager &m, Recorder *r) : E(e), mm(m)
+        {
+            E.mm.swap(mm);
+            E.rec = r;
+        }
+        ~Swap()
+        {
+            E.mm.swap(mm);
+            E.rec = nullptr;
+        }
+    };
+    B.rec = Recorder();
+    B.rec.batch_chains = !(B.flags & SDB_BATCH_NO_CHAIN_BATCH);
+    B.pend.clear();
+    Swap guard(E, mm, &B.rec);
+    for (const std::string &pt : plans) {
+        B.rec.plans.emplace_back();
+        B.pend.push_back(run_plan(E, pt));
+    }
+}
+
+void replay(sdb_batch &B, cudaStream_t main)
+{
+    if (B.mm.zused()) SDB_CUDA(cudaMemsetAsync(B.mm.zero_base(), 0, B.mm.zused(), main));
+    const size_t K = B.side.size();
+    auto phase = [&](bool post) {
+        SDB_CUDA(cudaEventRecord(B.fork, main));
+        for (size_t i = 0; i < K; i++) SDB_CUDA(cudaStreamWaitEvent(B.side[i], B.fork, 0));
+        for (size_t p = 0; p < B.rec.plans.size(); p++) {
+            cudaStream_t s = B.side[p % K];
+            for (const DevOp &op : post ? B.rec.plans[p].post : B.rec.plans[p].pre) check(op.fn(s));
+        }
+        for (size_t i = 0; i < K; i++) {
+            SDB_CUDA(cudaEventRecord(B.join[i], B.side[i]));
+            SDB_CUDA(cudaStreamWaitEvent(main, B.join[i], 0));
+        }
+    };
+    phase(false);
+    if (B.cb) check(sdb_chain_batch_launch(B.cb, (sdb_stream_t)main));
+    phase(true);
+}
+
+void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plans)
+{
+    // sizing pass: addresses only
+    MemoryManager vm;
+    vm.init_virtual();
+    record_plans(E, B, vm, plans);
+    const uint64_t used = vm.used(), zused = vm.zused();
+    const size_t cb_bytes = B.rec.chains.empty()
+                                ? 0
+                                : sdb_chain_batch_scratch_bytes(B.rec.chains.data(), (int)B.rec.chains.size());
+    vm.release();
+
+    // real pass against an arena of exactly that size
+    B.mm.init_sized(used + cb_bytes + 256, zused, E.stream);
+    record_plans(E, B, B.mm, plans);
+    if (!B.rec.chains.empty()) {
+        void *scratch = B.mm.alloc<uint8_t>(cb_bytes);
+        check(sdb_chain_batch_create(B.rec.chains.data(), (int)B.rec.chains.size(), scratch, cb_bytes,
+                                     (sdb_stream_t)E.stream, &B.cb));
+        B.chain_groups = sdb_chain_batch_kernels(B.cb);
+    }
+
+    // pinned staging: per plan and segment, the count and every column at
+    // full capacity; the copies go at the end of the plan's work
+    size_t off = 0;
+    B.stage.assign(plans.size(), {});
+    for (size_t p = 0; p < plans.size(); p++) {
+        const PendingResult &pr = B.pend[p];
+        for (const PendingSeg &sg : pr.segs) {
+            sdb_batch::Stage st;
+            st.count_off = off;
+            off += 64;
+            for (size_t c = 0; c < pr.types.size(); c++) {
+                st.col_off.push_back(off);
+                off += (sg.cap * (pr.types[c] == 1 ? 8 : 4) + 63) & ~(size_t)63;
+            }
+            B.stage[p].push_back(st);
+        }
+    }
+    B.host_bytes = std::max<size_t>(off, 64);
+    SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&B.host), B.host_bytes, cudaHostAllocDefault));
+    for (size_t p = 0; p < plans.size(); p++) {
+        PlanRecord &rp = B.rec.plans[p];
+        auto &ops = rp.after ? rp.post : rp.pre;
+        const PendingResult &pr = B.pend[p];
+        for (size_t s = 0; s < pr.segs.size(); s++) {
+            const PendingSeg &sg = pr.segs[s];
+            char *dst = B.host + B.stage[p][s].count_off;
+            const void *cnt = sg.count;
+            ops.push_back({"d2h", [dst, cnt](cudaStream_t st) {
+                               return cudaMemcpyAsync(dst, cnt, 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                                          ? SDB_OK
+                                          : sdb_set_error(SDB_ERR_CUDA, "batch result copy failed");
+                           }});
+            for (size_t c = 0; c < pr.types.size(); c++) {
+                char *d = B.host + B.stage[p][s].col_off[c];
+                const void *src = sg.dev[c];
+                const size_t bytes = sg.cap * (pr.types[c] == 1 ? 8 : 4);
+                if (!bytes) continue;
+                ops.push_back({"d2h", [d, src, bytes](cudaStream_t st) {
+                                   return cudaMemcpyAsync(d, src, bytes, cudaMemcpyDeviceToHost, st) == cudaSuccess
+                                              ? SDB_OK
+                                              : sdb_set_error(SDB_ERR_CUDA, "batch result copy failed");
+                               }});
+            }
+        }
+    }
+
+    // streams and events; the plans' work is spread over up to 8 streams
+    SDB_CUDA(cudaStreamCreateWithFlags(&B.bs, cudaStreamNonBlocking));
+    const size_t K = std::min<size_t>(std::max<size_t>(plans.size(), 1), 8);
+    for (size_t i = 0; i < K; i++) {
+        cudaStream_t s;
+        SDB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+        B.side.push_back(s);
+        cudaEvent_t e;
+        SDB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        B.join.push_back(e);
+    }
+    SDB_CUDA(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming));
+    SDB_CUDA(cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming));
+    SDB_CUDA(cudaEventCreate(&B.ev_a));
+    SDB_CUDA(cudaEventCreate(&B.ev_b));
+    SDB_CUDA(cudaStreamSynchronize(E.stream));
+
+    const uint64_t l0 = sdb_launch_count();
+    if (!(B.flags & SDB_BATCH_EAGER)) {
+        SDB_CUDA(cudaStreamBeginCapture(B.bs, cudaStreamCaptureModeThreadLocal));
+        try {
+            replay(B, B.bs);
+        } catch (...) {
+            cudaGraph_t g = nullptr;
+            cudaStreamEndCapture(B.bs, &g);
+            if (g) cudaGraphDestroy(g);
+            throw;
+        }
+        SDB_CUDA(cudaStreamEndCapture(B.bs, &B.graph));
+        SDB_CUDA(cudaGraphInstantiate(&B.exec, B.graph, 0));
+        B.kernels = (int)(sdb_launch_count() - l0);
+    } else {
+        B.kernels = -1;  // counted on the first run
+    }
+}
+
+void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
+{
+    SDB_CUDA(cudaEventRecord(B.ev_in, E.stream));
+    SDB_CUDA(cudaStreamWaitEvent(B.bs, B.ev_in, 0));
+    SDB_CUDA(cudaEventRecord(B.ev_a, B.bs));
+    if (B.exec) {
+        SDB_CUDA(cudaGraphLaunch(B.exec, B.bs));
+    } else {
+        const uint64_t l0 = sdb_launch_count();
+        replay(B, B.bs);
+        B.kernels = (int)(sdb_launch_count() - l0);
+    }
+    SDB_CUDA(cudaEventRecord(B.ev_b, B.bs));
+    SDB_CUDA(cudaStreamSynchronize(B.bs));
+    float ms = 0;
+    SDB_CUDA(cudaEventElapsedTime(&ms, B.ev_a, B.ev_b));
+    B.last_ms = ms;
+    if (!out) return;
+    for (size_t p = 0; p < B.pend.size(); p++) {
+        const PendingResult &pr = B.pend[p];
+        auto res = std::make_unique<sdb_result>();
+        res->types = pr.types;
+        const size_t ncols = pr.types.size();
+        res->i32.resize(ncols);
+        res->u64.resize(ncols);
+        std::vector<uint32_t> counts(pr.segs.size());
+        uint64_t total = 0;
+        for (size_t s = 0; s < pr.segs.size(); s++) {
+            std::memcpy(&counts[s], B.host + B.stage[p][s].count_off, 4);
+            if (counts[s] > pr.segs[s].cap) throw Error(SDB_ERR_DEVICE, "batch result count exceeds its capacity");
+            total += counts[s];
+        }
+        for (size_t c = 0; c < ncols; c++) {
+            if (pr.types[c] == 1)
+                res->u64[c].resize(total);
+            else
+                res->i32[c].resize(total);
+        }
+        uint64_t base = 0;
+        for (size_t s = 0; s < pr.segs.size(); s++) {
+            for (size_t c = 0; c < ncols; c++) {
+                const char *src = B.host + B.stage[p][s].col_off[c];
+                if (pr.types[c] == 1)
+                    std::memcpy(res->u64[c].data() + base, src, counts[s] * sizeof(uint64_t));
+                else
+                    std::memcpy(res->i32[c].data() + base, src, counts[s] * sizeof(int32_t));
+            }
+            base += counts[s];
+        }
+        res->nrows = total;
+        out[p] = res.release();
+    }
 }
 
 template <class F>
@@ -1744,5 +2089,50 @@ int sdb_engine_last_plan_ms(const sdb_engine *eng, double *ms)
     *ms = eng->E.last_plan_ms;
     return SDB_OK;
 }
+
+int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int n_plans, int flags, sdb_batch **out)
+{
+    if (!eng || !out || n_plans < 1 || !plans_json)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_batch_prepare: bad argument");
+    if (flags & ~(SDB_BATCH_EAGER | SDB_BATCH_NO_CHAIN_BATCH))
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_batch_prepare: unknown flags 0x%x", flags);
+    *out = nullptr;
+    std::vector<std::string> plans;
+    for (int i = 0; i < n_plans; i++) {
+        if (!plans_json[i]) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_batch_prepare: plan %d is NULL", i);
+        plans.emplace_back(plans_json[i]);
+    }
+    auto B = std::make_unique<sdb_batch>();
+    B->eng = eng;
+    B->flags = flags;
+    int st = sdb::guarded([&] { sdb::batch_prepare(eng->E, *B, plans); });
+    if (st != SDB_OK) return st;
+    *out = B.release();
+    return SDB_OK;
+}
+
+int sdb_batch_run(sdb_batch *b, sdb_result **results)
+{
+    if (!b) return sdb_set_error(SDB_ERR_INVALID, "sdb_batch_run: NULL batch");
+    return sdb::guarded([&] { sdb::batch_run(b->eng->E, *b, results); });
+}
+
+int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
+{
+    if (!b || !info) return sdb_set_error(SDB_ERR_INVALID, "sdb_batch_info: NULL argument");
+    info->n_plans = (int32_t)b->pend.size();
+    info->kernels_per_run = b->kernels;
+    info->graph = b->exec ? 1 : 0;
+    info->chain_launches = b->chain_groups;
+    info->batched_chains = (int32_t)b->rec.chains.size();
+    info->pad = 0;
+    info->arena_bytes = b->mm.size();
+    info->zero_bytes = b->mm.zused();
+    info->host_bytes = b->host_bytes;
+    info->last_run_ms = b->last_ms;
+    return SDB_OK;
+}
+
+void sdb_batch_free(sdb_batch *b) { delete b; }
 
 }  // extern "C"

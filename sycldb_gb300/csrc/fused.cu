@@ -21,8 +21,10 @@
 // hash tables through the read-only path so they stay in L2.
 #include <algorithm>
 #include <cstdio>
+#include <atomic>
 #include <cstring>
 #include <utility>
+#include <vector>
 
 #include "common.cuh"
 
@@ -744,65 +746,209 @@ __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsi
 template <int STAGES>
 __host__ __device__ constexpr int dense_min_blocks() { return STAGES >= 3 ? 3 : 5; }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
-__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(const __grid_constant__ Launch L)
+// ---- pieces shared by the single-chain pass and the batched pass ----------
+
+template <int TERM>
+__device__ __forceinline__ void group_table_reset(uint32_t *s_key, unsigned long long *s_sum)
 {
-    constexpr int kStages = STAGES;
-    constexpr int N = sizeof...(KS);
-    constexpr bool kCompact = SPLIT <= N;
-    constexpr int kDenseOps = kCompact ? SPLIT : N;
-    extern __shared__ int4 s_buf[];  // [kStages][kSlots][kThreads], then the semi-join bitmap
-    __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
-    __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
-    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
-    const bool direct = L.P <= kDenseCap;
-    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
-    if (TERM == T_GROUP) {
+    if (TERM == T_GROUP)
         for (uint32_t i = threadIdx.x; i < kDenseCap; i += blockDim.x) {
             s_key[i] = kEmpty;
             s_sum[i] = 0;
         }
-    }
-    if (L.bitmap_ht) {
-        // Pack the bool table into bits: word w holds entries 32w .. 32w + 31.
-        const uint32_t words = (L.bitmap_len + 31) / 32;
-        for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
-            uint32_t bits = 0;
-            const uint32_t e0 = w * 32;
-            if (e0 + 32 <= L.bitmap_len && sdb::aligned(L.bitmap_ht, 4)) {
-                const uint32_t *q = reinterpret_cast<const uint32_t *>(L.bitmap_ht + e0);
+}
+
+// Packs the chain's semi-join table into the shared-memory bitmap: word w
+// holds entries 32w .. 32w + 31.
+__device__ __forceinline__ void stage_bitmap(const Launch &L, uint32_t *s_bits)
+{
+    if (!L.bitmap_ht) return;
+    const uint32_t words = (L.bitmap_len + 31) / 32;
+    for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
+        uint32_t bits = 0;
+        const uint32_t e0 = w * 32;
+        if (e0 + 32 <= L.bitmap_len && sdb::aligned(L.bitmap_ht, 4)) {
+            const uint32_t *q = reinterpret_cast<const uint32_t *>(L.bitmap_ht + e0);
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const uint32_t x = __vcmpne4(__ldg(q + j), 0u);
-                    bits |= (((x >> 7) & 1u) | ((x >> 14) & 2u) | ((x >> 21) & 4u) | ((x >> 28) & 8u)) << (4 * j);
-                }
-            } else {
-                for (uint32_t j = 0; j < 32 && e0 + j < L.bitmap_len; j++) bits |= (uint32_t)(L.bitmap_ht[e0 + j] != 0) << j;
+            for (int j = 0; j < 8; j++) {
+                const uint32_t x = __vcmpne4(__ldg(q + j), 0u);
+                bits |= (((x >> 7) & 1u) | ((x >> 14) & 2u) | ((x >> 21) & 4u) | ((x >> 28) & 8u)) << (4 * j);
             }
-            s_bits[w] = bits;
+        } else {
+            for (uint32_t j = 0; j < 32 && e0 + j < L.bitmap_len; j++) bits |= (uint32_t)(L.bitmap_ht[e0 + j] != 0) << j;
+        }
+        s_bits[w] = bits;
+    }
+}
+
+// Copies this thread's 4 rows of every slot column of `tile` (rows
+// tile + 4t .. +3) into ring stage `st`; rows past the end are zero-filled
+// or skipped.  Always commits one group (possibly empty) so every thread
+// counts groups the same way.
+template <int STAGES>
+__device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nslot, uint64_t n, int4 *s_buf, int st,
+                                           uint64_t tile)
+{
+    const uint64_t r0 = tile + (uint64_t)kItems * threadIdx.x;
+    if (r0 < n) {
+        const uint64_t left = n - r0;
+        const uint32_t bytes = left >= kItems ? 16u : (uint32_t)(left * 4);
+#pragma unroll
+        for (int sl = 0; sl < kSlots; sl++)
+            if (sl < nslot) cp_async16(&s_buf[(st * kSlots + sl) * kThreads + threadIdx.x], slot[sl] + r0, bytes);
+    }
+    cp_async_commit();
+}
+
+// One tile of one chain: the ops before SPLIT on 4-row groups, then (if
+// SPLIT <= N) warp compaction and the remaining ops one row per lane, then
+// the terminal into the block's partials.
+template <int TERM, int NREGS, int SPLIT, int... KS>
+__device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, const int4 *s_buf, int st, uint64_t tile,
+                                          uint8_t *s_list, uint32_t *s_key, unsigned long long *s_sum,
+                                          const uint32_t *s_bits, bool direct, uint64_t &acc)
+{
+    constexpr int N = sizeof...(KS);
+    constexpr bool kCompact = SPLIT <= N;
+    constexpr int kDenseOps = kCompact ? SPLIT : N;
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    S.stage = &s_buf[st * kSlots * kThreads + threadIdx.x];
+    S.base = tile + (uint64_t)kItems * threadIdx.x;
+    S.valid = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; k++) S.valid |= (uint32_t)(S.base + k < L.n) << k;
+    if (L.flags_in && S.valid) {
+        uint32_t m = 0;
+#pragma unroll
+        for (int k = 0; k < kItems; k++)
+            if ((S.valid >> k) & 1u) m |= (uint32_t)(L.flags_in[S.base + k] != 0) << k;
+        S.live = m;
+    } else {
+        S.live = S.valid;
+    }
+    run_steps<NREGS, 0, KS...>(L, S, std::make_integer_sequence<int, kDenseOps>{});
+
+    if constexpr (kCompact) {
+        // warp prefix sum of the live-row counts
+        const uint32_t cnt = __popc(S.live);
+        uint32_t incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+        uint8_t *list = s_list + warp * 32 * kItems;
+        uint32_t pos = incl - cnt;
+#pragma unroll
+        for (int k = 0; k < kItems; k++)
+            if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
+        __syncwarp();
+        Row<NREGS> R;
+        R.wstage = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
+        for (uint32_t b = 0; b < total; b += 32) {
+            const uint32_t idx = b + lane;
+            R.live = idx < total;
+            R.r = R.live ? list[idx] : 0;
+            R.grow = tile + (uint64_t)warp * 32 * kItems + R.r;
+#pragma unroll
+            for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
+            run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
+            if (R.live) {
+                if (TERM == T_SUM) {
+                    acc += sdb::widen(fetch1(L.value, R));
+                } else if (TERM == T_GROUP) {
+                    uint32_t h = 0;
+#pragma unroll
+                    for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+                        if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
+                    group_row(L, s_key, s_sum, direct, h, fetch1(L.value, R),
+                              [R, &L](int kk) { return fetch1(L.keys[kk], R); });
+                }
+            }
+        }
+        __syncwarp();
+    } else {
+        if (TERM == T_FLAGS || L.flags_out) {
+#pragma unroll
+            for (int k = 0; k < kItems; k++)
+                if ((S.valid >> k) & 1u) L.flags_out[S.base + k] = (uint8_t)((S.live >> k) & 1u);
+        }
+        if (S.live) {
+            int32_t v[kItems];
+            if (TERM == T_SUM) {
+                fetch4(L.value, S, v);
+#pragma unroll
+                for (int k = 0; k < kItems; k++)
+                    if ((S.live >> k) & 1u) acc += sdb::widen(v[k]);
+            } else if (TERM == T_GROUP) {
+                fetch4(L.value, S, v);
+                uint32_t h[kItems] = {0, 0, 0, 0};
+#pragma unroll
+                for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+                    if (kk < L.n_keys) {
+                        int32_t kv[kItems];
+                        fetch4(L.keys[kk], S, kv);
+#pragma unroll
+                        for (int k = 0; k < kItems; k++) h[k] += ((uint32_t)kv[k] - (uint32_t)L.key_min[kk]) * L.mults[kk];
+                    }
+#pragma unroll
+                for (int k = 0; k < kItems; k++)
+                    if ((S.live >> k) & 1u)
+                        group_row(L, s_key, s_sum, direct, h[k], v[k], [&](int kk) {
+                            int32_t kv[kItems];
+                            fetch4(L.keys[kk], S, kv);
+                            return kv[k];
+                        });
+            }
         }
     }
+}
+
+// Flushes a block's partials of one chain into its global outputs: one
+// 64-bit atomic per block for SUM, one per touched slot for group-by.  The
+// caller synchronises the block before and (to reuse the table) after.
+template <int TERM>
+__device__ __forceinline__ void block_flush(const Launch &L, uint32_t *s_key, unsigned long long *s_sum,
+                                            uint64_t *s_part, uint64_t &acc)
+{
+    if (TERM == T_SUM) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+        acc = 0;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint64_t t = 0;
+            for (int w = 0; w < kThreads / 32; w++) t += s_part[w];
+            if (t) atomicAdd(reinterpret_cast<unsigned long long *>(L.sum_out), (unsigned long long)t);
+        }
+    } else if (TERM == T_GROUP) {
+        __syncthreads();
+        for (uint32_t i = threadIdx.x; i < kDenseCap; i += blockDim.x) {
+            const uint32_t k = s_key[i];
+            if (k != kEmpty) atomicAdd(reinterpret_cast<unsigned long long *>(&L.out_sum[k]), s_sum[i]);
+        }
+    }
+}
+
+template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(const __grid_constant__ Launch L)
+{
+    constexpr int kStages = STAGES;
+    constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    extern __shared__ int4 s_buf[];  // [kStages][kSlots][kThreads], then the semi-join bitmap
+    __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
+    __shared__ uint64_t s_part[kThreads / 32];
+    const bool direct = L.P <= kDenseCap;
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
+    group_table_reset<TERM>(s_key, s_sum);
+    stage_bitmap(L, s_bits);
     if (TERM == T_GROUP || L.bitmap_ht) __syncthreads();
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
     const uint64_t stride = (uint64_t)gridDim.x * kTile;
-    const int nslot = L.nslot;
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-
-    // Copies this thread's 4 rows of every slot column for `tile` into ring
-    // stage `st` (rows past the end are zero-filled or skipped), then commits
-    // one group (possibly empty, so every thread counts groups the same way).
-    auto issue = [&](int st, uint64_t tile) {
-        const uint64_t r0 = tile + (uint64_t)kItems * threadIdx.x;
-        if (r0 < L.n) {
-            const uint64_t left = L.n - r0;
-            const uint32_t bytes = left >= kItems ? 16u : (uint32_t)(left * 4);
-#pragma unroll
-            for (int sl = 0; sl < kSlots; sl++)
-                if (sl < nslot)
-                    cp_async16(&s_buf[(st * kSlots + sl) * kThreads + threadIdx.x], L.slot[sl] + r0, bytes);
-        }
-        cp_async_commit();
-    };
 
     State<NREGS> S;
     S.bits = s_bits;
@@ -814,124 +960,98 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
 
     uint64_t tile = (uint64_t)blockIdx.x * kTile;
 #pragma unroll
-    for (int p = 0; p < kStages - 1; p++) issue(p, tile + p * stride);
+    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, p, tile + p * stride);
     int st = 0;
     for (; tile < L.n; tile += stride) {
-        issue((st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
+        issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, (st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
-        S.stage = &s_buf[st * kSlots * kThreads + threadIdx.x];
-        S.base = tile + (uint64_t)kItems * threadIdx.x;
-        S.valid = 0;
-#pragma unroll
-        for (int k = 0; k < kItems; k++) S.valid |= (uint32_t)(S.base + k < L.n) << k;
-        if (L.flags_in && S.valid) {
-            uint32_t m = 0;
-#pragma unroll
-            for (int k = 0; k < kItems; k++)
-                if ((S.valid >> k) & 1u) m |= (uint32_t)(L.flags_in[S.base + k] != 0) << k;
-            S.live = m;
-        } else {
-            S.live = S.valid;
-        }
-        run_steps<NREGS, 0, KS...>(L, S, std::make_integer_sequence<int, kDenseOps>{});
-
-        if constexpr (kCompact) {
-            // warp prefix sum of the live-row counts
-            const uint32_t cnt = __popc(S.live);
-            uint32_t incl = cnt;
-#pragma unroll
-            for (int o = 1; o < 32; o <<= 1) {
-                const uint32_t y = __shfl_up_sync(0xffffffffu, incl, o);
-                if (lane >= (uint32_t)o) incl += y;
-            }
-            const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-            uint8_t *list = s_list + warp * 32 * kItems;
-            uint32_t pos = incl - cnt;
-#pragma unroll
-            for (int k = 0; k < kItems; k++)
-                if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
-            __syncwarp();
-            Row<NREGS> R;
-            R.wstage = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
-            for (uint32_t b = 0; b < total; b += 32) {
-                const uint32_t idx = b + lane;
-                R.live = idx < total;
-                R.r = R.live ? list[idx] : 0;
-                R.grow = tile + (uint64_t)warp * 32 * kItems + R.r;
-#pragma unroll
-                for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
-                run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
-                if (R.live) {
-                    if (TERM == T_SUM) {
-                        acc += sdb::widen(fetch1(L.value, R));
-                    } else if (TERM == T_GROUP) {
-                        uint32_t h = 0;
-#pragma unroll
-                        for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-                            if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
-                        group_row(L, s_key, s_sum, direct, h, fetch1(L.value, R),
-                                  [R, &L](int kk) { return fetch1(L.keys[kk], R); });
-                    }
-                }
-            }
-            __syncwarp();
-        } else {
-            if (TERM == T_FLAGS || L.flags_out) {
-#pragma unroll
-                for (int k = 0; k < kItems; k++)
-                    if ((S.valid >> k) & 1u) L.flags_out[S.base + k] = (uint8_t)((S.live >> k) & 1u);
-            }
-            if (S.live) {
-                int32_t v[kItems];
-                if (TERM == T_SUM) {
-                    fetch4(L.value, S, v);
-#pragma unroll
-                    for (int k = 0; k < kItems; k++)
-                        if ((S.live >> k) & 1u) acc += sdb::widen(v[k]);
-                } else if (TERM == T_GROUP) {
-                    fetch4(L.value, S, v);
-                    uint32_t h[kItems] = {0, 0, 0, 0};
-#pragma unroll
-                    for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-                        if (kk < L.n_keys) {
-                            int32_t kv[kItems];
-                            fetch4(L.keys[kk], S, kv);
-#pragma unroll
-                            for (int k = 0; k < kItems; k++) h[k] += ((uint32_t)kv[k] - (uint32_t)L.key_min[kk]) * L.mults[kk];
-                        }
-#pragma unroll
-                    for (int k = 0; k < kItems; k++)
-                        if ((S.live >> k) & 1u)
-                            group_row(L, s_key, s_sum, direct, h[k], v[k], [&](int kk) {
-                                int32_t kv[kItems];
-                                fetch4(L.keys[kk], S, kv);
-                                return kv[k];
-                            });
-                }
-            }
-        }
+        tile_body<TERM, NREGS, SPLIT, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc);
         st = (st + 1) % kStages;
     }
     cp_async_wait<0>();
+    block_flush<TERM>(L, s_key, s_sum, s_part, acc);
+}
 
-    if (TERM == T_SUM) {
-        __shared__ uint64_t part[kThreads / 32];
+// A run of consecutive tiles of one chain: the unit the batched pass pulls
+// from its work queue.
+struct Span {
+    uint32_t chain, t0, t1, pad;
+};
+
+// Batched pass: one persistent launch over many chains of one shape.  Blocks
+// pull spans from a device work queue (one 32-bit head counter, zero before
+// the launch) until it runs dry; nothing waits on anything.  The current
+// chain's descriptor lives in shared memory; when a block's next span belongs
+// to another chain it flushes the previous chain's partials, then loads the
+// new descriptor, resets its group table and re-stages the semi-join bitmap.
+// Within a span the tiles go through the same cp.async ring as the
+// single-chain pass.
+template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
+    k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
+            uint32_t *__restrict__ head)
+{
+    constexpr int kStages = STAGES;
+    constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
+    extern __shared__ int4 s_buf[];
+    __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];
+    __shared__ uint64_t s_part[kThreads / 32];
+    __shared__ Launch s_L;
+    __shared__ uint32_t s_next;
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
+
+    State<NREGS> S;
+    S.bits = s_bits;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-        if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = acc;
+    for (int r = 0; r < NREGS; r++)
+#pragma unroll
+        for (int k = 0; k < kItems; k++) S.reg[r][k] = 0;
+    uint64_t acc = 0;
+    uint32_t cur = ~0u;
+
+    for (;;) {
+        if (threadIdx.x == 0) s_next = atomicAdd(head, 1u);
         __syncthreads();
-        if (threadIdx.x == 0) {
-            uint64_t t = 0;
-            for (int w = 0; w < kThreads / 32; w++) t += part[w];
-            if (t) atomicAdd(reinterpret_cast<unsigned long long *>(L.sum_out), (unsigned long long)t);
+        const uint32_t sp = s_next;
+        __syncthreads();  // every thread has read s_next before thread 0 writes it again
+        if (sp >= n_spans) break;
+        const Span span = spans[sp];
+        if (span.chain != cur) {
+            if (cur != ~0u) block_flush<TERM>(s_L, s_key, s_sum, s_part, acc);
+            __syncthreads();
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(&launches[span.chain]);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&s_L);
+            for (uint32_t w = threadIdx.x; w < sizeof(Launch) / 4; w += blockDim.x) dst[w] = src[w];
+            group_table_reset<TERM>(s_key, s_sum);
+            __syncthreads();
+            stage_bitmap(s_L, s_bits);
+            __syncthreads();
+            cur = span.chain;
         }
-    } else if (TERM == T_GROUP) {
-        __syncthreads();
-        for (uint32_t i = threadIdx.x; i < kDenseCap; i += blockDim.x) {
-            const uint32_t k = s_key[i];
-            if (k != kEmpty) atomicAdd(reinterpret_cast<unsigned long long *>(&L.out_sum[k]), s_sum[i]);
+        const bool direct = s_L.P <= kDenseCap;
+        const uint64_t n = s_L.n;
+#pragma unroll
+        for (int p = 0; p < kStages - 1; p++) {
+            const uint32_t t = span.t0 + p;
+            if (t < span.t1) issue_tile<kStages>(s_L.slot, s_L.nslot, n, s_buf, p, (uint64_t)t * kTile);
+            else cp_async_commit();
         }
+        int st = 0;
+        for (uint32_t t = span.t0; t < span.t1; t++) {
+            const uint32_t tn = t + kStages - 1;
+            if (tn < span.t1) issue_tile<kStages>(s_L.slot, s_L.nslot, n, s_buf, (st + kStages - 1) % kStages, (uint64_t)tn * kTile);
+            else cp_async_commit();
+            cp_async_wait<kStages - 1>();
+            tile_body<TERM, NREGS, SPLIT, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum, s_bits,
+                                                direct, acc);
+            st = (st + 1) % kStages;
+        }
+        cp_async_wait<0>();
     }
+    if (cur != ~0u) block_flush<TERM>(s_L, s_key, s_sum, s_part, acc);
 }
 
 template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
@@ -1053,38 +1173,113 @@ bool can_compact(const Launch &D, int term, int split)
     return true;
 }
 
-// Instantiated shapes.  Returns SDB_ERR_UNSUPPORTED (without launching) for
-// any other chain.  `compact`: 1 = compact after the first op when allowed.
-int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, cudaStream_t s)
+// Calls f.run<TERM, NREGS, SPLIT, KS...>() for the instantiated shape that
+// matches D, or returns SDB_ERR_UNSUPPORTED (without calling f).  `compact`:
+// 1 = compact after the first op when allowed.
+template <class F>
+int with_shape(const Launch &D, int term, int compact, F &f)
 {
-    Launch D;
-    if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
     int k[kMaxOps];
     for (int i = 0; i < D.n_ops; i++) k[i] = D.ops[i].kind;
     const int n = D.n_ops;
     const bool c1 = compact && can_compact(D, term, 1);
     // star join: semi + full + full -> group-by (SSB flight 2)
     if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_FULL_PROBE)
-        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, stages, s)
-                  : launch<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, stages, s);
+        return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>()
+                  : f.template run<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
     // full + full -> group-by
     if (term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
-        return launch<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D, stages, s);
+        return f.template run<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
     // range filter + one join + projection -> group-by
     if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_BINOP)
-        return c1 ? launch<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, stages, s)
-                  : launch<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D, stages, s);
+        return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>()
+                  : f.template run<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
     // filter-project-sum (SSB flight 1)
     if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE && k[2] == SDB_OP_SELECT &&
         k[3] == SDB_OP_BINOP)
-        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, stages, s)
-                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D, stages, s);
+        return c1 ? f.template run<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>()
+                  : f.template run<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>();
     if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
         k[2] == SDB_OP_SEARCH_RANGE && k[3] == SDB_OP_BINOP)
-        return c1 ? launch<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, stages, s)
-                  : launch<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>(D, stages, s);
+        return c1 ? f.template run<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>()
+                  : f.template run<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>();
     return SDB_ERR_UNSUPPORTED;
 }
+
+// Shape identity of a launch: which kernel instantiation with_shape picks.
+struct ShapeProbe {
+    int id = -1;
+    template <int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        static const int kId = next_shape_id();
+        id = kId;
+        return SDB_OK;
+    }
+    static int next_shape_id()
+    {
+        static std::atomic<int> n{0};
+        return n++;
+    }
+};
+
+struct SingleLauncher {
+    const Launch &D;
+    int stages;
+    cudaStream_t s;
+    template <int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        return launch<TERM, NREGS, SPLIT, KS...>(D, stages, s);
+    }
+};
+
+int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, cudaStream_t s)
+{
+    Launch D;
+    if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
+    SingleLauncher f{D, stages, s};
+    return with_shape(D, term, compact, f);
+}
+
+// One launch of k_batch over the chains of one shape group.
+template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, uint32_t *head, uint32_t bitmap_words,
+                 cudaStream_t s)
+{
+    auto kern = k_batch<TERM, NREGS, STAGES, SPLIT, KS...>;
+    const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
+    const int smem = ring + (int)(bitmap_words * 4);
+    static int attr_set = 0;
+    if (!attr_set) {
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
+        attr_set = 1;
+    }
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    uint64_t blocks = (uint64_t)num_sms() * per_sm;
+    if (blocks > n_spans) blocks = n_spans;
+    if (blocks == 0) return SDB_OK;
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(launches, spans, n_spans, head);
+    return sdb_check_launch("sdb_chain_batch_launch");
+}
+
+struct BatchLauncher {
+    const Launch *launches;
+    const Span *spans;
+    uint32_t n_spans;
+    uint32_t *head;
+    uint32_t bitmap_words;
+    int stages;
+    cudaStream_t s;
+    template <int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        return stages >= 3 ? batch_stages<TERM, NREGS, 3, SPLIT, KS...>(launches, spans, n_spans, head, bitmap_words, s)
+                           : batch_stages<TERM, NREGS, 2, SPLIT, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+    }
+};
 
 }  // namespace dense
 
@@ -1253,6 +1448,198 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
     default: return launch_regs<T_GROUP>(L, nregs, variant, s);
     }
 }
+
+// ---- batched form -----------------------------------------------------------
+
+struct sdb_chain_batch {
+    struct Group {
+        int term, compact, stages;
+        dense::Launch first;             // host copy, picks the instantiation
+        const dense::Launch *launches;   // device
+        const dense::Span *spans;        // device
+        uint32_t n_spans;
+        uint32_t *head;                  // device work-queue head
+        uint32_t bitmap_words;
+    };
+    std::vector<Group> groups;
+    std::vector<sdb_chain_desc> singles;  // chains with no batched instantiation
+    uint32_t *heads = nullptr;
+    size_t n_heads = 0;
+};
+
+namespace {
+
+// Host-side layout of a batch: groups of chains sharing one instantiation,
+// their spans, and the device bytes they take.
+struct BatchPlan {
+    struct G {
+        int term, compact, stages, shape;
+        std::vector<dense::Launch> launches;
+        std::vector<dense::Span> spans;
+        uint32_t bitmap_words = 0;
+    };
+    std::vector<G> groups;
+    std::vector<sdb_chain_desc> singles;
+    size_t bytes = 0;
+};
+
+size_t round256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
+{
+    if (n_chains < 0 || (n_chains > 0 && !chains)) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch: bad chain list");
+    constexpr uint64_t kTile = (uint64_t)kThreads * dense::kItems;
+    uint64_t total_tiles = 0;
+    struct Item {
+        dense::Launch D;
+        int term, compact, stages, shape;
+        uint64_t tiles;
+    };
+    std::vector<Item> items;
+    for (int i = 0; i < n_chains; i++) {
+        ChainLaunch L;
+        int nregs = 1, term = 0;
+        int st = sdb_chain_prepare(&chains[i], &L, sizeof L, &nregs, &term);
+        if (st != SDB_OK) return st;
+        if (L.d.n == 0) continue;
+        Item it;
+        int variant = -1;
+        if (g_tune_init) variant = g_tune[term][reg_class(nregs)][rows_bucket(L.d.n)];
+        if (variant < 0) variant = kCompact2Variant;
+        it.term = term;
+        it.compact = variant != kDenseVariant;
+        it.stages = variant == kCompact2Variant ? 2 : 3;
+        dense::ShapeProbe probe;
+        if (variant < kDenseVariant || !dense::convert(L, nregs, it.D) ||
+            dense::with_shape(it.D, term, it.compact, probe) != SDB_OK || (L.d.n + kTile - 1) / kTile > 0xffffffffull) {
+            bp.singles.push_back(chains[i]);
+            continue;
+        }
+        it.shape = probe.id;
+        it.tiles = (L.d.n + kTile - 1) / kTile;
+        total_tiles += it.tiles;
+        items.push_back(it);
+    }
+    // spans of S tiles: about 8 per resident block over the whole batch
+    const uint64_t target = (uint64_t)num_sms() * 5 * 8;
+    uint64_t S = (total_tiles + target - 1) / std::max<uint64_t>(target, 1);
+    S = std::min<uint64_t>(std::max<uint64_t>(S, 2), 64);
+    for (const Item &it : items) {
+        size_t g = 0;
+        while (g < bp.groups.size() &&
+               !(bp.groups[g].shape == it.shape && bp.groups[g].term == it.term && bp.groups[g].stages == it.stages))
+            g++;
+        if (g == bp.groups.size()) {
+            BatchPlan::G ng;
+            ng.term = it.term;
+            ng.compact = it.compact;
+            ng.stages = it.stages;
+            ng.shape = it.shape;
+            bp.groups.push_back(ng);
+        }
+        BatchPlan::G &G = bp.groups[g];
+        const uint32_t c = (uint32_t)G.launches.size();
+        G.launches.push_back(it.D);
+        if (it.D.bitmap_ht) G.bitmap_words = std::max<uint32_t>(G.bitmap_words, (it.D.bitmap_len + 31) / 32);
+        for (uint64_t t = 0; t < it.tiles; t += S)
+            G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + S, it.tiles), 0});
+    }
+    bp.bytes = round256(bp.groups.size() * sizeof(uint32_t));
+    for (const auto &G : bp.groups)
+        bp.bytes += round256(G.launches.size() * sizeof(dense::Launch)) + round256(G.spans.size() * sizeof(dense::Span));
+    return SDB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t sdb_chain_batch_scratch_bytes(const sdb_chain_desc *chains, int n_chains)
+{
+    BatchPlan bp;
+    if (plan_batch(chains, n_chains, bp) != SDB_OK) return 0;
+    return std::max<size_t>(bp.bytes, 256);
+}
+
+int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
+                           sdb_stream_t stream, sdb_chain_batch **out)
+{
+    if (!out) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create: NULL out");
+    *out = nullptr;
+    BatchPlan bp;
+    int st = plan_batch(chains, n_chains, bp);
+    if (st != SDB_OK) return st;
+    if (dev_bytes < bp.bytes || (bp.bytes && !dev_scratch))
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create: scratch of %zu bytes, %zu needed", dev_bytes,
+                             bp.bytes);
+    if (!sdb::aligned(dev_scratch, 256)) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create: scratch not 256-byte aligned");
+    std::vector<char> host(bp.bytes, 0);
+    auto *b = new sdb_chain_batch;
+    char *dev = static_cast<char *>(dev_scratch);
+    size_t off = round256(bp.groups.size() * sizeof(uint32_t));
+    b->heads = reinterpret_cast<uint32_t *>(dev);
+    b->n_heads = bp.groups.size();
+    for (size_t g = 0; g < bp.groups.size(); g++) {
+        const auto &G = bp.groups[g];
+        sdb_chain_batch::Group o;
+        o.term = G.term;
+        o.compact = G.compact;
+        o.stages = G.stages;
+        o.first = G.launches[0];
+        o.head = b->heads + g;
+        o.bitmap_words = G.bitmap_words;
+        std::memcpy(host.data() + off, G.launches.data(), G.launches.size() * sizeof(dense::Launch));
+        o.launches = reinterpret_cast<const dense::Launch *>(dev + off);
+        off += round256(G.launches.size() * sizeof(dense::Launch));
+        std::memcpy(host.data() + off, G.spans.data(), G.spans.size() * sizeof(dense::Span));
+        o.spans = reinterpret_cast<const dense::Span *>(dev + off);
+        o.n_spans = (uint32_t)G.spans.size();
+        off += round256(G.spans.size() * sizeof(dense::Span));
+        b->groups.push_back(o);
+    }
+    b->singles = bp.singles;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (bp.bytes) {
+        cudaError_t e = cudaMemcpyAsync(dev_scratch, host.data(), bp.bytes, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            delete b;
+            return sdb_set_error(SDB_ERR_CUDA, "sdb_chain_batch_create: %s", cudaGetErrorString(e));
+        }
+    }
+    *out = b;
+    return SDB_OK;
+}
+
+int sdb_chain_batch_launch(const sdb_chain_batch *b, sdb_stream_t stream)
+{
+    if (!b) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_launch: NULL batch");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (b->n_heads) {
+        cudaError_t e = cudaMemsetAsync(b->heads, 0, b->n_heads * sizeof(uint32_t), s);
+        if (e != cudaSuccess) return sdb_set_error(SDB_ERR_CUDA, "sdb_chain_batch_launch: %s", cudaGetErrorString(e));
+    }
+    for (const auto &G : b->groups) {
+        dense::BatchLauncher f{G.launches, G.spans, G.n_spans, G.head, G.bitmap_words, G.stages, s};
+        int st = dense::with_shape(G.first, G.term, G.compact, f);
+        if (st != SDB_OK) return st;
+    }
+    for (const auto &c : b->singles) {
+        int st = fused_chain_impl(&c, -1, stream);
+        if (st != SDB_OK) return st;
+    }
+    return SDB_OK;
+}
+
+int sdb_chain_batch_kernels(const sdb_chain_batch *b)
+{
+    if (!b) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_kernels: NULL batch");
+    return (int)(b->groups.size() + b->singles.size());
+}
+
+void sdb_chain_batch_destroy(sdb_chain_batch *b) { delete b; }
+
+}  // extern "C"
 
 extern "C" {
 

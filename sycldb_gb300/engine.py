@@ -55,6 +55,28 @@ class Result:
         return r
 
 
+def _take_result(r) -> Result:
+    """Copies a native sdb_result into numpy columns and frees it."""
+    L = capi.lib()
+    try:
+        ncols, nrows = ctypes.c_int(), ctypes.c_uint64()
+        L.sdb_result_shape(r, ctypes.byref(ncols), ctypes.byref(nrows))
+        cols = []
+        for c in range(ncols.value):
+            t, d = ctypes.c_int(), ctypes.c_void_p()
+            capi.check(L.sdb_result_column(r, c, ctypes.byref(t), ctypes.byref(d)))
+            dt = np.uint64 if t.value == 1 else np.int32
+            n = nrows.value
+            if n == 0:
+                cols.append(np.empty(0, dtype=dt))
+            else:
+                buf = (ctypes.c_char * (n * np.dtype(dt).itemsize)).from_address(d.value)
+                cols.append(np.frombuffer(buf, dtype=dt).copy())
+        return Result(cols)
+    finally:
+        L.sdb_result_free(r)
+
+
 class Engine:
     def __init__(self, arena_bytes: int = 0, segment_rows: int = 0, fuse: bool = True, profile: bool = False,
                  stream: Optional[int] = None):
@@ -113,23 +135,11 @@ class Engine:
         L = capi.lib()
         r = ctypes.c_void_p()
         capi.check(L.sdb_engine_execute(self._h, text.encode(), ctypes.byref(r)))
-        try:
-            ncols, nrows = ctypes.c_int(), ctypes.c_uint64()
-            L.sdb_result_shape(r, ctypes.byref(ncols), ctypes.byref(nrows))
-            cols = []
-            for c in range(ncols.value):
-                t, d = ctypes.c_int(), ctypes.c_void_p()
-                capi.check(L.sdb_result_column(r, c, ctypes.byref(t), ctypes.byref(d)))
-                dt = np.uint64 if t.value == 1 else np.int32
-                n = nrows.value
-                if n == 0:
-                    cols.append(np.empty(0, dtype=dt))
-                else:
-                    buf = (ctypes.c_char * (n * np.dtype(dt).itemsize)).from_address(d.value)
-                    cols.append(np.frombuffer(buf, dtype=dt).copy())
-            return Result(cols)
-        finally:
-            L.sdb_result_free(r)
+        return _take_result(r)
+
+    def batch(self, plans, eager: bool = False, chain_batch: bool = True) -> "Batch":
+        """Prepares ``plans`` as one batch (see ``Batch``)."""
+        return Batch(self, plans, eager=eager, chain_batch=chain_batch)
 
     def execute_to_res(self, plan, path: str):
         """Runs ``plan`` and writes the rows as the reference's ``.res`` file."""
@@ -156,3 +166,55 @@ class Engine:
             L.sdb_engine_kernel_stats(self._h, k, ctypes.byref(name), ctypes.byref(cnt), ctypes.byref(ms))
             out[name.value.decode()] = (cnt.value, ms.value)
         return out
+
+
+class Batch:
+    """Many plans prepared once and run together (``sdb_engine_batch_*``).
+
+    Each run replays every plan's recorded device work -- as one CUDA graph
+    unless ``eager`` -- with the plans' aggregating fused chains in one
+    persistent launch per chain shape (unless ``chain_batch`` is False), and
+    returns one ``Result`` per plan, each equal to what ``Engine.execute``
+    gives for that plan alone."""
+
+    def __init__(self, engine: Engine, plans, eager: bool = False, chain_batch: bool = True):
+        L = capi.lib()
+        texts = [p if isinstance(p, str) else json.dumps(p) for p in plans]
+        arr = (ctypes.c_char_p * len(texts))(*[t.encode() for t in texts])
+        flags = (capi.SDB_BATCH_EAGER if eager else 0) | (0 if chain_batch else capi.SDB_BATCH_NO_CHAIN_BATCH)
+        h = ctypes.c_void_p()
+        capi.check(L.sdb_engine_batch_prepare(engine._h, arr, len(texts), flags, ctypes.byref(h)))
+        self._h = h
+        self._engine = engine  # the batch reads the engine's tables
+        self.n_plans = len(texts)
+
+    def run(self, unpack: bool = True) -> Optional[List[Result]]:
+        L = capi.lib()
+        if not unpack:
+            capi.check(L.sdb_batch_run(self._h, None))
+            return None
+        out = (ctypes.c_void_p * self.n_plans)()
+        capi.check(L.sdb_batch_run(self._h, out))
+        return [_take_result(ctypes.c_void_p(out[i])) for i in range(self.n_plans)]
+
+    def stats(self) -> dict:
+        st = capi.BatchStats()
+        capi.check(capi.lib().sdb_batch_info(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in capi.BatchStats._fields_ if f != "pad"}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().sdb_batch_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
