@@ -14,6 +14,11 @@ to result rows in host memory.
              the measured HBM copy bandwidth
   cpu_baseline  the CPU oracle (operator-at-a-time C/OpenMP restatement of
              the reference executor) on a bounded row sample, host cores
+  batched    64 star-join plans over fact partitions of 1M..50M rows
+             (lognormal), SF20 dimensions: queries/s and p50/p99 latency of the
+             prepared batch (one CUDA graph, one persistent chain-batch launch)
+             against the same 64 plans executed one at a time, results
+             compared plan by plan
 
 --impl reference times the reference path's CPU restatement (the oracle port:
 the reference itself needs AdaptiveCpp, oneDPL and Thrift and cannot be built
@@ -34,7 +39,7 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "rows/s & %HBM roofline (SF20 star join)"
+METRIC = "rows/s & %HBM roofline (SF20 star join); batched qps + p99 vs plain"
 UNIT = "rows/s"
 SF = 20.0
 REGION, CATEGORY = 2, 11
@@ -51,6 +56,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=10, help="0 skips the host-buffer leg")
     ap.add_argument("--arena-gb", type=float, default=0.0, help="executor arena; 0 = the default budget")
+    ap.add_argument("--batched-runs", type=int, default=20,
+                    help="timed runs of the 64-plan batch (0 skips the batched form)")
+    ap.add_argument("--plain-rounds", type=int, default=3, help="timed rounds of the 64 plans one at a time")
     return ap.parse_args()
 
 
@@ -293,6 +301,10 @@ def run_ours(args, rank, world, local, pg):
 
     # e2e through the C ABI with host (pinned) buffers
     e2e = run_e2e(args, eng, plan, n, cols, sf, rank, stream, pg) if args.e2e_steps > 0 else None
+    eng.close()
+    del fact
+    torch.cuda.empty_cache()
+    batched = run_batched(args, rank, world, local, pg, stream, peak) if args.batched_runs > 0 else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -303,6 +315,7 @@ def run_ours(args, rank, world, local, pg):
                    "segment_rows": 1 << 28, "fused": True, "parallelism": "replicas" if world > 1 else "1 GPU"},
         "roofline": roof,
         "e2e": e2e,
+        "batched": batched,
         "gpu_launches": launches,
         "kernel_ms_last_step": {k: v[1] for k, v in stats_last.items()},
         "clocks": clk,
@@ -312,7 +325,6 @@ def run_ours(args, rank, world, local, pg):
         v, cores, _ = cpu_oracle_run(sample, sf, steps=3, warmup=1)
         line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                                 "sample": "3 runs on the first %d of %d fact rows (1/16), full dimensions" % (sample, n)}
-    eng.close()
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
@@ -348,6 +360,96 @@ def run_e2e(args, eng, plan, n, cols, sf, rank, stream, pg):
     return {"value": rows / dt, "unit": UNIT, "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
             "ms_per_step": dt / args.e2e_steps * 1e3, "steps": args.e2e_steps,
             "timing": "host wall clock around load_table(host pinned columns) + execute, synchronised"}
+
+
+def _pct(xs, q):
+    xs = sorted(xs)
+    if not xs:
+        return None
+    k = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
+    return xs[k]
+
+
+def run_batched(args, rank, world, local, pg, stream, peak):
+    """The batched form against the plain one-plan-at-a-time path, same
+    plans, same engine, same device-resident partitions."""
+    import torch
+
+    from sycldb_gb300 import ssb, workloads
+    from sycldb_gb300.engine import Engine
+
+    wl = workloads.batch_workload(seed=ssb.SEED + rank)
+    eng = Engine(arena_bytes=int(args.arena_gb * (1 << 30)), fuse=True, stream=stream.cuda_stream)
+    workloads.load_batch_tables(eng, wl, device=True)
+    pls = wl.plans()
+    torch.cuda.synchronize()
+
+    alone = None
+    for _ in range(2):
+        alone = [eng.execute(p).canonical() for p in pls]
+    lat_plain = []
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(args.plain_rounds):
+        for p in pls:
+            t = time.perf_counter()
+            eng.execute(p)
+            lat_plain.append(time.perf_counter() - t)
+    plain_s = max_over_ranks(pg, time.perf_counter() - t0)
+
+    b = eng.batch(pls)
+    got = [r.canonical() for r in b.run()]
+    exact = got == alone
+    for _ in range(3):
+        b.run()
+    clocks = ClockSampler(local)
+    clocks.start()
+    time.sleep(0.1)
+    lat_b, dev_ms, chain_ms = [], [], []
+    barrier(pg)
+    t0 = time.perf_counter()
+    for _ in range(args.batched_runs):
+        t = time.perf_counter()
+        b.run()
+        lat_b.append(time.perf_counter() - t)
+        st = b.stats()
+        dev_ms.append(st["last_run_ms"])
+        chain_ms.append(st["last_chain_ms"])
+    batch_s = max_over_ranks(pg, time.perf_counter() - t0)
+    clk = clocks.stop()
+    st = b.stats()
+    b.close()
+    eng.close()
+
+    nq = len(pls)
+    qps_plain = sum_over_ranks(pg, float(nq * args.plain_rounds)) / plain_s
+    qps_batched = sum_over_ranks(pg, float(nq * args.batched_runs)) / batch_s
+    chain_med = statistics.median(chain_ms)
+    fact_bytes = 16 * wl.total_rows
+    achieved = fact_bytes / (chain_med / 1e3) / 1e9 if chain_med > 0 else None
+    return {
+        "workload": "%d star-join plans (supplier region semi join, part category + brand window, date year "
+                    "window; group by (d_year, p_brand1), SUM(lo_revenue)), each over its own fact partition; "
+                    "partition rows lognormal (median 7M, log-sd 1) clipped to [1M, 50M], total %d rows; SF20 "
+                    "dimensions" % (nq, wl.total_rows),
+        "partition_rows": {"min": min(wl.rows), "max": max(wl.rows), "total": wl.total_rows},
+        "group_counts": {"min": min(len(r) for r in alone), "max": max(len(r) for r in alone)},
+        "qps_batched": qps_batched, "qps_plain": qps_plain, "speedup": qps_batched / qps_plain,
+        "latency_ms": {
+            "batched_p50": _pct(lat_b, 50) * 1e3, "batched_p99": _pct(lat_b, 99) * 1e3,
+            "plain_p50": _pct(lat_plain, 50) * 1e3, "plain_p99": _pct(lat_plain, 99) * 1e3,
+            "note": "batched: every plan of a batch completes when the batch run returns (host wall clock "
+                    "around sdb_batch_run incl. result unpacking); plain: each sdb_engine_execute alone"},
+        "device_ms_per_batch": statistics.median(dev_ms),
+        "chain_batch": {"kernel": "k_batch (persistent, span work queue; semi + full + full probe, group-by)",
+                        "ms": chain_med, "algorithmic_bytes": fact_bytes,
+                        "achieved": achieved, "peak": peak, "unit": "GB/s",
+                        "frac": achieved / peak if achieved else None},
+        "kernels_per_run": st["kernels_per_run"], "graph": bool(st["graph"]),
+        "chain_launches": st["chain_launches"], "batched_chains": st["batched_chains"],
+        "arena_bytes": st["arena_bytes"], "bit_exact_vs_plain": exact,
+        "plain_rounds": args.plain_rounds, "batched_runs": args.batched_runs, "clocks": clk,
+    }
 
 
 def main():

@@ -431,6 +431,7 @@ typedef struct sdb_batch_stats {
     uint64_t zero_bytes;      /* of it, the region cleared on each run */
     uint64_t host_bytes;      /* pinned staging */
     double last_run_ms;       /* device milliseconds of the last run */
+    double last_chain_ms;     /* of it, the chain batch's launches (0: none) */
 } sdb_batch_stats;
 
 int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int n_plans, int flags,

@@ -1463,6 +1463,8 @@ struct sdb_batch {
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr, ev_in = nullptr;
+    cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;  // around the chain batch
+    double last_chain_ms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int kernels = 0;
@@ -1477,7 +1479,7 @@ struct sdb_batch {
         if (cb) sdb_chain_batch_destroy(cb);
         for (auto s : side) cudaStreamDestroy(s);
         for (auto e : join) cudaEventDestroy(e);
-        for (auto e : {fork, ev_a, ev_b, ev_in})
+        for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_c1})
             if (e) cudaEventDestroy(e);
         if (bs) cudaStreamDestroy(bs);
         if (host) cudaFreeHost(host);
@@ -1772,7 +1774,12 @@ void replay(sdb_batch &B, cudaStream_t main)
         }
     };
     phase(false);
-    if (B.cb) check(sdb_chain_batch_launch(B.cb, (sdb_stream_t)main));
+    if (B.cb) {
+        // external records: they stay timing events inside a captured graph
+        SDB_CUDA(cudaEventRecordWithFlags(B.ev_c0, main, cudaEventRecordExternal));
+        check(sdb_chain_batch_launch(B.cb, (sdb_stream_t)main));
+        SDB_CUDA(cudaEventRecordWithFlags(B.ev_c1, main, cudaEventRecordExternal));
+    }
     phase(true);
 }
 
@@ -1859,6 +1866,8 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
     SDB_CUDA(cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming));
     SDB_CUDA(cudaEventCreate(&B.ev_a));
     SDB_CUDA(cudaEventCreate(&B.ev_b));
+    SDB_CUDA(cudaEventCreate(&B.ev_c0));
+    SDB_CUDA(cudaEventCreate(&B.ev_c1));
     SDB_CUDA(cudaStreamSynchronize(E.stream));
 
     const uint64_t l0 = sdb_launch_count();
@@ -1897,6 +1906,10 @@ void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
     float ms = 0;
     SDB_CUDA(cudaEventElapsedTime(&ms, B.ev_a, B.ev_b));
     B.last_ms = ms;
+    if (B.cb) {
+        float cms = 0;
+        B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_c0, B.ev_c1) == cudaSuccess ? cms : -1.0;
+    }
     if (!out) return;
     for (size_t p = 0; p < B.pend.size(); p++) {
         const PendingResult &pr = B.pend[p];
@@ -2130,6 +2143,7 @@ int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
     info->zero_bytes = b->mm.zused();
     info->host_bytes = b->host_bytes;
     info->last_run_ms = b->last_ms;
+    info->last_chain_ms = b->last_chain_ms;
     return SDB_OK;
 }
 
