@@ -316,6 +316,12 @@ typedef struct sdb_chain_batch sdb_chain_batch;
 size_t sdb_chain_batch_scratch_bytes(const sdb_chain_desc *chains, int n_chains);
 int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
                            sdb_stream_t stream, sdb_chain_batch **out);
+/* As sdb_chain_batch_create, without waiting: the tables are written into
+ * `host_staging` (pinned host memory of at least the scratch size), copied
+ * with one cudaMemcpyAsync on `stream`, and `host_staging` must stay
+ * untouched until that copy has completed. */
+int sdb_chain_batch_create_async(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
+                                 void *host_staging, size_t host_bytes, sdb_stream_t stream, sdb_chain_batch **out);
 int sdb_chain_batch_launch(const sdb_chain_batch *batch, sdb_stream_t stream);
 /* Kernel launches one sdb_chain_batch_launch makes (the memset excluded). */
 int sdb_chain_batch_kernels(const sdb_chain_batch *batch);
@@ -442,6 +448,70 @@ int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int
 int sdb_batch_run(sdb_batch *batch, sdb_result **results);
 int sdb_batch_info(const sdb_batch *batch, sdb_batch_stats *info);
 void sdb_batch_free(sdb_batch *batch);
+
+/* ----------------------------------------------------------------- server
+ * Continuous batching of arriving plans over the engine's loaded tables.  No
+ * counterpart in the reference, whose application runs one plan at a time
+ * (app/application.cpp:37-48); every result equals what sdb_engine_execute
+ * gives for the plan alone.
+ *
+ * One dispatcher thread owns the device work and keeps up to `slots` batches
+ * in flight, each on its own streams.  Whenever a slot is free and requests
+ * wait, it admits the longest first-come prefix (at most max_batch plans)
+ * whose hash tables and intermediates fit the free part of the device budget,
+ * records those plans against memory carved from the budget (exact sizes from
+ * a sizing pass) and enqueues them as one batch (sdb_engine_batch_prepare's
+ * phases, without a graph: each batch runs once).  Requests arriving while
+ * batches run go into the next free slot, so their work overlaps on the
+ * device.  A request whose plan is invalid, or needs more than the whole
+ * budget, finishes with an error status.  While a server exists its engine
+ * must not be used by any other call (sdb_engine_execute, load_table, ...). */
+typedef struct sdb_server sdb_server;
+
+typedef struct sdb_server_config {
+    uint64_t budget_bytes;    /* device memory for admitted plans' tables and intermediates; 0 = 60 GB */
+    uint64_t pinned_bytes;    /* pinned host staging of results; 0 = 1 GB */
+    int32_t slots;            /* batches in flight; 0 = 4 */
+    int32_t max_batch;        /* plans per batch; 0 = 64 */
+    int32_t streams_per_slot; /* 0 = 4 */
+    int32_t pad;
+} sdb_server_config;
+
+typedef struct sdb_server_stats {
+    uint64_t submitted, completed, failed;
+    uint64_t batches, batched_plans;   /* batches launched, plans in them */
+    uint64_t max_batch_plans;          /* largest batch */
+    uint64_t max_inflight_plans;       /* most plans admitted and unfinished at once */
+    uint64_t peak_device_bytes;        /* most budget bytes in use at once */
+    uint64_t peak_pinned_bytes;
+    uint64_t budget_bytes;
+} sdb_server_stats;
+
+int sdb_server_create(sdb_engine *eng, const sdb_server_config *cfg, sdb_server **out);
+/* Queues a plan (thread-safe, does not wait); *id identifies its result. */
+int sdb_server_submit(sdb_server *server, const char *plan_json, int64_t *id);
+/* Waits up to timeout_ms (< 0: without limit) for the next finished request:
+ * its id, status (SDB_OK or the failure; sdb_last_error() then holds the
+ * message), result (NULL on failure; free with sdb_result_free) and latency
+ * (ms from submission to the result reaching the host).  SDB_ERR_TIMEOUT when
+ * none finished in time. */
+int sdb_server_next(sdb_server *server, int timeout_ms, int64_t *id, int *status, sdb_result **result,
+                    double *latency_ms);
+int sdb_server_stats_get(sdb_server *server, sdb_server_stats *out);
+/* Finishes every queued request, then frees the server (unread results too). */
+int sdb_server_destroy(sdb_server *server);
+
+/* Load generator over an arrival trace: plan i is submitted arrival_s[i]
+ * seconds after the start (open loop, from an internal thread) and its status,
+ * latency (from its scheduled arrival) and, if `results` is not NULL, result
+ * are stored at index i.  *wall_s = seconds from the start to the last
+ * completion.  Nothing else may submit to the server meanwhile. */
+int sdb_server_replay(sdb_server *server, const char *const *plans, const double *arrival_s, int n, int *status,
+                      sdb_result **results, double *latency_ms, double *wall_s);
+/* The same trace through the plain path: one plan at a time, in arrival
+ * order, each started at its arrival or when the previous one finished. */
+int sdb_engine_replay_plain(sdb_engine *eng, const char *const *plans, const double *arrival_s, int n, int *status,
+                            sdb_result **results, double *latency_ms, double *wall_s);
 
 #ifdef __cplusplus
 }

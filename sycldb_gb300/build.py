@@ -23,7 +23,7 @@ LIB = os.path.join(OUT, "libsycldb_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_SOURCES = ["kernels.cu", "fused.cu"]
-CPP_SOURCES = ["errors.cpp", os.path.join("engine", "engine.cpp")]
+CPP_SOURCES = ["errors.cpp", os.path.join("engine", "engine.cpp"), os.path.join("engine", "server.cpp")]
 
 
 def _nvcc() -> str:

@@ -66,6 +66,17 @@ class BatchStats(ctypes.Structure):
                 ("host_bytes", c_uint64), ("last_run_ms", c_double), ("last_chain_ms", c_double)]
 
 
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("budget_bytes", c_uint64), ("pinned_bytes", c_uint64), ("slots", c_int32), ("max_batch", c_int32),
+                ("streams_per_slot", c_int32), ("pad", c_int32)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(f, c_uint64) for f in ("submitted", "completed", "failed", "batches", "batched_plans",
+                                        "max_batch_plans", "max_inflight_plans", "peak_device_bytes",
+                                        "peak_pinned_bytes", "budget_bytes")]
+
+
 SDB_BATCH_EAGER = 1
 SDB_BATCH_NO_CHAIN_BATCH = 2
 
@@ -106,6 +117,8 @@ _SIGS = {
     "sdb_chain_registers": (c_int, [POINTER(ChainDesc)]),
     "sdb_chain_batch_scratch_bytes": (c_size_t, [POINTER(ChainDesc), c_int]),
     "sdb_chain_batch_create": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
+    "sdb_chain_batch_create_async": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, c_void_p, c_size_t, _P,
+                                             POINTER(c_void_p)]),
     "sdb_chain_batch_launch": (c_int, [c_void_p, _P]),
     "sdb_chain_batch_kernels": (c_int, [c_void_p]),
     "sdb_chain_batch_destroy": (None, [c_void_p]),
@@ -130,6 +143,16 @@ _SIGS = {
     "sdb_batch_run": (c_int, [c_void_p, POINTER(c_void_p)]),
     "sdb_batch_info": (c_int, [c_void_p, POINTER(BatchStats)]),
     "sdb_batch_free": (None, [c_void_p]),
+    "sdb_server_create": (c_int, [c_void_p, POINTER(ServerConfig), POINTER(c_void_p)]),
+    "sdb_server_submit": (c_int, [c_void_p, c_char_p, POINTER(c_int64)]),
+    "sdb_server_next": (c_int, [c_void_p, c_int, POINTER(c_int64), POINTER(c_int), POINTER(c_void_p),
+                                POINTER(c_double)]),
+    "sdb_server_stats_get": (c_int, [c_void_p, POINTER(ServerStats)]),
+    "sdb_server_destroy": (c_int, [c_void_p]),
+    "sdb_server_replay": (c_int, [c_void_p, POINTER(c_char_p), POINTER(c_double), c_int, POINTER(c_int),
+                                  POINTER(c_void_p), POINTER(c_double), POINTER(c_double)]),
+    "sdb_engine_replay_plain": (c_int, [c_void_p, POINTER(c_char_p), POINTER(c_double), c_int, POINTER(c_int),
+                                        POINTER(c_void_p), POINTER(c_double), POINTER(c_double)]),
 }
 
 _LIB = None
@@ -148,7 +171,8 @@ def lib():
             fn.restype = res
             fn.argtypes = args
         for cls, name in ((Operand, "sdb_operand"), (ChainOp, "sdb_chain_op"), (ChainDesc, "sdb_chain_desc"),
-                          (EngineConfig, "sdb_engine_config"), (BatchStats, "sdb_batch_stats")):
+                          (EngineConfig, "sdb_engine_config"), (BatchStats, "sdb_batch_stats"),
+                          (ServerConfig, "sdb_server_config"), (ServerStats, "sdb_server_stats")):
             n = L.sdb_abi_sizeof(name.encode())
             if n != ctypes.sizeof(cls):
                 raise RuntimeError("ABI mismatch for %s: C %d, ctypes %d" % (name, n, ctypes.sizeof(cls)))

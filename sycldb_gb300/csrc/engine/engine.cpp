@@ -36,6 +36,7 @@
 
 #include <cuda_runtime.h>
 
+#include "batch_api.hpp"
 #include "plan.hpp"
 #include "sycldb_gpu.h"
 
@@ -72,11 +73,6 @@ std::string base_name(const std::string &name)
     size_t at = name.find('@');
     return at == std::string::npos ? name : name.substr(0, at);
 }
-
-struct Error : std::runtime_error {
-    int status;
-    Error(int s, const std::string &m) : std::runtime_error(m), status(s) {}
-};
 
 #define SDB_CUDA(x)                                                                                   \
     do {                                                                                              \
@@ -169,13 +165,26 @@ public:
         used_ = zused_ = zdirty_ = peak_ = 0;
     }
 
+    // Carves the arena out of memory the caller owns (a server's pool); the
+    // caller clears the zeroed region before the work that uses it.
+    void init_external(char *base, uint64_t size, char *zbase, uint64_t zsize)
+    {
+        release();
+        external_ = true;
+        base_ = base;
+        zbase_ = zbase;
+        size_ = size;
+        zsize_ = zsize;
+        used_ = zused_ = zdirty_ = peak_ = 0;
+    }
+
     void release()
     {
-        if (!virtual_) {
+        if (!virtual_ && !external_) {
             if (base_) cudaFree(base_);
             if (zbase_) cudaFree(zbase_);
         }
-        virtual_ = false;
+        virtual_ = external_ = false;
         base_ = zbase_ = nullptr;
     }
 
@@ -190,6 +199,7 @@ public:
         std::swap(zused_, o.zused_);
         std::swap(zdirty_, o.zdirty_);
         std::swap(virtual_, o.virtual_);
+        std::swap(external_, o.external_);
     }
 
     uint64_t used() const { return used_; }
@@ -242,6 +252,7 @@ private:
     uint64_t size_ = 0, used_ = 0, peak_ = 0;
     uint64_t zsize_ = 0, zused_ = 0, zdirty_ = 0;
     bool virtual_ = false;
+    bool external_ = false;
 };
 
 // ------------------------------------------------------------------ storage
@@ -1470,13 +1481,17 @@ struct sdb_batch {
     int kernels = 0;
     int chain_groups = 0;
     double last_ms = 0;
+    // false: streams, events, staging and arena belong to the caller (a
+    // server slot), the batch runs once
+    bool owns = true;
 
     ~sdb_batch()
     {
+        if (cb) sdb_chain_batch_destroy(cb);
+        if (!owns) return;
         if (bs) cudaStreamSynchronize(bs);
         if (exec) cudaGraphExecDestroy(exec);
         if (graph) cudaGraphDestroy(graph);
-        if (cb) sdb_chain_batch_destroy(cb);
         for (auto s : side) cudaStreamDestroy(s);
         for (auto e : join) cudaEventDestroy(e);
         for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_c1})
@@ -1775,41 +1790,25 @@ void replay(sdb_batch &B, cudaStream_t main)
     };
     phase(false);
     if (B.cb) {
-        // external records: they stay timing events inside a captured graph
-        SDB_CUDA(cudaEventRecordWithFlags(B.ev_c0, main, cudaEventRecordExternal));
+        // under capture, external records: they stay timing events in the graph
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        SDB_CUDA(cudaStreamIsCapturing(main, &cs));
+        const unsigned rf = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+        if (B.ev_c0) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c0, main, rf));
         check(sdb_chain_batch_launch(B.cb, (sdb_stream_t)main));
-        SDB_CUDA(cudaEventRecordWithFlags(B.ev_c1, main, cudaEventRecordExternal));
+        if (B.ev_c1) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c1, main, rf));
     }
     phase(true);
 }
 
-void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plans)
+// Pinned staging of a recorded batch: per plan and segment, the count and
+// every result column at full capacity.  Lays it out (B.stage) and returns
+// its size.
+size_t staging_bytes(sdb_batch &B)
 {
-    // sizing pass: addresses only
-    MemoryManager vm;
-    vm.init_virtual();
-    record_plans(E, B, vm, plans);
-    const uint64_t used = vm.used(), zused = vm.zused();
-    const size_t cb_bytes = B.rec.chains.empty()
-                                ? 0
-                                : sdb_chain_batch_scratch_bytes(B.rec.chains.data(), (int)B.rec.chains.size());
-    vm.release();
-
-    // real pass against an arena of exactly that size
-    B.mm.init_sized(used + cb_bytes + 256, zused, E.stream);
-    record_plans(E, B, B.mm, plans);
-    if (!B.rec.chains.empty()) {
-        void *scratch = B.mm.alloc<uint8_t>(cb_bytes);
-        check(sdb_chain_batch_create(B.rec.chains.data(), (int)B.rec.chains.size(), scratch, cb_bytes,
-                                     (sdb_stream_t)E.stream, &B.cb));
-        B.chain_groups = sdb_chain_batch_kernels(B.cb);
-    }
-
-    // pinned staging: per plan and segment, the count and every column at
-    // full capacity; the copies go at the end of the plan's work
     size_t off = 0;
-    B.stage.assign(plans.size(), {});
-    for (size_t p = 0; p < plans.size(); p++) {
+    B.stage.assign(B.pend.size(), {});
+    for (size_t p = 0; p < B.pend.size(); p++) {
         const PendingResult &pr = B.pend[p];
         for (const PendingSeg &sg : pr.segs) {
             sdb_batch::Stage st;
@@ -1822,9 +1821,14 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
             B.stage[p].push_back(st);
         }
     }
-    B.host_bytes = std::max<size_t>(off, 64);
-    SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&B.host), B.host_bytes, cudaHostAllocDefault));
-    for (size_t p = 0; p < plans.size(); p++) {
+    return off;
+}
+
+// Appends to every plan the copies of its results into B.host (laid out by
+// staging_bytes), after the plan's last kernel.
+void add_result_copies(sdb_batch &B)
+{
+    for (size_t p = 0; p < B.pend.size(); p++) {
         PlanRecord &rp = B.rec.plans[p];
         auto &ops = rp.after ? rp.post : rp.pre;
         const PendingResult &pr = B.pend[p];
@@ -1850,6 +1854,70 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
             }
         }
     }
+}
+
+// Plan p's result from the staging of a finished run.
+sdb_result *unpack_result(const sdb_batch &B, size_t p)
+{
+    const PendingResult &pr = B.pend[p];
+    auto res = std::make_unique<sdb_result>();
+    res->types = pr.types;
+    const size_t ncols = pr.types.size();
+    res->i32.resize(ncols);
+    res->u64.resize(ncols);
+    std::vector<uint32_t> counts(pr.segs.size());
+    uint64_t total = 0;
+    for (size_t s = 0; s < pr.segs.size(); s++) {
+        std::memcpy(&counts[s], B.host + B.stage[p][s].count_off, 4);
+        if (counts[s] > pr.segs[s].cap) throw Error(SDB_ERR_DEVICE, "batch result count exceeds its capacity");
+        total += counts[s];
+    }
+    for (size_t c = 0; c < ncols; c++) {
+        if (pr.types[c] == 1)
+            res->u64[c].resize(total);
+        else
+            res->i32[c].resize(total);
+    }
+    uint64_t base = 0;
+    for (size_t s = 0; s < pr.segs.size(); s++) {
+        for (size_t c = 0; c < ncols; c++) {
+            const char *src = B.host + B.stage[p][s].col_off[c];
+            if (pr.types[c] == 1)
+                std::memcpy(res->u64[c].data() + base, src, counts[s] * sizeof(uint64_t));
+            else
+                std::memcpy(res->i32[c].data() + base, src, counts[s] * sizeof(int32_t));
+        }
+        base += counts[s];
+    }
+    res->nrows = total;
+    return res.release();
+}
+
+void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plans)
+{
+    // sizing pass: addresses only
+    MemoryManager vm;
+    vm.init_virtual();
+    record_plans(E, B, vm, plans);
+    const uint64_t used = vm.used(), zused = vm.zused();
+    const size_t cb_bytes = B.rec.chains.empty()
+                                ? 0
+                                : sdb_chain_batch_scratch_bytes(B.rec.chains.data(), (int)B.rec.chains.size());
+    vm.release();
+
+    // real pass against an arena of exactly that size
+    B.mm.init_sized(used + cb_bytes + 256, zused, E.stream);
+    record_plans(E, B, B.mm, plans);
+    if (!B.rec.chains.empty()) {
+        void *scratch = B.mm.alloc<uint8_t>(cb_bytes);
+        check(sdb_chain_batch_create(B.rec.chains.data(), (int)B.rec.chains.size(), scratch, cb_bytes,
+                                     (sdb_stream_t)E.stream, &B.cb));
+        B.chain_groups = sdb_chain_batch_kernels(B.cb);
+    }
+
+    B.host_bytes = std::max<size_t>(staging_bytes(B), 64);
+    SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&B.host), B.host_bytes, cudaHostAllocDefault));
+    add_result_copies(B);
 
     // streams and events; the plans' work is spread over up to 8 streams
     SDB_CUDA(cudaStreamCreateWithFlags(&B.bs, cudaStreamNonBlocking));
@@ -1911,40 +1979,77 @@ void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
         B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_c0, B.ev_c1) == cudaSuccess ? cms : -1.0;
     }
     if (!out) return;
-    for (size_t p = 0; p < B.pend.size(); p++) {
-        const PendingResult &pr = B.pend[p];
-        auto res = std::make_unique<sdb_result>();
-        res->types = pr.types;
-        const size_t ncols = pr.types.size();
-        res->i32.resize(ncols);
-        res->u64.resize(ncols);
-        std::vector<uint32_t> counts(pr.segs.size());
-        uint64_t total = 0;
-        for (size_t s = 0; s < pr.segs.size(); s++) {
-            std::memcpy(&counts[s], B.host + B.stage[p][s].count_off, 4);
-            if (counts[s] > pr.segs[s].cap) throw Error(SDB_ERR_DEVICE, "batch result count exceeds its capacity");
-            total += counts[s];
-        }
-        for (size_t c = 0; c < ncols; c++) {
-            if (pr.types[c] == 1)
-                res->u64[c].resize(total);
-            else
-                res->i32[c].resize(total);
-        }
-        uint64_t base = 0;
-        for (size_t s = 0; s < pr.segs.size(); s++) {
-            for (size_t c = 0; c < ncols; c++) {
-                const char *src = B.host + B.stage[p][s].col_off[c];
-                if (pr.types[c] == 1)
-                    std::memcpy(res->u64[c].data() + base, src, counts[s] * sizeof(uint64_t));
-                else
-                    std::memcpy(res->i32[c].data() + base, src, counts[s] * sizeof(int32_t));
-            }
-            base += counts[s];
-        }
-        res->nrows = total;
-        out[p] = res.release();
+    for (size_t p = 0; p < B.pend.size(); p++) out[p] = unpack_result(B, p);
+}
+
+// ------------------------------------------------------------------ batches on caller memory
+// Used by the request server: a batch sized from a sizing pass, built on
+// memory carved from the server's pools and run once, eagerly, on a slot's
+// streams.
+
+BatchSize batch_size(sdb_engine *eng, const std::vector<std::string> &plans)
+{
+    Engine &E = eng->E;
+    sdb_batch B;
+    MemoryManager vm;
+    vm.init_virtual();
+    record_plans(E, B, vm, plans);
+    BatchSize z;
+    z.arena = vm.used();
+    z.zero = vm.zused();
+    z.staging = staging_bytes(B);
+    z.chains = B.rec.chains;
+    return z;
+}
+
+size_t batch_chain_bytes(const std::vector<sdb_chain_desc> &chains)
+{
+    return chains.empty() ? 0 : sdb_chain_batch_scratch_bytes(chains.data(), (int)chains.size());
+}
+
+sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string> &plans, const BatchSize &z,
+                                 char *dev, size_t dev_bytes, char *pinned, size_t pinned_bytes, const SlotStreams &ss)
+{
+    Engine &E = eng->E;
+    auto Bp = std::make_unique<sdb_batch>();
+    sdb_batch &B = *Bp;
+    B.eng = eng;
+    B.owns = false;
+    const uint64_t arena = (z.arena + 255) & ~uint64_t(255), zero = (z.zero + 255) & ~uint64_t(255);
+    const size_t cb_bytes = batch_chain_bytes(z.chains);
+    if (arena + zero + cb_bytes > dev_bytes) throw Error(SDB_ERR_INVALID, "batch region too small");
+    B.mm.init_external(dev, arena, dev + arena, zero);
+    record_plans(E, B, B.mm, plans);
+    if (B.mm.used() != z.arena || B.mm.zused() != z.zero) throw Error(SDB_ERR_INVALID, "batch sizing mismatch");
+    const size_t stage = staging_bytes(B);
+    if (cb_bytes + stage > pinned_bytes) throw Error(SDB_ERR_INVALID, "batch staging too small");
+    B.host = pinned + cb_bytes;
+    B.host_bytes = stage;
+    add_result_copies(B);
+    B.side = ss.side;
+    B.join = ss.join;
+    B.fork = ss.fork;
+    if (!B.rec.chains.empty())
+        check(sdb_chain_batch_create_async(B.rec.chains.data(), (int)B.rec.chains.size(), dev + arena + zero, cb_bytes,
+                                           pinned, cb_bytes, (sdb_stream_t)ss.main, &B.cb));
+    replay(B, ss.main);
+    return Bp.release();
+}
+
+sdb_result *batch_take_result(const sdb_batch *B, size_t p) { return unpack_result(*B, p); }
+
+sdb_result *execute_plain(sdb_engine *eng, const std::string &plan) { return execute_plan(eng->E, plan).release(); }
+
+void batch_destroy(sdb_batch *B)
+{
+    if (B && !B->owns) {
+        // the slot's streams and events are not the batch's
+        B->side.clear();
+        B->join.clear();
+        B->fork = nullptr;
+        B->host = nullptr;
     }
+    delete B;
 }
 
 template <class F>

@@ -66,6 +66,8 @@ size_t sdb_abi_sizeof(const char *type_name)
     if (t == "sdb_chain_desc") return sizeof(sdb_chain_desc);
     if (t == "sdb_engine_config") return sizeof(sdb_engine_config);
     if (t == "sdb_batch_stats") return sizeof(sdb_batch_stats);
+    if (t == "sdb_server_config") return sizeof(sdb_server_config);
+    if (t == "sdb_server_stats") return sizeof(sdb_server_stats);
     return 0;
 }
 

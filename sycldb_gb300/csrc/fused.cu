@@ -1561,8 +1561,8 @@ size_t sdb_chain_batch_scratch_bytes(const sdb_chain_desc *chains, int n_chains)
     return std::max<size_t>(bp.bytes, 256);
 }
 
-int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
-                           sdb_stream_t stream, sdb_chain_batch **out)
+static int chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
+                              void *host_staging, size_t host_bytes, sdb_stream_t stream, sdb_chain_batch **out)
 {
     if (!out) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create: NULL out");
     *out = nullptr;
@@ -1573,7 +1573,17 @@ int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev
         return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create: scratch of %zu bytes, %zu needed", dev_bytes,
                              bp.bytes);
     if (!sdb::aligned(dev_scratch, 256)) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create: scratch not 256-byte aligned");
-    std::vector<char> host(bp.bytes, 0);
+    if (host_staging && host_bytes < bp.bytes)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create_async: staging of %zu bytes, %zu needed",
+                             host_bytes, bp.bytes);
+    std::vector<char> own;
+    char *host = static_cast<char *>(host_staging);
+    if (!host) {
+        own.assign(bp.bytes, 0);
+        host = own.data();
+    } else {
+        std::memset(host, 0, bp.bytes);
+    }
     auto *b = new sdb_chain_batch;
     char *dev = static_cast<char *>(dev_scratch);
     size_t off = round256(bp.groups.size() * sizeof(uint32_t));
@@ -1588,10 +1598,10 @@ int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev
         o.first = G.launches[0];
         o.head = b->heads + g;
         o.bitmap_words = G.bitmap_words;
-        std::memcpy(host.data() + off, G.launches.data(), G.launches.size() * sizeof(dense::Launch));
+        std::memcpy(host + off, G.launches.data(), G.launches.size() * sizeof(dense::Launch));
         o.launches = reinterpret_cast<const dense::Launch *>(dev + off);
         off += round256(G.launches.size() * sizeof(dense::Launch));
-        std::memcpy(host.data() + off, G.spans.data(), G.spans.size() * sizeof(dense::Span));
+        std::memcpy(host + off, G.spans.data(), G.spans.size() * sizeof(dense::Span));
         o.spans = reinterpret_cast<const dense::Span *>(dev + off);
         o.n_spans = (uint32_t)G.spans.size();
         off += round256(G.spans.size() * sizeof(dense::Span));
@@ -1600,8 +1610,8 @@ int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev
     b->singles = bp.singles;
     cudaStream_t s = (cudaStream_t)stream;
     if (bp.bytes) {
-        cudaError_t e = cudaMemcpyAsync(dev_scratch, host.data(), bp.bytes, cudaMemcpyHostToDevice, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        cudaError_t e = cudaMemcpyAsync(dev_scratch, host, bp.bytes, cudaMemcpyHostToDevice, s);
+        if (e == cudaSuccess && !host_staging) e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             delete b;
             return sdb_set_error(SDB_ERR_CUDA, "sdb_chain_batch_create: %s", cudaGetErrorString(e));
@@ -1609,6 +1619,19 @@ int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev
     }
     *out = b;
     return SDB_OK;
+}
+
+int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
+                           sdb_stream_t stream, sdb_chain_batch **out)
+{
+    return chain_batch_create(chains, n_chains, dev_scratch, dev_bytes, nullptr, 0, stream, out);
+}
+
+int sdb_chain_batch_create_async(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
+                                 void *host_staging, size_t host_bytes, sdb_stream_t stream, sdb_chain_batch **out)
+{
+    if (!host_staging) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_create_async: NULL staging");
+    return chain_batch_create(chains, n_chains, dev_scratch, dev_bytes, host_staging, host_bytes, stream, out);
 }
 
 int sdb_chain_batch_launch(const sdb_chain_batch *b, sdb_stream_t stream)

@@ -218,3 +218,85 @@ class Batch:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Server:
+    """Continuous batching of arriving plans (``sdb_server_*``): a native
+    dispatcher thread admits waiting plans against a device budget into up to
+    ``slots`` batches in flight.  While a server exists its engine must not be
+    used otherwise."""
+
+    def __init__(self, engine: Engine, budget_bytes: int = 0, pinned_bytes: int = 0, slots: int = 0,
+                 max_batch: int = 0, streams_per_slot: int = 0):
+        L = capi.lib()
+        cfg = capi.ServerConfig(budget_bytes, pinned_bytes, slots, max_batch, streams_per_slot, 0)
+        h = ctypes.c_void_p()
+        capi.check(L.sdb_server_create(engine._h, ctypes.byref(cfg), ctypes.byref(h)))
+        self._h = h
+        self._engine = engine
+
+    def submit(self, plan) -> int:
+        text = plan if isinstance(plan, str) else json.dumps(plan)
+        rid = ctypes.c_int64()
+        capi.check(capi.lib().sdb_server_submit(self._h, text.encode(), ctypes.byref(rid)))
+        return rid.value
+
+    def next(self, timeout_ms: int = -1):
+        """(id, status, Result or None, latency_ms, error message) of the next
+        finished request; raises SdbError(SDB_ERR_TIMEOUT) if none finished in
+        time."""
+        L = capi.lib()
+        rid, st, r, ms = ctypes.c_int64(), ctypes.c_int(), ctypes.c_void_p(), ctypes.c_double()
+        capi.check(L.sdb_server_next(self._h, timeout_ms, ctypes.byref(rid), ctypes.byref(st), ctypes.byref(r),
+                                     ctypes.byref(ms)))
+        err = "" if st.value == capi.SDB_OK else capi.last_error()
+        res = _take_result(r) if r.value else None
+        return rid.value, st.value, res, ms.value, err
+
+    def stats(self) -> dict:
+        st = capi.ServerStats()
+        capi.check(capi.lib().sdb_server_stats_get(self._h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in capi.ServerStats._fields_}
+
+    def replay(self, plans, arrivals_s, keep_results: bool = True):
+        """Open-loop replay of an arrival trace; returns (statuses, latencies_ms,
+        results or None, wall_s)."""
+        return _replay(capi.lib().sdb_server_replay, self._h, plans, arrivals_s, keep_results)
+
+    def close(self):
+        if getattr(self, "_h", None):
+            capi.lib().sdb_server_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def replay_plain(engine: Engine, plans, arrivals_s, keep_results: bool = True):
+    """The plain path over the same trace: one plan at a time in arrival order."""
+    return _replay(capi.lib().sdb_engine_replay_plain, engine._h, plans, arrivals_s, keep_results)
+
+
+def _replay(fn, handle, plans, arrivals_s, keep_results):
+    n = len(plans)
+    texts = [(p if isinstance(p, str) else json.dumps(p)).encode() for p in plans]
+    arr = (ctypes.c_char_p * n)(*texts)
+    at = (ctypes.c_double * n)(*[float(x) for x in arrivals_s])
+    st = (ctypes.c_int * n)()
+    lat = (ctypes.c_double * n)()
+    res = (ctypes.c_void_p * n)() if keep_results else None
+    wall = ctypes.c_double()
+    capi.check(fn(handle, arr, at, n, st, res, lat, ctypes.byref(wall)))
+    results = None
+    if keep_results:
+        results = [_take_result(ctypes.c_void_p(res[i])) if res[i] else None for i in range(n)]
+    return list(st), list(lat), results, wall.value

@@ -1,0 +1,106 @@
+"""The served form on the GPU: plans arriving as a Poisson stream are admitted
+against a device budget and batched while others run.  Every result must be
+the one the plan gives alone (exactly: integer keys and uint64 sums), and the
+plain one-at-a-time replay of the same trace must give the same results."""
+import numpy as np
+import pytest
+
+from sycldb_gb300 import capi, plans, workloads
+from sycldb_gb300.engine import Engine, Server, replay_plain
+from tests import datasets
+
+pytestmark = pytest.mark.gpu
+
+SF = 0.2
+
+
+@pytest.fixture(scope="module")
+def ds():
+    return datasets.dataset(SF)
+
+
+def make_engine(ds, **kw):
+    eng = Engine(arena_bytes=1 << 30, **kw)
+    for name, cols in ds.items():
+        eng.load_table(name, cols)
+    return eng
+
+
+def trace(rate, n, seed=5):
+    reqs = workloads.poisson_stream(rate, n, seed=seed)
+    return [r.plan for r in reqs], [r.t for r in reqs]
+
+
+@pytest.mark.parametrize("seg", [0, 1 << 18])
+def test_each_result_is_the_same_alone_and_in_the_mix(ds, seg):
+    pls, at = trace(2000, 240)
+    with make_engine(ds, segment_rows=seg) as eng:
+        alone = [eng.execute(p).canonical() for p in pls]
+        with Server(eng, budget_bytes=8 << 30) as srv:
+            st, lat, res, wall = srv.replay(pls, at)
+            stats = srv.stats()
+        assert st == [capi.SDB_OK] * len(pls)
+        assert [r.canonical() for r in res] == alone
+        assert all(x >= 0 for x in lat) and wall > 0
+        assert stats["completed"] == len(pls) and stats["failed"] == 0
+        assert stats["batches"] < len(pls)  # requests were batched
+        assert stats["peak_device_bytes"] <= stats["budget_bytes"]
+        pst, plat, pres, pwall = replay_plain(eng, pls, at)
+        assert pst == [capi.SDB_OK] * len(pls)
+        assert [r.canonical() for r in pres] == alone
+    # a few against the oracle too
+    for i in (0, 1, 2, 3, 57, 150):
+        assert alone[i] == datasets.oracle_run(ds, pls[i], seg or None)
+
+
+def test_submit_and_next_burst(ds):
+    pls, _ = trace(1000, 60, seed=9)
+    with make_engine(ds) as eng:
+        alone = [eng.execute(p).canonical() for p in pls]
+        with Server(eng, budget_bytes=4 << 30, slots=2, max_batch=16) as srv:
+            ids = [srv.submit(p) for p in pls]
+            got = {}
+            for _ in pls:
+                rid, st, res, ms, err = srv.next(timeout_ms=60_000)
+                assert st == capi.SDB_OK, err
+                got[rid] = res.canonical()
+            stats = srv.stats()
+            with pytest.raises(capi.SdbError) as e:
+                srv.next(timeout_ms=10)
+            assert e.value.status == capi.SDB_ERR_TIMEOUT
+    assert [got[i] for i in ids] == alone
+    assert 1 < stats["max_batch_plans"] <= 16
+
+
+def test_admission_under_a_small_budget(ds):
+    """A budget that holds only a few plans at once: everything still
+    finishes, correctly, and in-flight memory never exceeds the budget; bad
+    plans and plans larger than the whole budget fail alone."""
+    pls, at = trace(3000, 80, seed=13)
+    with make_engine(ds) as eng:
+        alone = [eng.execute(p).canonical() for p in pls]
+        budget = 24 << 20
+        with Server(eng, budget_bytes=budget, slots=4) as srv:
+            st, lat, res, wall = srv.replay(pls, at)
+            stats = srv.stats()
+            bad = srv.submit(plans.plan_filter_sum(1994, fact_tag=77))  # no such table
+            rid, s_bad, r_bad, _, err = srv.next(timeout_ms=30_000)
+        assert st == [capi.SDB_OK] * len(pls)
+        assert [r.canonical() for r in res] == alone
+        assert stats["peak_device_bytes"] <= budget
+        assert rid == bad and s_bad == capi.SDB_ERR_INVALID and r_bad is None and "not found" in err
+        with Server(eng, budget_bytes=1 << 20) as tiny:
+            rid = tiny.submit(pls[0])
+            _, s, r, _, err = tiny.next(timeout_ms=30_000)
+        assert s == capi.SDB_ERR_NOMEM and r is None
+
+
+def test_server_is_reusable_after_destroy(ds):
+    pls, at = trace(500, 20, seed=21)
+    with make_engine(ds) as eng:
+        alone = [eng.execute(p).canonical() for p in pls]
+        for _ in range(2):
+            with Server(eng, budget_bytes=2 << 30) as srv:
+                st, _, res, _ = srv.replay(pls, at)
+            assert [r.canonical() for r in res] == alone
+        assert eng.execute(pls[0]).canonical() == alone[0]  # the engine works again afterwards
