@@ -19,6 +19,12 @@ to result rows in host memory.
              prepared batch (one CUDA graph, one persistent chain-batch launch)
              against the same 64 plans executed one at a time, results
              compared plan by plan
+  served     SF50 fact (300M rows x 17 columns) resident; a seeded Poisson
+             stream of mixed plans (filter-sum, date join, star join, star join
+             with year/brand windows) replayed open-loop through the request
+             server (continuous batching, 60 GB admission budget) and through
+             the plain one-at-a-time path: queries/s and p50/p99 latency per
+             arrival rate, results compared request by request
 
 --impl reference times the reference path's CPU restatement (the oracle port:
 the reference itself needs AdaptiveCpp, oneDPL and Thrift and cannot be built
@@ -59,6 +65,9 @@ def parse_args():
     ap.add_argument("--batched-runs", type=int, default=20,
                     help="timed runs of the 64-plan batch (0 skips the batched form)")
     ap.add_argument("--plain-rounds", type=int, default=3, help="timed rounds of the 64 plans one at a time")
+    ap.add_argument("--served-rates", default="50,200,500,1000,2000",
+                    help="Poisson arrival rates (queries/s) of the served form; empty skips it")
+    ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival span per rate (at least 100 requests)")
     return ap.parse_args()
 
 
@@ -305,6 +314,7 @@ def run_ours(args, rank, world, local, pg):
     del fact
     torch.cuda.empty_cache()
     batched = run_batched(args, rank, world, local, pg, stream, peak) if args.batched_runs > 0 else None
+    served = run_served(args, rank, world, local, pg, stream) if args.served_rates.strip() else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -316,6 +326,7 @@ def run_ours(args, rank, world, local, pg):
         "roofline": roof,
         "e2e": e2e,
         "batched": batched,
+        "served": served,
         "gpu_launches": launches,
         "kernel_ms_last_step": {k: v[1] for k, v in stats_last.items()},
         "clocks": clk,
@@ -450,6 +461,58 @@ def run_batched(args, rank, world, local, pg, stream, peak):
         "arena_bytes": st["arena_bytes"], "bit_exact_vs_plain": exact,
         "plain_rounds": args.plain_rounds, "batched_runs": args.batched_runs, "clocks": clk,
     }
+
+
+def run_served(args, rank, world, local, pg, stream):
+    """The served form against the plain path on the same arrival traces."""
+    import torch
+
+    from sycldb_gb300 import ssb, workloads
+    from sycldb_gb300.engine import Engine, Server, replay_plain
+
+    sf = 50.0
+    n = ssb.fact_rows(sf)
+    eng = Engine(fuse=True, stream=stream.cuda_stream)
+    fact = ssb.gen_lineorder_device(n, range(17), sf, salt=rank)
+    eng.load_table("lineorder", fact)
+    for t, c in dims_host(sf).items():
+        eng.load_table(t, c)
+    torch.cuda.synchronize()
+    rates = [float(x) for x in args.served_rates.split(",") if x.strip()]
+    out = []
+    clocks = ClockSampler(local)
+    clocks.start()
+    for rate in rates:
+        nreq = max(100, int(rate * args.served_seconds))
+        reqs = workloads.poisson_stream(rate, nreq, seed=ssb.SEED + rank)
+        pls = [r.plan for r in reqs]
+        at = [r.t for r in reqs]
+        # warm both paths on a short prefix
+        replay_plain(eng, pls[:8], [0.0] * 8, keep_results=False)
+        pst, plat, pres, pwall = replay_plain(eng, pls, at)
+        with Server(eng, budget_bytes=60 << 30) as srv:
+            srv.replay(pls[:8], [0.0] * 8, keep_results=False)
+            sst, slat, sres, swall = srv.replay(pls, at)
+            st = srv.stats()
+        ok = all(x == 0 for x in pst) and all(x == 0 for x in sst)
+        exact = ok and all(a.canonical() == b.canonical() for a, b in zip(pres, sres))
+        out.append({
+            "rate_qps": rate, "requests": nreq,
+            "served": {"qps": nreq / swall, "p50_ms": _pct(slat, 50), "p99_ms": _pct(slat, 99),
+                       "batches": st["batches"] - 1, "mean_batch": (st["batched_plans"] - 8) / max(1, st["batches"] - 1),
+                       "max_inflight_plans": st["max_inflight_plans"], "peak_device_bytes": st["peak_device_bytes"]},
+            "plain": {"qps": nreq / pwall, "p50_ms": _pct(plat, 50), "p99_ms": _pct(plat, 99)},
+            "bit_exact": exact,
+        })
+    clk = clocks.stop()
+    eng.close()
+    del fact
+    torch.cuda.empty_cache()
+    return {"workload": "SF50 lineorder resident (%d rows x 17 int32 columns), SF50 dimensions; Poisson arrivals, "
+                        "plan mix 1/4 each: filter-project-sum (one-year window, discount range, quantity bound), "
+                        "filter + date join + group by year, star join, star join with year and brand windows" % n,
+            "latency": "host wall clock from each request's scheduled arrival to its result on the host",
+            "budget_bytes": 60 << 30, "slots": 4, "rates": out, "clocks": clk}
 
 
 def main():

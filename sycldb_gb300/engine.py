@@ -55,6 +55,20 @@ class Result:
         return r
 
 
+_TUNING_LOADED = False
+
+
+def _load_tuning_once():
+    """The first engine of a process loads the committed autotuner table
+    (``SYCLDB_TUNING`` names another file; an empty value skips it)."""
+    global _TUNING_LOADED
+    if not _TUNING_LOADED:
+        _TUNING_LOADED = True
+        from . import autotune
+
+        autotune.load_default()
+
+
 def _take_result(r) -> Result:
     """Copies a native sdb_result into numpy columns and frees it."""
     L = capi.lib()
@@ -81,6 +95,7 @@ class Engine:
     def __init__(self, arena_bytes: int = 0, segment_rows: int = 0, fuse: bool = True, profile: bool = False,
                  stream: Optional[int] = None):
         L = capi.lib()
+        _load_tuning_once()
         cfg = capi.EngineConfig(arena_bytes, segment_rows, 1 if fuse else 0, 1 if profile else 0, stream or None)
         h = ctypes.c_void_p()
         capi.check(L.sdb_engine_create(ctypes.byref(cfg), ctypes.byref(h)))

@@ -1,0 +1,30 @@
+"""The autotuner's table format and its loading into the library (no GPU)."""
+import json
+
+from sycldb_gb300 import autotune, capi
+
+
+def test_rows_bucket_matches_the_library():
+    for n in (1, 2, 3, 1023, 1024, 1 << 20, 120_000_000, 300_000_000):
+        assert 2 ** autotune.rows_bucket(n) <= n < 2 ** (autotune.rows_bucket(n) + 1)
+
+
+def test_load_sets_the_tuning_table(tmp_path):
+    L = capi.lib()
+    table = {"entries": [{"terminal": "groupby", "nregs": 2, "rows_bucket": 26, "variant": 4},
+                         {"terminal": "sum", "nregs": 1, "rows_bucket": 20, "variant": 3}]}
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps(table))
+    try:
+        assert autotune.load_default(str(p)) == table
+        assert L.sdb_chain_tune_get(2, 2, 1 << 26) == 4
+        assert L.sdb_chain_tune_get(2, 2, (1 << 27) - 1) == 4
+        assert L.sdb_chain_tune_get(1, 1, 1 << 20) == 3
+        assert L.sdb_chain_tune_get(1, 1, 1 << 21) in range(6)
+    finally:
+        capi.force_chain_variant(-1)
+        autotune.load_default()
+
+
+def test_missing_table_is_not_an_error(tmp_path):
+    assert autotune.load_default(str(tmp_path / "absent.json")) is None
