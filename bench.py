@@ -49,12 +49,41 @@ METRIC = "rows/s & %HBM roofline (SF20 star join); batched qps + p99 vs plain"
 UNIT = "rows/s"
 SF = 20.0
 REGION, CATEGORY = 2, 11
+
+
+def _plan_star():
+    from sycldb_gb300 import plans
+
+    return plans.plan_star(REGION, CATEGORY)
+
+
+def _plan_filter_sum():
+    from sycldb_gb300 import plans
+
+    return plans.plan_filter_sum(1994)
+
+
+def _plan_date_join():
+    from sycldb_gb300 import plans
+
+    return plans.plan_date_join(1994)
+
+
+# name -> (plan builder, fact columns key, dominant kernel)
+PLANS = {
+    "star": (_plan_star, "star", "k_dense (fused chain: semi + full + full probe, warp compaction, group-by)"),
+    "filter_sum": (_plan_filter_sum, "q1", "k_dense (fused chain: range + range + select + projection, sum)"),
+    "date_join": (_plan_date_join, "q2", "k_dense (fused chain: range + full probe + projection, group-by)"),
+}
 PROFILE_SUMMARY = os.path.join(ROOT, "profiles", "fused_chain_star_sf20.txt")
 
 
 def parse_args():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--plan", default="star", choices=sorted(PLANS),
+                    help="plan of the main measurement (the headline is the star join; the others profile the "
+                         "filter-sum and date-join passes)")
     ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
@@ -251,8 +280,9 @@ def run_ours(args, rank, world, local, pg):
     L = capi.lib()
     sf = args.sf
     n = ssb.fact_rows(sf)
-    cols = ssb.QUERY_COLUMNS["star"]
-    plan = plans.plan_star(REGION, CATEGORY)
+    build_plan, cols_key, kernel_name = PLANS[args.plan]
+    cols = ssb.QUERY_COLUMNS[cols_key]
+    plan = build_plan()
     dims = dims_host(sf)
     fact = ssb.gen_lineorder_device(n, cols, sf, salt=rank)
     torch.cuda.synchronize()
@@ -301,8 +331,8 @@ def run_ours(args, rank, world, local, pg):
     alg_bytes = 4 * len(cols) * n
     per_launch_ms = fused_ms / max(1, fused_launches)
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if fused_launches else None
-    traffic = profile_traffic()
-    roof = {"kernel": "k_dense (fused chain: semi + full + full probe, warp compaction, group-by)", "bound": "hbm",
+    traffic = profile_traffic() if (args.plan == "star" and sf == SF) else None
+    roof = {"kernel": kernel_name, "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
@@ -320,7 +350,8 @@ def run_ours(args, rank, world, local, pg):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int32/uint64", "data": "synthetic (seeded SplitMix64 columns, SSB SF20 shapes)",
-        "config": {"workload": workload_name(sf), "fact_rows_per_gpu": n, "groups": n_groups,
+        "config": {"workload": workload_name(sf) if args.plan == "star" else "%s plan, SF%g (%d fact rows)" % (
+                       args.plan, sf, n), "fact_rows_per_gpu": n, "groups": n_groups,
                    "l2": "inputs larger than L2 (%.2f GB of fact columns per step)" % (alg_bytes / 1e9),
                    "segment_rows": 1 << 28, "fused": True, "parallelism": "replicas" if world > 1 else "1 GPU"},
         "roofline": roof,

@@ -80,6 +80,13 @@ __host__ __device__ __forceinline__ int64_t ht_slot(int32_t x, int32_t len, int3
 // back into an int.
 __host__ __device__ __forceinline__ int64_t group_slot(uint32_t hash, uint64_t P)
 {
+    // same value as the general form below: a non-negative hash below P is
+    // its own slot (every key tuple inside its ranges), and a non-negative
+    // hash needs only a 32-bit remainder when P fits 32 bits
+    if ((int32_t)hash >= 0) {
+        if ((uint64_t)hash < P) return (int64_t)hash;
+        if (P <= 0xffffffffull) return (int64_t)(hash % (uint32_t)P);
+    }
     return (int64_t)(int32_t)(uint32_t)((uint64_t)(int64_t)(int32_t)hash % P);
 }
 

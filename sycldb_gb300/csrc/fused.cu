@@ -1489,13 +1489,18 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
 {
     if (n_chains < 0 || (n_chains > 0 && !chains)) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch: bad chain list");
     constexpr uint64_t kTile = (uint64_t)kThreads * dense::kItems;
-    uint64_t total_tiles = 0;
+    // chains grouped by the shape-specialised instantiation they map to
     struct Item {
+        int index;
         dense::Launch D;
-        int term, compact, stages, shape;
         uint64_t tiles;
     };
-    std::vector<Item> items;
+    struct Family {
+        int shape, term, nregs;
+        uint64_t rows = 0;
+        std::vector<Item> items;
+    };
+    std::vector<Family> fams;
     for (int i = 0; i < n_chains; i++) {
         ChainLaunch L;
         int nregs = 1, term = 0;
@@ -1503,47 +1508,56 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         if (st != SDB_OK) return st;
         if (L.d.n == 0) continue;
         Item it;
-        int variant = -1;
-        if (g_tune_init) variant = g_tune[term][reg_class(nregs)][rows_bucket(L.d.n)];
-        if (variant < 0) variant = kCompact2Variant;
-        it.term = term;
-        it.compact = variant != kDenseVariant;
-        it.stages = variant == kCompact2Variant ? 2 : 3;
+        it.index = i;
         dense::ShapeProbe probe;
-        if (variant < kDenseVariant || !dense::convert(L, nregs, it.D) ||
-            dense::with_shape(it.D, term, it.compact, probe) != SDB_OK || (L.d.n + kTile - 1) / kTile > 0xffffffffull) {
+        if (!dense::convert(L, nregs, it.D) || dense::with_shape(it.D, term, 1, probe) != SDB_OK ||
+            (L.d.n + kTile - 1) / kTile > 0xffffffffull) {
             bp.singles.push_back(chains[i]);
             continue;
         }
-        it.shape = probe.id;
         it.tiles = (L.d.n + kTile - 1) / kTile;
-        total_tiles += it.tiles;
-        items.push_back(it);
+        size_t f = 0;
+        while (f < fams.size() && !(fams[f].shape == probe.id && fams[f].term == term)) f++;
+        if (f == fams.size()) fams.push_back(Family{probe.id, term, nregs});
+        fams[f].nregs = std::max(fams[f].nregs, nregs);
+        fams[f].rows += L.d.n;
+        fams[f].items.push_back(it);
+    }
+    // one launch per family, its variant tuned on the family's total rows
+    uint64_t total_tiles = 0;
+    std::vector<BatchPlan::G> groups;
+    std::vector<const Family *> of;
+    for (const Family &F : fams) {
+        int variant = g_tune_init ? g_tune[F.term][reg_class(F.nregs)][rows_bucket(F.rows)] : -1;
+        if (variant < 0) variant = kCompact2Variant;
+        if (variant < kDenseVariant) {  // the general pass: chain by chain
+            for (const Item &it : F.items) bp.singles.push_back(chains[it.index]);
+            continue;
+        }
+        BatchPlan::G g;
+        g.term = F.term;
+        g.compact = variant != kDenseVariant;
+        g.stages = variant == kCompact2Variant ? 2 : 3;
+        g.shape = F.shape;
+        groups.push_back(g);
+        of.push_back(&F);
+        for (const Item &it : F.items) total_tiles += it.tiles;
     }
     // spans of S tiles: about 8 per resident block over the whole batch
     const uint64_t target = (uint64_t)num_sms() * 5 * 8;
     uint64_t S = (total_tiles + target - 1) / std::max<uint64_t>(target, 1);
     S = std::min<uint64_t>(std::max<uint64_t>(S, 2), 64);
-    for (const Item &it : items) {
-        size_t g = 0;
-        while (g < bp.groups.size() &&
-               !(bp.groups[g].shape == it.shape && bp.groups[g].term == it.term && bp.groups[g].stages == it.stages))
-            g++;
-        if (g == bp.groups.size()) {
-            BatchPlan::G ng;
-            ng.term = it.term;
-            ng.compact = it.compact;
-            ng.stages = it.stages;
-            ng.shape = it.shape;
-            bp.groups.push_back(ng);
+    for (size_t g = 0; g < groups.size(); g++) {
+        BatchPlan::G &G = groups[g];
+        for (const Item &it : of[g]->items) {
+            const uint32_t c = (uint32_t)G.launches.size();
+            G.launches.push_back(it.D);
+            if (it.D.bitmap_ht) G.bitmap_words = std::max<uint32_t>(G.bitmap_words, (it.D.bitmap_len + 31) / 32);
+            for (uint64_t t = 0; t < it.tiles; t += S)
+                G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + S, it.tiles), 0});
         }
-        BatchPlan::G &G = bp.groups[g];
-        const uint32_t c = (uint32_t)G.launches.size();
-        G.launches.push_back(it.D);
-        if (it.D.bitmap_ht) G.bitmap_words = std::max<uint32_t>(G.bitmap_words, (it.D.bitmap_len + 31) / 32);
-        for (uint64_t t = 0; t < it.tiles; t += S)
-            G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + S, it.tiles), 0});
     }
+    bp.groups = std::move(groups);
     bp.bytes = round256(bp.groups.size() * sizeof(uint32_t));
     for (const auto &G : bp.groups)
         bp.bytes += round256(G.launches.size() * sizeof(dense::Launch)) + round256(G.spans.size() * sizeof(dense::Span));
