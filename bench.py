@@ -94,6 +94,10 @@ def parse_args():
     ap.add_argument("--batched-runs", type=int, default=20,
                     help="timed runs of the 64-plan batch (0 skips the batched form)")
     ap.add_argument("--plain-rounds", type=int, default=3, help="timed rounds of the 64 plans one at a time")
+    ap.add_argument("--batched-plans", type=int, default=64, help="plans (fact partitions) in the batch")
+    ap.add_argument("--batched-median", type=float, default=7e6,
+                    help="median partition rows (lognormal, clipped to [1M, 50M]); smaller values make a small "
+                         "case of the same kernel for profiling")
     ap.add_argument("--served-rates", default="50,200,500,1000,2000",
                     help="Poisson arrival rates (queries/s) of the served form; empty skips it")
     ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival span per rate (at least 100 requests)")
@@ -420,7 +424,7 @@ def run_batched(args, rank, world, local, pg, stream, peak):
     from sycldb_gb300 import ssb, workloads
     from sycldb_gb300.engine import Engine
 
-    wl = workloads.batch_workload(seed=ssb.SEED + rank)
+    wl = workloads.batch_workload(n_plans=args.batched_plans, median=args.batched_median, seed=ssb.SEED + rank)
     eng = Engine(arena_bytes=int(args.arena_gb * (1 << 30)), fuse=True, stream=stream.cuda_stream)
     workloads.load_batch_tables(eng, wl, device=True)
     pls = wl.plans()
@@ -472,8 +476,8 @@ def run_batched(args, rank, world, local, pg, stream, peak):
     return {
         "workload": "%d star-join plans (supplier region semi join, part category + brand window, date year "
                     "window; group by (d_year, p_brand1), SUM(lo_revenue)), each over its own fact partition; "
-                    "partition rows lognormal (median 7M, log-sd 1) clipped to [1M, 50M], total %d rows; SF20 "
-                    "dimensions" % (nq, wl.total_rows),
+                    "partition rows lognormal (median %g, log-sd 1) clipped to [1M, 50M], total %d rows; SF20 "
+                    "dimensions" % (nq, args.batched_median, wl.total_rows),
         "partition_rows": {"min": min(wl.rows), "max": max(wl.rows), "total": wl.total_rows},
         "group_counts": {"min": min(len(r) for r in alone), "max": max(len(r) for r in alone)},
         "qps_batched": qps_batched, "qps_plain": qps_plain, "speedup": qps_batched / qps_plain,
