@@ -285,14 +285,22 @@ int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream);
  * memory by asynchronous copies while the current tile is probed).  4: as 3,
  * and after the first op each warp compacts its surviving rows so that the
  * remaining ops run one row per lane.  5: as 4 with a 2-stage copy ring (less
- * shared memory, more resident blocks).  Shapes without a specialised pass
- * fall back to the general pass.  Default (and an unset tuning entry): 5. */
+ * shared memory, more resident blocks).  6: as 5, and a warp's surviving rows
+ * that do not fill a last group of 32 are carried (their column values) into
+ * the next tile, so the one-row-per-lane ops run on full warps (chains whose
+ * later ops write no column).  Shapes without a specialised pass fall back to
+ * the general pass.  Default (and an unset tuning entry): 5. */
 int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream);
 /* Tuning table used by sdb_fused_chain: variant for chains with this
  * terminal (sdb_chain_terminal), register count and row count (bucketed by
  * log2).  variant -1 restores the default.  _get returns the variant used. */
 int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant);
 int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows);
+/* The same per kind of the chain's first op (SDB_OP_*, 7 = a chain without
+ * ops), which tells shapes of one terminal apart; first_op -1 in _set_op sets
+ * every kind (what sdb_chain_tune_set does). */
+int sdb_chain_tune_set_op(int terminal, int nregs, int first_op, uint64_t rows, int variant);
+int sdb_chain_tune_get_op(int terminal, int nregs, int first_op, uint64_t rows);
 /* Registers (1..8) a chain needs, or a negative status if it is invalid. */
 int sdb_chain_registers(const sdb_chain_desc *chain);
 

@@ -7,14 +7,16 @@ The fused chain has six kernel variants (``sdb_fused_chain_variant``):
   4      shape-specialised pass, rows compacted per warp after the first op,
          3-stage cp.async copy ring (3 blocks of 256 threads per SM)
   5      as 4 with a 2-stage ring (5 blocks per SM)
+  6      as 5, surviving rows that do not fill a warp carried into the next tile
 
 Block size is 256 threads throughout; the group-by tables are direct-address
 (the reference's HASH is the identity on its range), so there is no load
 factor to pick for the joins, and the shared-memory group table of the
 specialised passes has a fixed 512-slot capacity.  The tuner times every
 variant on the plan shapes of the benchmark at several fact sizes, picks the
-fastest per tuning key -- (terminal, register class, log2 rows bucket), the
-key of ``sdb_chain_tune_set`` -- and writes the table as JSON.  ``load`` puts a
+fastest per tuning key -- (terminal, register class, kind of the chain's
+first op, log2 rows bucket), the key of ``sdb_chain_tune_set_op`` -- and
+writes the table as JSON.  ``load`` puts a
 table into the library; ``Engine`` loads the default table for the device at
 creation.
 
@@ -34,14 +36,16 @@ from . import capi, plans, ssb
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_TABLE = os.path.join(HERE, "tuning", "gb300.json")
-VARIANTS = (0, 1, 2, 3, 4, 5)
+VARIANTS = (0, 1, 2, 3, 4, 5, 6)
 TERMINALS = {"flags": 0, "sum": 1, "groupby": 2}
 
-# benchmark plan shapes: (name, terminal, registers, fact columns, plan builder)
+OP_SEARCH_RANGE, OP_SEMI_PROBE = 1, 3  # SDB_OP_* kinds of a chain's first op
+
+# benchmark plan shapes: (name, terminal, registers, first op, fact columns, plan builder)
 SHAPES = [
-    ("filter_sum", "sum", 1, ssb.QUERY_COLUMNS["q1"], lambda: plans.plan_filter_sum(1994)),
-    ("date_join", "groupby", 2, ssb.QUERY_COLUMNS["q2"], lambda: plans.plan_date_join(1994)),
-    ("star", "groupby", 2, ssb.QUERY_COLUMNS["star"], lambda: plans.plan_star(2, 11)),
+    ("filter_sum", "sum", 1, OP_SEARCH_RANGE, ssb.QUERY_COLUMNS["q1"], lambda: plans.plan_filter_sum(1994)),
+    ("date_join", "groupby", 2, OP_SEARCH_RANGE, ssb.QUERY_COLUMNS["q2"], lambda: plans.plan_date_join(1994)),
+    ("star", "groupby", 2, OP_SEMI_PROBE, ssb.QUERY_COLUMNS["star"], lambda: plans.plan_star(2, 11)),
 ]
 
 
@@ -55,7 +59,8 @@ def load(table: dict) -> int:
     L = capi.lib()
     k = 0
     for e in table.get("entries", []):
-        capi.check(L.sdb_chain_tune_set(TERMINALS[e["terminal"]], e["nregs"], 1 << e["rows_bucket"], e["variant"]))
+        capi.check(L.sdb_chain_tune_set_op(TERMINALS[e["terminal"]], e["nregs"], e.get("first_op", -1),
+                                           1 << e["rows_bucket"], e["variant"]))
         k += 1
     return k
 
@@ -91,7 +96,7 @@ def tune(sizes: Iterable[int] = (1 << 20, 1 << 22, 1 << 24, 1 << 26, 120_000_000
     from .engine import Engine
 
     dims = ssb.gen_dims(sf_dims)
-    cols = sorted({c for s in shapes for c in s[3]})
+    cols = sorted({c for s in shapes for c in s[4]})
     timings: Dict[tuple, Dict[int, float]] = {}
     per_shape = []
     for n in sizes:
@@ -101,10 +106,10 @@ def tune(sizes: Iterable[int] = (1 << 20, 1 << 22, 1 << 24, 1 << 26, 120_000_000
             eng.load_table("lineorder", fact)
             for t in ("supplier", "part", "ddate"):
                 eng.load_table(t, dims[t])
-            for name, term, nregs, _, build in shapes:
+            for name, term, nregs, first_op, _, build in shapes:
                 plan = build()
                 res = {v: _time_variant(eng, plan, v, reps) for v in variants}
-                key = (term, nregs, rows_bucket(int(n)))
+                key = (term, nregs, first_op, rows_bucket(int(n)))
                 acc = timings.setdefault(key, {})
                 for v, t in res.items():
                     acc[v] = acc.get(v, 0.0) + t
@@ -114,9 +119,9 @@ def tune(sizes: Iterable[int] = (1 << 20, 1 << 22, 1 << 24, 1 << 26, 120_000_000
         torch.cuda.empty_cache()
     capi.force_chain_variant(-1)
     entries = []
-    for (term, nregs, b), acc in sorted(timings.items()):
+    for (term, nregs, first_op, b), acc in sorted(timings.items()):
         best = min(acc, key=acc.get)
-        entries.append({"terminal": term, "nregs": nregs, "rows_bucket": b, "variant": best,
+        entries.append({"terminal": term, "nregs": nregs, "first_op": first_op, "rows_bucket": b, "variant": best,
                         "ms_sum": {str(v): t for v, t in acc.items()}})
     return {"device": torch.cuda.get_device_name(), "created": time.strftime("%Y-%m-%d %H:%M:%S"),
             "reps": reps, "sizes": [int(n) for n in sizes], "entries": entries, "measurements": per_shape}

@@ -471,7 +471,8 @@ struct Launch {
     Op ops[kMaxOps];
     Src value;
     uint64_t *sum_out;
-    int32_t n_keys, pad;
+    int32_t n_keys;
+    uint32_t tail_slots;  // slots read after the first op (bit s = slot s): what a carried row keeps
     Src keys[SDB_CHAIN_MAX_KEYS];
     int32_t key_min[SDB_CHAIN_MAX_KEYS];
     uint32_t mults[SDB_CHAIN_MAX_KEYS];
@@ -647,12 +648,37 @@ __device__ __forceinline__ void run_steps(const Launch &L, State<NREGS> &S, std:
 // dense list instead of over mostly-dead 4-row groups.
 template <int NREGS>
 struct Row {
+    static constexpr int kRegs = NREGS;
     int32_t reg[NREGS];
     const int32_t *wstage;  // the warp's 128 staged rows of slot 0 (slot s at + s * 4 * kThreads)
     uint32_t r;             // row within the warp's 128
     uint64_t grow;          // global row
     bool live;
 };
+
+// A row whose slot values sit in registers (rows carried from one tile to the
+// next; the chain writes no column after its first op, so no global row).
+template <int NREGS>
+struct VRow {
+    static constexpr int kRegs = NREGS;
+    static constexpr uint64_t grow = 0;
+    int32_t reg[NREGS];
+    int32_t v0, v1, v2, v3;  // slot values (scalars: selected, never indexed)
+    bool live;
+};
+
+template <int NREGS>
+__device__ __forceinline__ int32_t fetch1(const Src &s, const VRow<NREGS> &R)
+{
+    if (s.src == 0) return s.idx == 0 ? R.v0 : (s.idx == 1 ? R.v1 : (s.idx == 2 ? R.v2 : R.v3));
+    if (s.src == 1) {
+        int32_t v = R.reg[0];
+#pragma unroll
+        for (int i = 1; i < NREGS; i++) v = s.idx == i ? R.reg[i] : v;
+        return v;
+    }
+    return s.lit;
+}
 
 template <int NREGS>
 __device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
@@ -667,9 +693,10 @@ __device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
     return s.lit;
 }
 
-template <int K, int NREGS>
-__device__ __forceinline__ void step1(const Op &op, Row<NREGS> &R, const uint32_t *bits)
+template <int K, class RowT>
+__device__ __forceinline__ void step1(const Op &op, RowT &R, const uint32_t *bits)
 {
+    constexpr int NREGS = RowT::kRegs;
     if (!R.live) return;
     if (K == SDB_OP_SELECT) {
         R.live = sdb::compare(op.cmp, fetch1(op.a, R), fetch1(op.b, R));
@@ -706,12 +733,12 @@ __device__ __forceinline__ void step1(const Op &op, Row<NREGS> &R, const uint32_
     }
 }
 
-template <int NREGS, int BEGIN, int... KS, int... IS>
-__device__ __forceinline__ void run_steps1(const Launch &L, Row<NREGS> &R, const uint32_t *bits,
+template <int NREGS, int BEGIN, int... KS, class RowT, int... IS>
+__device__ __forceinline__ void run_steps1(const Launch &L, RowT &R, const uint32_t *bits,
                                            std::integer_sequence<int, IS...>)
 {
     constexpr int kinds[] = {KS...};
-    (step1<kinds[BEGIN + IS], NREGS>(L.ops[BEGIN + IS], R, bits), ...);
+    (step1<kinds[BEGIN + IS]>(L.ops[BEGIN + IS], R, bits), ...);
 }
 
 // Adds one row to the group-by (block table first, global on overflow) and
@@ -803,10 +830,56 @@ __device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nslot
 // One tile of one chain: the ops before SPLIT on 4-row groups, then (if
 // SPLIT <= N) warp compaction and the remaining ops one row per lane, then
 // the terminal into the block's partials.
+// The ops from SPLIT on and the terminal, for one row held by one lane.
+template <int TERM, int NREGS, int SPLIT, int... KS, class RowT>
+__device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint32_t *s_bits, uint32_t *s_key,
+                                           unsigned long long *s_sum, bool direct, uint64_t &acc)
+{
+    constexpr int N = sizeof...(KS);
+#pragma unroll
+    for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
+    run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
+    if (R.live) {
+        if (TERM == T_SUM) {
+            acc += sdb::widen(fetch1(L.value, R));
+        } else if (TERM == T_GROUP) {
+            uint32_t h = 0;
+#pragma unroll
+            for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+                if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
+            group_row(L, s_key, s_sum, direct, h, fetch1(L.value, R), [&R, &L](int kk) { return fetch1(L.keys[kk], R); });
+        }
+    }
+}
+
+// Carried rows: each warp parks up to 31 surviving rows of a tile (their
+// tail-slot values) in q = s_carry + 32 * warp and runs them together with the
+// next tile's survivors, so the row-per-lane phase runs full warps.  drain
+// runs what is left (at the end of a block's rows of a chain).
 template <int TERM, int NREGS, int SPLIT, int... KS>
+__device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, int4 *s_carry, const uint32_t *s_bits,
+                                            uint32_t *s_key, unsigned long long *s_sum, bool direct, uint64_t &acc)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    if (carry) {
+        const int4 e = s_carry[(threadIdx.x & ~31u) + lane];
+        VRow<NREGS> R;
+        R.v0 = e.x;
+        R.v1 = e.y;
+        R.v2 = e.z;
+        R.v3 = e.w;
+        R.live = lane < carry;
+        sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+    }
+    carry = 0;
+    __syncwarp();
+}
+
+template <int TERM, int NREGS, int SPLIT, bool CARRY, int... KS>
 __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, const int4 *s_buf, int st, uint64_t tile,
                                           uint8_t *s_list, uint32_t *s_key, unsigned long long *s_sum,
-                                          const uint32_t *s_bits, bool direct, uint64_t &acc)
+                                          const uint32_t *s_bits, bool direct, uint64_t &acc, uint32_t &carry,
+                                          int4 *s_carry)
 {
     constexpr int N = sizeof...(KS);
     constexpr bool kCompact = SPLIT <= N;
@@ -844,30 +917,57 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
         for (int k = 0; k < kItems; k++)
             if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
         __syncwarp();
-        Row<NREGS> R;
-        R.wstage = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
-        for (uint32_t b = 0; b < total; b += 32) {
-            const uint32_t idx = b + lane;
-            R.live = idx < total;
-            R.r = R.live ? list[idx] : 0;
-            R.grow = tile + (uint64_t)warp * 32 * kItems + R.r;
-#pragma unroll
-            for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
-            run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
-            if (R.live) {
-                if (TERM == T_SUM) {
-                    acc += sdb::widen(fetch1(L.value, R));
-                } else if (TERM == T_GROUP) {
-                    uint32_t h = 0;
-#pragma unroll
-                    for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-                        if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
-                    group_row(L, s_key, s_sum, direct, h, fetch1(L.value, R),
-                              [R, &L](int kk) { return fetch1(L.keys[kk], R); });
+        const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
+        if constexpr (CARRY) {
+            // entries 0 .. carry-1 are the parked rows, then this tile's survivors
+            int4 *q = s_carry + warp * 32;
+            const uint32_t avail = carry + total;
+            uint32_t b = 0;
+            for (; b + 32 <= avail; b += 32) {
+                const uint32_t idx = b + lane;
+                int4 e;
+                if (idx < carry) {
+                    e = q[idx];
+                } else {
+                    const uint32_t r = list[idx - carry];
+                    e.x = (L.tail_slots & 1u) ? ws[r] : 0;
+                    e.y = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
+                    e.z = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
+                    e.w = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
                 }
+                VRow<NREGS> R;
+                R.v0 = e.x;
+                R.v1 = e.y;
+                R.v2 = e.z;
+                R.v3 = e.w;
+                R.live = true;
+                sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
+            __syncwarp();
+            const uint32_t rem = avail - b;
+            if (lane < rem && b + lane >= carry) {  // park a survivor of this tile
+                const uint32_t r = list[b + lane - carry];
+                int4 e;
+                e.x = (L.tail_slots & 1u) ? ws[r] : 0;
+                e.y = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
+                e.z = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
+                e.w = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
+                q[lane] = e;
+            }
+            carry = rem;
+            __syncwarp();
+        } else {
+            Row<NREGS> R;
+            R.wstage = ws;
+            for (uint32_t b = 0; b < total; b += 32) {
+                const uint32_t idx = b + lane;
+                R.live = idx < total;
+                R.r = R.live ? list[idx] : 0;
+                R.grow = tile + (uint64_t)warp * 32 * kItems + R.r;
+                sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+            }
+            __syncwarp();
         }
-        __syncwarp();
     } else {
         if (TERM == T_FLAGS || L.flags_out) {
 #pragma unroll
@@ -932,7 +1032,7 @@ __device__ __forceinline__ void block_flush(const Launch &L, uint32_t *s_key, un
     }
 }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
 __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(const __grid_constant__ Launch L)
 {
     constexpr int kStages = STAGES;
@@ -942,6 +1042,8 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
     __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
     __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
     __shared__ uint64_t s_part[kThreads / 32];
+    __shared__ int4 s_carry[CARRY ? kThreads : 1];  // per warp: 32 parked rows
+    uint32_t carry = 0;
     const bool direct = L.P <= kDenseCap;
     uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
     group_table_reset<TERM>(s_key, s_sum);
@@ -965,10 +1067,12 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
     for (; tile < L.n; tile += stride) {
         issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, (st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
-        tile_body<TERM, NREGS, SPLIT, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc);
+        tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
+                                                   carry, s_carry);
         st = (st + 1) % kStages;
     }
     cp_async_wait<0>();
+    if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(L, carry, s_carry, s_bits, s_key, s_sum, direct, acc);
     block_flush<TERM>(L, s_key, s_sum, s_part, acc);
 }
 
@@ -986,11 +1090,13 @@ struct Span {
 // new descriptor, resets its group table and re-stages the semi-join bitmap.
 // Within a span the tiles go through the same cp.async ring as the
 // single-chain pass.
-template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
 __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
     k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
             uint32_t *__restrict__ head)
 {
+    __shared__ int4 s_carry[CARRY ? kThreads : 1];
+    uint32_t carry = 0;
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
@@ -1045,19 +1151,21 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
             if (tn < span.t1) issue_tile<kStages>(s_L.slot, s_L.nslot, n, s_buf, (st + kStages - 1) % kStages, (uint64_t)tn * kTile);
             else cp_async_commit();
             cp_async_wait<kStages - 1>();
-            tile_body<TERM, NREGS, SPLIT, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum, s_bits,
-                                                direct, acc);
+            tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum,
+                                                       s_bits, direct, acc, carry, s_carry);
             st = (st + 1) % kStages;
         }
         cp_async_wait<0>();
+        // parked rows belong to this span's chain: run them before the next pull
+        if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(s_L, carry, s_carry, s_bits, s_key, s_sum, direct, acc);
     }
     if (cur != ~0u) block_flush<TERM>(s_L, s_key, s_sum, s_part, acc);
 }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
 int launch_stages(const Launch &L, cudaStream_t s)
 {
-    auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, KS...>;
+    auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
     const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
     static bool attr = false;
@@ -1077,10 +1185,15 @@ int launch_stages(const Launch &L, cudaStream_t s)
     return sdb_check_launch("sdb_fused_chain (dense)");
 }
 
+// Ring stages 3 or 2; rows carried between tiles only with compaction and a
+// 2-stage ring.
 template <int TERM, int NREGS, int SPLIT, int... KS>
-int launch(const Launch &L, int stages, cudaStream_t s)
+int launch(const Launch &L, int stages, bool carry, cudaStream_t s)
 {
-    return stages >= 3 ? launch_stages<TERM, NREGS, 3, SPLIT, KS...>(L, s) : launch_stages<TERM, NREGS, 2, SPLIT, KS...>(L, s);
+    constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    if (stages >= 3) return launch_stages<TERM, NREGS, 3, SPLIT, false, KS...>(L, s);
+    if (kCompact && carry) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact, KS...>(L, s);
+    return launch_stages<TERM, NREGS, 2, SPLIT, false, KS...>(L, s);
 }
 
 // Converts a checked chain into a dense launch.  Returns false when the chain
@@ -1148,11 +1261,15 @@ bool convert(const ChainLaunch &C, int nregs, Launch &D)
     D.P = c.P;
     D.out_sum = c.out_sum;
     D.occ = c.occ;
+    // slots a row still needs after the first op
+    auto slot_bit = [](const Src &x) { return x.src == 0 ? (1u << x.idx) : 0u; };
+    D.tail_slots = 0;
+    for (int k = 1; k < c.n_ops; k++) D.tail_slots |= slot_bit(D.ops[k].a) | slot_bit(D.ops[k].b);
+    if (c.terminal != SDB_TERM_FLAGS) D.tail_slots |= slot_bit(D.value);
+    for (int j = 0; j < D.n_keys; j++) D.tail_slots |= slot_bit(D.keys[j]);
     return true;
 }
 
-// Instantiated shapes.  Returns SDB_ERR_UNSUPPORTED (without launching) for
-// any other chain.
 // Whether the ops from index `split` on can run on compacted rows: no flags
 // output, and every later op only keeps or clears a row's flag (no NONE/OR
 // selection, no literal fill); ops before the split produce no register.
@@ -1170,6 +1287,17 @@ bool can_compact(const Launch &D, int term, int split)
                 return false;
         }
     }
+    return true;
+}
+
+// Whether compacted rows can be carried from one tile to the next: besides
+// compaction after the first op, no op after it writes a column (a carried
+// row keeps its slot values, not its row number).
+bool can_carry(const Launch &D, int term)
+{
+    if (!can_compact(D, term, 1)) return false;
+    for (int i = 1; i < D.n_ops; i++)
+        if (D.ops[i].out_col) return false;
     return true;
 }
 
@@ -1226,28 +1354,29 @@ struct ShapeProbe {
 struct SingleLauncher {
     const Launch &D;
     int stages;
+    bool carry;
     cudaStream_t s;
     template <int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
-        return launch<TERM, NREGS, SPLIT, KS...>(D, stages, s);
+        return launch<TERM, NREGS, SPLIT, KS...>(D, stages, carry, s);
     }
 };
 
-int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, cudaStream_t s)
+int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, bool carry, cudaStream_t s)
 {
     Launch D;
     if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
-    SingleLauncher f{D, stages, s};
+    SingleLauncher f{D, stages, carry && can_carry(D, term), s};
     return with_shape(D, term, compact, f);
 }
 
 // One launch of k_batch over the chains of one shape group.
-template <int TERM, int NREGS, int STAGES, int SPLIT, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
 int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, uint32_t *head, uint32_t bitmap_words,
                  cudaStream_t s)
 {
-    auto kern = k_batch<TERM, NREGS, STAGES, SPLIT, KS...>;
+    auto kern = k_batch<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
     const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
     const int smem = ring + (int)(bitmap_words * 4);
     static int attr_set = 0;
@@ -1272,22 +1401,34 @@ struct BatchLauncher {
     uint32_t *head;
     uint32_t bitmap_words;
     int stages;
+    bool carry;
     cudaStream_t s;
     template <int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
-        return stages >= 3 ? batch_stages<TERM, NREGS, 3, SPLIT, KS...>(launches, spans, n_spans, head, bitmap_words, s)
-                           : batch_stages<TERM, NREGS, 2, SPLIT, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+        constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+        if (stages >= 3)
+            return batch_stages<TERM, NREGS, 3, SPLIT, false, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+        if (kCompact && carry)
+            return batch_stages<TERM, NREGS, 2, SPLIT, kCompact, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+        return batch_stages<TERM, NREGS, 2, SPLIT, false, KS...>(launches, spans, n_spans, head, bitmap_words, s);
     }
 };
 
 }  // namespace dense
 
-// Tuning table: variant per (terminal, register class, log2 rows bucket);
-// -1 = default.  Set by sdb_chain_tune_set (the autotuner persists its
-// choices and loads them at start-up).
-int g_tune[3][3][40];
+// Tuning table: variant per (terminal, register class, kind of the first op,
+// log2 rows bucket); -1 = default.  Set by sdb_chain_tune_set(_op) (the
+// autotuner persists its choices and loads them at start-up).  The first op
+// tells the shapes of one terminal apart (a star join starts with a semi
+// join, a date join with a range filter).
+constexpr int kOpClasses = 8;  // SDB_OP_* kinds 0..6, 7 = no op
+int g_tune[3][3][kOpClasses][40];
 bool g_tune_init = false;
+
+int op_class(const sdb_chain_desc &d) { return d.n_ops > 0 && d.ops[0].kind >= 0 && d.ops[0].kind < 7 ? d.ops[0].kind : 7; }
+
+int &tune_entry(int term, int nregs, int opc, uint64_t rows);
 
 int reg_class(int nregs) { return nregs <= 2 ? 0 : (nregs <= 4 ? 1 : 2); }
 int rows_bucket(uint64_t n)
@@ -1297,11 +1438,24 @@ int rows_bucket(uint64_t n)
     return b;
 }
 
+int &tune_entry(int term, int nregs, int opc, uint64_t rows)
+{
+    if (!g_tune_init) {
+        memset(g_tune, 0xff, sizeof g_tune);
+        g_tune_init = true;
+    }
+    return g_tune[term][reg_class(nregs)][opc][rows_bucket(rows)];
+}
+
 int default_variant(int nregs) { return nregs <= 4 ? 1 : 0; }
 
 constexpr int kDenseVariant = 3;
 constexpr int kCompactVariant = 4;
 constexpr int kCompact2Variant = 5;  // as 4 with a 2-stage copy ring
+constexpr int kCarryVariant = 6;     // as 5, compacted rows carried across tiles
+constexpr int kMaxVariant = 6;
+
+int variant_stages(int v) { return (v == kCompact2Variant || v == kCarryVariant) ? 2 : 3; }
 
 bool operand_ok(const sdb_operand &o, int &nregs, bool &vec, const char **why)
 {
@@ -1430,15 +1584,12 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
     if (L.d.n == 0) return SDB_OK;
     cudaStream_t s = (cudaStream_t)stream;
     if (variant < 0) {
-        if (!g_tune_init) {
-            memset(g_tune, 0xff, sizeof g_tune);
-            g_tune_init = true;
-        }
-        variant = g_tune[term][reg_class(nregs)][rows_bucket(L.d.n)];
+        variant = tune_entry(term, nregs, op_class(L.d), L.d.n);
         if (variant < 0) variant = kCompact2Variant;  // shape-specialised pass when one exists
     }
     if (variant >= kDenseVariant) {
-        const int st2 = dense::dispatch(L, nregs, term, variant != kDenseVariant, variant == kCompact2Variant ? 2 : 3, s);
+        const int st2 = dense::dispatch(L, nregs, term, variant != kDenseVariant, variant_stages(variant),
+                                        variant == kCarryVariant, s);
         if (st2 != SDB_ERR_UNSUPPORTED) return st2;
         variant = default_variant(nregs);
     }
@@ -1454,6 +1605,7 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
 struct sdb_chain_batch {
     struct Group {
         int term, compact, stages;
+        bool carry;
         dense::Launch first;             // host copy, picks the instantiation
         const dense::Launch *launches;   // device
         const dense::Span *spans;        // device
@@ -1474,6 +1626,7 @@ namespace {
 struct BatchPlan {
     struct G {
         int term, compact, stages, shape;
+        bool carry = false;
         std::vector<dense::Launch> launches;
         std::vector<dense::Span> spans;
         uint32_t bitmap_words = 0;
@@ -1496,7 +1649,7 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         uint64_t tiles;
     };
     struct Family {
-        int shape, term, nregs;
+        int shape, term, nregs, opc;
         uint64_t rows = 0;
         std::vector<Item> items;
     };
@@ -1518,7 +1671,7 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         it.tiles = (L.d.n + kTile - 1) / kTile;
         size_t f = 0;
         while (f < fams.size() && !(fams[f].shape == probe.id && fams[f].term == term)) f++;
-        if (f == fams.size()) fams.push_back(Family{probe.id, term, nregs});
+        if (f == fams.size()) fams.push_back(Family{probe.id, term, nregs, op_class(L.d)});
         fams[f].nregs = std::max(fams[f].nregs, nregs);
         fams[f].rows += L.d.n;
         fams[f].items.push_back(it);
@@ -1528,7 +1681,7 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
     std::vector<BatchPlan::G> groups;
     std::vector<const Family *> of;
     for (const Family &F : fams) {
-        int variant = g_tune_init ? g_tune[F.term][reg_class(F.nregs)][rows_bucket(F.rows)] : -1;
+        int variant = g_tune_init ? tune_entry(F.term, F.nregs, F.opc, F.rows) : -1;
         if (variant < 0) variant = kCompact2Variant;
         if (variant < kDenseVariant) {  // the general pass: chain by chain
             for (const Item &it : F.items) bp.singles.push_back(chains[it.index]);
@@ -1537,7 +1690,8 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         BatchPlan::G g;
         g.term = F.term;
         g.compact = variant != kDenseVariant;
-        g.stages = variant == kCompact2Variant ? 2 : 3;
+        g.stages = variant_stages(variant);
+        g.carry = variant == kCarryVariant;
         g.shape = F.shape;
         groups.push_back(g);
         of.push_back(&F);
@@ -1550,6 +1704,7 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
     for (size_t g = 0; g < groups.size(); g++) {
         BatchPlan::G &G = groups[g];
         for (const Item &it : of[g]->items) {
+            if (G.carry && !dense::can_carry(it.D, G.term)) G.carry = false;  // every chain of the launch must allow it
             const uint32_t c = (uint32_t)G.launches.size();
             G.launches.push_back(it.D);
             if (it.D.bitmap_ht) G.bitmap_words = std::max<uint32_t>(G.bitmap_words, (it.D.bitmap_len + 31) / 32);
@@ -1609,6 +1764,7 @@ static int chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *
         o.term = G.term;
         o.compact = G.compact;
         o.stages = G.stages;
+        o.carry = G.carry;
         o.first = G.launches[0];
         o.head = b->heads + g;
         o.bitmap_words = G.bitmap_words;
@@ -1657,7 +1813,7 @@ int sdb_chain_batch_launch(const sdb_chain_batch *b, sdb_stream_t stream)
         if (e != cudaSuccess) return sdb_set_error(SDB_ERR_CUDA, "sdb_chain_batch_launch: %s", cudaGetErrorString(e));
     }
     for (const auto &G : b->groups) {
-        dense::BatchLauncher f{G.launches, G.spans, G.n_spans, G.head, G.bitmap_words, G.stages, s};
+        dense::BatchLauncher f{G.launches, G.spans, G.n_spans, G.head, G.bitmap_words, G.stages, G.carry, s};
         int st = dense::with_shape(G.first, G.term, G.compact, f);
         if (st != SDB_OK) return st;
     }
@@ -1684,28 +1840,39 @@ int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream) { return f
 
 int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream)
 {
-    if (variant < 0 || variant > 5) return sdb_set_error(SDB_ERR_INVALID, "sdb_fused_chain_variant: variant %d", variant);
+    if (variant < 0 || variant > kMaxVariant)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_fused_chain_variant: variant %d", variant);
     return fused_chain_impl(chain, variant, stream);
+}
+
+int sdb_chain_tune_set_op(int terminal, int nregs, int first_op, uint64_t rows, int variant)
+{
+    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS || variant < -1 ||
+        variant > kMaxVariant || first_op < -1 || first_op >= kOpClasses)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_tune_set: bad argument");
+    for (int c = 0; c < kOpClasses; c++)
+        if (first_op < 0 || c == first_op) tune_entry(terminal, nregs, c, rows) = variant;
+    return SDB_OK;
 }
 
 int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant)
 {
-    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS || variant < -1 || variant > 5)
-        return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_tune_set: bad argument");
-    if (!g_tune_init) {
-        memset(g_tune, 0xff, sizeof g_tune);
-        g_tune_init = true;
-    }
-    g_tune[terminal][reg_class(nregs)][rows_bucket(rows)] = variant;
-    return SDB_OK;
+    return sdb_chain_tune_set_op(terminal, nregs, -1, rows, variant);
+}
+
+int sdb_chain_tune_get_op(int terminal, int nregs, int first_op, uint64_t rows)
+{
+    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS || first_op < 0 ||
+        first_op >= kOpClasses)
+        return -1;
+    if (!g_tune_init) return kCompact2Variant;
+    int v = tune_entry(terminal, nregs, first_op, rows);
+    return v < 0 ? kCompact2Variant : v;
 }
 
 int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows)
 {
-    if (terminal < 0 || terminal > 2 || nregs < 1 || nregs > SDB_CHAIN_MAX_REGS) return -1;
-    if (!g_tune_init) return kCompact2Variant;
-    int v = g_tune[terminal][reg_class(nregs)][rows_bucket(rows)];
-    return v < 0 ? kCompact2Variant : v;
+    return sdb_chain_tune_get_op(terminal, nregs, 7, rows);
 }
 
 int sdb_chain_registers(const sdb_chain_desc *chain)

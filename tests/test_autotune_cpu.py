@@ -28,3 +28,20 @@ def test_load_sets_the_tuning_table(tmp_path):
 
 def test_missing_table_is_not_an_error(tmp_path):
     assert autotune.load_default(str(tmp_path / "absent.json")) is None
+
+
+def test_first_op_keys_are_separate():
+    L = capi.lib()
+    table = {"entries": [{"terminal": "groupby", "nregs": 2, "first_op": 3, "rows_bucket": 26, "variant": 5},
+                         {"terminal": "groupby", "nregs": 2, "first_op": 1, "rows_bucket": 26, "variant": 6}]}
+    try:
+        capi.force_chain_variant(-1)
+        autotune.load(table)
+        assert L.sdb_chain_tune_get_op(2, 2, 3, 1 << 26) == 5
+        assert L.sdb_chain_tune_get_op(2, 2, 1, 1 << 26) == 6
+        assert L.sdb_chain_tune_get_op(2, 2, 0, 1 << 26) == 5  # unset entries use the default
+        assert L.sdb_chain_tune_set_op(2, 2, 9, 1, 5) == capi.SDB_ERR_INVALID
+        assert L.sdb_chain_tune_set_op(2, 2, 1, 1, 7) == capi.SDB_ERR_INVALID
+    finally:
+        capi.force_chain_variant(-1)
+        autotune.load_default()

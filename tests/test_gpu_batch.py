@@ -144,3 +144,21 @@ def test_batched_form_full_size_equals_plain():
     assert st["batched_chains"] == 64 and st["chain_launches"] == 1
     groups = [len(r) for r in alone]
     assert max(groups) <= 280 and all(g <= p.max_groups for g, p in zip(groups, wl.params))
+
+
+@pytest.mark.parametrize("variant", [3, 4, 5, 6])
+def test_batch_under_each_specialised_variant(tables, oracle_rows, variant):
+    """The chain batch with every shape-specialised variant (dense, compacted
+    with a 3- or 2-stage ring, rows carried across tiles)."""
+    pls = small_plans()
+    try:
+        capi.force_chain_variant(variant)
+        with make_engine(tables) as eng:
+            with eng.batch(pls) as b:
+                got = [r.canonical() for r in b.run()]
+                assert b.stats()["chain_launches"] == 3
+            alone = [eng.execute(pl).canonical() for pl in pls]
+    finally:
+        capi.force_chain_variant(-1)
+    assert got == oracle_rows
+    assert alone == oracle_rows

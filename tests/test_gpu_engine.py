@@ -132,7 +132,7 @@ def test_star_sf20_full_size():
     torch.cuda.empty_cache()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
 def test_every_kernel_variant_matches_golden(variant):
     """The general pass at 4/8/16 rows per thread and the shape-specialised
     pass give the same rows."""
