@@ -852,17 +852,18 @@ __device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint3
     }
 }
 
-// Carried rows: each warp parks up to 31 surviving rows of a tile (their
-// tail-slot values) in q = s_carry + 32 * warp and runs them together with the
-// next tile's survivors, so the row-per-lane phase runs full warps.  drain
-// runs what is left (at the end of a block's rows of a chain).
+// Carried rows: a warp keeps the up to 31 surviving rows of a tile that do
+// not fill a last group of 32 -- row j's tail-slot values in lane j's
+// registers (`ce`) -- and runs them with the next tile's survivors, so the
+// row-per-lane phase runs full warps.  drain runs what is left (at the end of
+// a block's rows of a chain).
 template <int TERM, int NREGS, int SPLIT, int... KS>
-__device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, int4 *s_carry, const uint32_t *s_bits,
+__device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, const int4 &ce, const uint32_t *s_bits,
                                             uint32_t *s_key, unsigned long long *s_sum, bool direct, uint64_t &acc)
 {
     const uint32_t lane = threadIdx.x & 31u;
     if (carry) {
-        const int4 e = s_carry[(threadIdx.x & ~31u) + lane];
+        const int4 e = ce;
         VRow<NREGS> R;
         R.v0 = e.x;
         R.v1 = e.y;
@@ -879,7 +880,7 @@ template <int TERM, int NREGS, int SPLIT, bool CARRY, int... KS>
 __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, const int4 *s_buf, int st, uint64_t tile,
                                           uint8_t *s_list, uint32_t *s_key, unsigned long long *s_sum,
                                           const uint32_t *s_bits, bool direct, uint64_t &acc, uint32_t &carry,
-                                          int4 *s_carry)
+                                          int4 &ce)
 {
     constexpr int N = sizeof...(KS);
     constexpr bool kCompact = SPLIT <= N;
@@ -919,15 +920,15 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
         __syncwarp();
         const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
         if constexpr (CARRY) {
-            // entries 0 .. carry-1 are the parked rows, then this tile's survivors
-            int4 *q = s_carry + warp * 32;
+            // entries 0 .. carry-1 are the carried rows (entry j in lane j),
+            // then this tile's survivors
             const uint32_t avail = carry + total;
             uint32_t b = 0;
             for (; b + 32 <= avail; b += 32) {
                 const uint32_t idx = b + lane;
                 int4 e;
                 if (idx < carry) {
-                    e = q[idx];
+                    e = ce;  // only in the first group: idx == lane
                 } else {
                     const uint32_t r = list[idx - carry];
                     e.x = (L.tail_slots & 1u) ? ws[r] : 0;
@@ -943,16 +944,13 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
                 R.live = true;
                 sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
-            __syncwarp();
             const uint32_t rem = avail - b;
-            if (lane < rem && b + lane >= carry) {  // park a survivor of this tile
+            if (lane < rem && b + lane >= carry) {  // carry a survivor of this tile
                 const uint32_t r = list[b + lane - carry];
-                int4 e;
-                e.x = (L.tail_slots & 1u) ? ws[r] : 0;
-                e.y = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
-                e.z = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
-                e.w = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
-                q[lane] = e;
+                ce.x = (L.tail_slots & 1u) ? ws[r] : 0;
+                ce.y = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
+                ce.z = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
+                ce.w = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
             }
             carry = rem;
             __syncwarp();
@@ -1042,8 +1040,8 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
     __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
     __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
     __shared__ uint64_t s_part[kThreads / 32];
-    __shared__ int4 s_carry[CARRY ? kThreads : 1];  // per warp: 32 parked rows
-    uint32_t carry = 0;
+    uint32_t carry = 0;  // rows the warp carries (warp-uniform)
+    int4 ce = make_int4(0, 0, 0, 0);
     const bool direct = L.P <= kDenseCap;
     uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
     group_table_reset<TERM>(s_key, s_sum);
@@ -1068,11 +1066,11 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
         issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, (st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
         tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
-                                                   carry, s_carry);
+                                                   carry, ce);
         st = (st + 1) % kStages;
     }
     cp_async_wait<0>();
-    if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(L, carry, s_carry, s_bits, s_key, s_sum, direct, acc);
+    if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(L, carry, ce, s_bits, s_key, s_sum, direct, acc);
     block_flush<TERM>(L, s_key, s_sum, s_part, acc);
 }
 
@@ -1095,8 +1093,8 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
     k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
             uint32_t *__restrict__ head)
 {
-    __shared__ int4 s_carry[CARRY ? kThreads : 1];
     uint32_t carry = 0;
+    int4 ce = make_int4(0, 0, 0, 0);
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
@@ -1152,12 +1150,12 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
             else cp_async_commit();
             cp_async_wait<kStages - 1>();
             tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum,
-                                                       s_bits, direct, acc, carry, s_carry);
+                                                       s_bits, direct, acc, carry, ce);
             st = (st + 1) % kStages;
         }
         cp_async_wait<0>();
         // parked rows belong to this span's chain: run them before the next pull
-        if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(s_L, carry, s_carry, s_bits, s_key, s_sum, direct, acc);
+        if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(s_L, carry, ce, s_bits, s_key, s_sum, direct, acc);
     }
     if (cur != ~0u) block_flush<TERM>(s_L, s_key, s_sum, s_part, acc);
 }
