@@ -436,11 +436,8 @@ int launch_regs(const ChainLaunch &L, int nregs, int variant, cudaStream_t s)
 // bandwidth at 4 B per column per row.
 namespace dense {
 
-// lo <= a <= hi as one unsigned compare (lo <= hi).
-__device__ __forceinline__ bool in_range(int32_t a, int32_t lo, int32_t hi)
-{
-    return (uint32_t)a - (uint32_t)lo <= (uint32_t)hi - (uint32_t)lo;
-}
+// lo <= a <= hi (empty when lo > hi).
+__device__ __forceinline__ bool in_range(int32_t a, int32_t lo, int32_t hi) { return a >= lo && a <= hi; }
 
 constexpr int kItems = 4;
 constexpr int kSlots = 4;
@@ -580,12 +577,13 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         const uint8_t *ht = static_cast<const uint8_t *>(op.ht);
         uint32_t m = 0;
         if (op.smem_bits) {
+            // branch-free: out-of-range keys read word 0 and are masked off
 #pragma unroll
-            for (int k = 0; k < kItems; k++)
-                if (((S.live >> k) & 1u) && in_range(a[k], op.lo, op.hi)) {
-                    const uint32_t h = (uint32_t)a[k] - (uint32_t)op.lo;
-                    m |= ((S.bits[h >> 5] >> (h & 31u)) & 1u) << k;
-                }
+            for (int k = 0; k < kItems; k++) {
+                const uint32_t ok = in_range(a[k], op.lo, op.hi);
+                const uint32_t h = ok ? (uint32_t)a[k] - (uint32_t)op.lo : 0u;
+                m |= ((S.bits[h >> 5] >> (h & 31u)) & ok) << k;
+            }
         } else {
             uint8_t h[kItems];
 #pragma unroll
@@ -693,6 +691,7 @@ __device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
     return s.lit;
 }
 
+// One op on one row per lane.
 template <int K, class RowT>
 __device__ __forceinline__ void step1(const Op &op, RowT &R, const uint32_t *bits)
 {
@@ -707,24 +706,19 @@ __device__ __forceinline__ void step1(const Op &op, RowT &R, const uint32_t *bit
         R.live = a == op.lo || a == op.hi;
     } else if (K == SDB_OP_SEMI_PROBE) {
         const int32_t a = fetch1(op.a, R);
-        if (!in_range(a, op.lo, op.hi)) {
-            R.live = false;
-        } else {
-            const uint32_t h = (uint32_t)a - (uint32_t)op.lo;
-            R.live = op.smem_bits ? ((bits[h >> 5] >> (h & 31u)) & 1u) != 0
-                                  : __ldg(static_cast<const uint8_t *>(op.ht) + h) != 0;
-        }
+        const bool ok = in_range(a, op.lo, op.hi);
+        const uint32_t i = ok ? (uint32_t)a - (uint32_t)op.lo : 0u;
+        const bool hit = op.smem_bits ? ((bits[i >> 5] >> (i & 31u)) & 1u) != 0
+                                      : __ldg(static_cast<const uint8_t *>(op.ht) + i) != 0;
+        R.live = ok && hit;
     } else if (K == SDB_OP_FULL_PROBE) {
         const int32_t a = fetch1(op.a, R);
-        if (!in_range(a, op.lo, op.hi)) {
-            R.live = false;
-        } else {
-            const int2 e = __ldg(static_cast<const int2 *>(op.ht) + ((uint32_t)a - (uint32_t)op.lo));
-            R.live = e.x == 1;
+        const bool ok = in_range(a, op.lo, op.hi);
+        const int2 e = __ldg(static_cast<const int2 *>(op.ht) + (ok ? (uint32_t)a - (uint32_t)op.lo : 0u));
+        R.live = ok && e.x == 1;
 #pragma unroll
-            for (int i = 0; i < NREGS; i++) R.reg[i] = (R.live && op.out_reg == i) ? e.y : R.reg[i];
-            if (R.live && op.out_col) op.out_col[R.grow] = e.y;
-        }
+        for (int i = 0; i < NREGS; i++) R.reg[i] = (R.live && op.out_reg == i) ? e.y : R.reg[i];
+        if (R.live && op.out_col) op.out_col[R.grow] = e.y;
     } else if (K == SDB_OP_BINOP) {
         const int32_t v = sdb::binop(fetch1(op.a, R), fetch1(op.b, R), op.bin);
 #pragma unroll
@@ -888,9 +882,13 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     S.stage = &s_buf[st * kSlots * kThreads + threadIdx.x];
     S.base = tile + (uint64_t)kItems * threadIdx.x;
-    S.valid = 0;
+    if (S.base + kItems <= L.n) {
+        S.valid = (1u << kItems) - 1u;
+    } else {
+        S.valid = 0;
 #pragma unroll
-    for (int k = 0; k < kItems; k++) S.valid |= (uint32_t)(S.base + k < L.n) << k;
+        for (int k = 0; k < kItems; k++) S.valid |= (uint32_t)(S.base + k < L.n) << k;
+    }
     if (L.flags_in && S.valid) {
         uint32_t m = 0;
 #pragma unroll

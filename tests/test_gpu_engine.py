@@ -146,3 +146,34 @@ def test_every_kernel_variant_matches_golden(variant):
             assert [list(r) for r in got] == case["rows"], (variant, case["name"])
     finally:
         capi.force_chain_variant(-1)
+
+
+@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6])
+def test_reversed_search_range_is_empty(variant):
+    """A SEARCH range whose low bound is above its high bound selects no row
+    (the reference's `c >= lo` then `c <= hi`), in every fused variant."""
+    ds = datasets.dataset(0.01)
+    P = plans
+    b = P.PlanBuilder()
+    b.scan("lineorder")
+    b.filter(P.AND(P.search(5, 19941231, 19940101), P.search(11, 1, 3), P.expr("<", P.col(8), P.lit(25))))
+    b.project([P.expr("*", P.col(9), P.col(11))])
+    b.aggregate([], 0)
+    rev = b.plan()
+    b = P.PlanBuilder()
+    f = b.scan("lineorder")
+    f = b.filter(P.search(11, 6, 4))
+    d = b.scan("ddate")
+    d = b.filter(P.search(4, 1993, 1994))
+    b.join(f, d, 5, 17)
+    b.project([P.col(17 + 4), P.expr("*", P.col(9), P.col(11))])
+    b.aggregate([0], 1)
+    rev_join = b.plan()
+    try:
+        capi.force_chain_variant(variant)
+        with Engine(arena_bytes=1 << 30, fuse=True) as eng:
+            load(eng, ds)
+            for plan in (rev, rev_join):
+                assert eng.execute(plan).canonical() == datasets.oracle_run(ds, plan), json.dumps(plan)
+    finally:
+        capi.force_chain_variant(-1)
