@@ -746,7 +746,17 @@ __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsi
         atomicAdd(&g_errors, 1ull);
         return;
     }
-    const unsigned long long val = (unsigned long long)sdb::widen(value);
+    unsigned long long val = (unsigned long long)sdb::widen(value);
+    // warp aggregation: lanes here with the same slot sum their values (exactly:
+    // 16-bit halves reduced in 32 bits, then recombined in 64) and only the
+    // lowest of them updates the table
+    const unsigned peers = __match_any_sync(__activemask(), (unsigned)sl);
+    if (__popc(peers) > 1) {
+        const uint32_t lo = __reduce_add_sync(peers, (uint32_t)value & 0xffffu);
+        const int32_t hi = (int32_t)__reduce_add_sync(peers, (uint32_t)(value >> 16));
+        if ((threadIdx.x & 31u) != (unsigned)(__ffs(peers) - 1)) return;
+        val = (unsigned long long)((int64_t)hi * 65536 + (int64_t)lo);
+    }
     bool first = false;
     if (smem_group_add<kDenseCap>(s_key, s_sum, (uint32_t)sl, val, direct, first)) {
         if (first) first = atomicExch(&L.occ[sl], 1u) == 0u;
@@ -824,15 +834,11 @@ __device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nslot
 // One tile of one chain: the ops before SPLIT on 4-row groups, then (if
 // SPLIT <= N) warp compaction and the remaining ops one row per lane, then
 // the terminal into the block's partials.
-// The ops from SPLIT on and the terminal, for one row held by one lane.
-template <int TERM, int NREGS, int SPLIT, int... KS, class RowT>
-__device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint32_t *s_bits, uint32_t *s_key,
-                                           unsigned long long *s_sum, bool direct, uint64_t &acc)
+// The terminal for one row held by one lane.
+template <int TERM, class RowT>
+__device__ __forceinline__ void finish_row(const Launch &L, RowT &R, uint32_t *s_key, unsigned long long *s_sum,
+                                           bool direct, uint64_t &acc)
 {
-    constexpr int N = sizeof...(KS);
-#pragma unroll
-    for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
-    run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
     if (R.live) {
         if (TERM == T_SUM) {
             acc += sdb::widen(fetch1(L.value, R));
@@ -845,6 +851,19 @@ __device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint3
         }
     }
 }
+
+// The ops from SPLIT on and the terminal, for one row held by one lane.
+template <int TERM, int NREGS, int SPLIT, int... KS, class RowT>
+__device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint32_t *s_bits, uint32_t *s_key,
+                                           unsigned long long *s_sum, bool direct, uint64_t &acc)
+{
+    constexpr int N = sizeof...(KS);
+#pragma unroll
+    for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
+    run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
+    finish_row<TERM>(L, R, s_key, s_sum, direct, acc);
+}
+
 
 // Carried rows: a warp keeps the up to 31 surviving rows of a tile that do
 // not fill a last group of 32 -- row j's tail-slot values in lane j's
@@ -921,25 +940,26 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             // entries 0 .. carry-1 are the carried rows (entry j in lane j),
             // then this tile's survivors
             const uint32_t avail = carry + total;
-            uint32_t b = 0;
-            for (; b + 32 <= avail; b += 32) {
-                const uint32_t idx = b + lane;
-                int4 e;
-                if (idx < carry) {
-                    e = ce;  // only in the first group: idx == lane
+            auto entry = [&](uint32_t idx) {
+                VRow<NREGS> R;
+                if (idx < carry) {  // only in the first group: idx == lane
+                    R.v0 = ce.x;
+                    R.v1 = ce.y;
+                    R.v2 = ce.z;
+                    R.v3 = ce.w;
                 } else {
                     const uint32_t r = list[idx - carry];
-                    e.x = (L.tail_slots & 1u) ? ws[r] : 0;
-                    e.y = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
-                    e.z = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
-                    e.w = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
+                    R.v0 = (L.tail_slots & 1u) ? ws[r] : 0;
+                    R.v1 = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
+                    R.v2 = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
+                    R.v3 = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
                 }
-                VRow<NREGS> R;
-                R.v0 = e.x;
-                R.v1 = e.y;
-                R.v2 = e.z;
-                R.v3 = e.w;
                 R.live = true;
+                return R;
+            };
+            uint32_t b = 0;
+            for (; b + 32 <= avail; b += 32) {
+                VRow<NREGS> R = entry(b + lane);
                 sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
             const uint32_t rem = avail - b;
