@@ -371,6 +371,8 @@ typedef struct sdb_engine_config {
     int32_t fuse;               /* 1: run fusable kernel runs as one sdb_fused_chain pass */
     int32_t profile;            /* 1: time every launch with CUDA events */
     sdb_stream_t stream;        /* NULL: the engine creates its own stream */
+    int32_t plan_cache;         /* > 0: prepared plans kept (see sdb_engine_execute); 0: none */
+    int32_t pad;
 } sdb_engine_config;
 
 /* Parses a plan and derives its execution order and group-by columns
@@ -390,7 +392,13 @@ int sdb_engine_destroy(sdb_engine *eng);
 int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const int32_t *const *cols,
                           uint64_t nrows, int on_device);
 
-/* Execute one plan; on success *out holds the result rows (host memory). */
+/* Execute one plan; on success *out holds the result rows (host memory).
+ * With plan_cache > 0 (and profile = 0) the second execution of the same plan
+ * text prepares it as a one-plan batch (sdb_engine_batch_prepare: recorded
+ * once against an arena of its own, captured as a CUDA graph); later
+ * executions replay the graph -- the same kernels on the same tables, without
+ * the host work of planning.  Up to plan_cache plans stay prepared (least
+ * recently used dropped); sdb_engine_load_table drops them all. */
 int sdb_engine_execute(sdb_engine *eng, const char *plan_json, sdb_result **out);
 
 /* Result: flagged rows of the final table in row order, non-null columns in

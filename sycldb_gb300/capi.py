@@ -57,7 +57,7 @@ class ChainDesc(ctypes.Structure):
 
 class EngineConfig(ctypes.Structure):
     _fields_ = [("arena_bytes", c_uint64), ("segment_rows", c_uint64), ("fuse", c_int32), ("profile", c_int32),
-                ("stream", c_void_p)]
+                ("stream", c_void_p), ("plan_cache", c_int32), ("pad", c_int32)]
 
 
 class BatchStats(ctypes.Structure):

@@ -1452,6 +1452,14 @@ struct sdb_result {
 
 struct sdb_engine {
     sdb::Engine E;
+    // Prepared plans (sdb_engine_config.plan_cache): plan text -> times seen,
+    // last use, and the one-plan batch replayed for it once prepared.
+    struct Cached {
+        uint64_t uses = 0, last = 0;
+        sdb_batch *batch = nullptr;
+    };
+    std::map<std::string, Cached> cache;
+    uint64_t tick = 0;
 };
 
 // A prepared batch: every plan's device work recorded once against the
@@ -1982,6 +1990,57 @@ void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
     for (size_t p = 0; p < B.pend.size(); p++) out[p] = unpack_result(B, p);
 }
 
+// Drops every prepared plan (their batches read the loaded tables).
+void plan_cache_clear(sdb_engine &eng)
+{
+    for (auto &c : eng.cache)
+        if (c.second.batch) delete c.second.batch;
+    eng.cache.clear();
+}
+
+// sdb_engine_execute with the plan cache: the second execution of a plan text
+// prepares it as a one-plan batch (recorded once against its own arena,
+// captured as a CUDA graph, fused chains launched on their own); from then on
+// an execution is one graph launch and the unpacking of its result.  The
+// device work is the plain path's, kernel for kernel.
+std::unique_ptr<sdb_result> execute_cached(sdb_engine &eng, const std::string &text)
+{
+    Engine &E = eng.E;
+    const uint64_t now = ++eng.tick;
+    auto it = eng.cache.find(text);
+    if (it == eng.cache.end()) {
+        if (eng.cache.size() >= 4096) {  // forget plans seen once
+            for (auto c = eng.cache.begin(); c != eng.cache.end();)
+                c = c->second.batch ? std::next(c) : eng.cache.erase(c);
+        }
+        it = eng.cache.emplace(text, sdb_engine::Cached{}).first;
+    }
+    sdb_engine::Cached &c = it->second;
+    c.last = now;
+    if (!c.batch && ++c.uses < 2) return execute_plan(E, text);
+    if (!c.batch) {
+        size_t prepared = 0;
+        for (auto &o : eng.cache) prepared += o.second.batch != nullptr;
+        while (prepared >= (size_t)E.cfg.plan_cache) {  // least recently used goes
+            auto lru = eng.cache.end();
+            for (auto o = eng.cache.begin(); o != eng.cache.end(); ++o)
+                if (o->second.batch && (lru == eng.cache.end() || o->second.last < lru->second.last)) lru = o;
+            delete lru->second.batch;
+            lru->second.batch = nullptr;
+            prepared--;
+        }
+        auto B = std::make_unique<sdb_batch>();
+        B->eng = &eng;
+        B->flags = SDB_BATCH_NO_CHAIN_BATCH;
+        batch_prepare(E, *B, {text});
+        c.batch = B.release();
+    }
+    sdb_result *r = nullptr;
+    batch_run(E, *c.batch, &r);
+    E.last_plan_ms = c.batch->last_ms;
+    return std::unique_ptr<sdb_result>(r);
+}
+
 // ------------------------------------------------------------------ batches on caller memory
 // Used by the request server: a batch sized from a sizing pass, built on
 // memory carved from the server's pools and run once, eagerly, on a slot's
@@ -2111,6 +2170,7 @@ int sdb_engine_create(const sdb_engine_config *cfg, sdb_engine **out)
         }
         E.mm.init(budget, E.stream);
         E.prof.on = E.cfg.profile != 0;
+        if (E.cfg.plan_cache < 0) throw sdb::Error(SDB_ERR_INVALID, "plan_cache must be >= 0");
         SDB_CUDA(cudaEventCreate(&E.plan_a));
         SDB_CUDA(cudaEventCreate(&E.plan_b));
         SDB_CUDA(cudaStreamSynchronize(E.stream));
@@ -2124,6 +2184,7 @@ int sdb_engine_destroy(sdb_engine *eng)
     if (!eng) return SDB_OK;
     sdb::Engine &E = eng->E;
     cudaStreamSynchronize(E.stream);
+    sdb::plan_cache_clear(*eng);
     for (auto &t : E.tables)
         for (auto p : t.second->owned) cudaFree(p);
     E.tables.clear();
@@ -2139,7 +2200,10 @@ int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const in
                           int on_device)
 {
     if (!eng) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_load_table: engine is NULL");
-    return sdb::guarded([&] { sdb::load_table(eng->E, name, ncols, cols, nrows, on_device); });
+    return sdb::guarded([&] {
+        sdb::plan_cache_clear(*eng);
+        sdb::load_table(eng->E, name, ncols, cols, nrows, on_device);
+    });
 }
 
 int sdb_engine_execute(sdb_engine *eng, const char *plan_json, sdb_result **out)
@@ -2147,7 +2211,8 @@ int sdb_engine_execute(sdb_engine *eng, const char *plan_json, sdb_result **out)
     if (!eng || !plan_json || !out) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_execute: NULL argument");
     *out = nullptr;
     return sdb::guarded([&] {
-        auto r = sdb::execute_plan(eng->E, plan_json);
+        auto r = (eng->E.cfg.plan_cache > 0 && !eng->E.prof.on) ? sdb::execute_cached(*eng, plan_json)
+                                                                  : sdb::execute_plan(eng->E, plan_json);
         *out = r.release();
     });
 }

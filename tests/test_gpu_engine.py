@@ -177,3 +177,28 @@ def test_reversed_search_range_is_empty(variant):
                 assert eng.execute(plan).canonical() == datasets.oracle_run(ds, plan), json.dumps(plan)
     finally:
         capi.force_chain_variant(-1)
+
+
+def test_plan_cache_replays_give_the_plain_results():
+    """plan_cache: a plan seen twice becomes a prepared graph; replays, LRU
+    eviction and table reloads all give the plain path's rows."""
+    ds = datasets.dataset(0.05)
+    pls = [plans.plan_star(2, 11), plans.plan_filter_sum(1994), plans.plan_date_join(1995),
+           plans.plan_star(1, 3, 1993, 1996, 12)]
+    with Engine(arena_bytes=1 << 30) as plain:
+        load(plain, ds)
+        want = [plain.execute(p).canonical() for p in pls]
+    with Engine(arena_bytes=1 << 30, plan_cache=2) as eng:
+        load(eng, ds)
+        for _ in range(4):  # two plans fit the cache: the others keep being evicted and prepared again
+            for p, w in zip(pls, want):
+                assert eng.execute(p).canonical() == w
+                assert eng.last_plan_ms() > 0
+        # reloading a table drops the prepared plans: new data, new rows
+        lo = ds["lineorder"]
+        lo2 = {c: (a[::-1].copy() if c == 12 else a) for c, a in lo.items()}  # revenue permuted
+        eng.load_table("lineorder", lo2)
+        ds2 = dict(ds)
+        ds2["lineorder"] = lo2
+        for _ in range(3):
+            assert eng.execute(pls[0]).canonical() == datasets.oracle_run(ds2, pls[0])
