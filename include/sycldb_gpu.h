@@ -392,6 +392,24 @@ int sdb_engine_destroy(sdb_engine *eng);
 int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const int32_t *const *cols,
                           uint64_t nrows, int on_device);
 
+/* Register a base table from the reference's columnar files (Table::Table,
+ * models/models.hpp:1659-1708): one file per column, dir/<NAME><i> with the
+ * table name upper-cased ("LINEORDER5"), raw int32 in the machine's byte
+ * order.  column_mask: bit i loads column i; 0 = the reference loader's
+ * column set (kernels/types.cpp:3-11).  The row count is the first loaded
+ * column's; a missing file, or one of another length, leaves that column
+ * unloaded with a warning on stderr, as the reference does.  Files are read
+ * in 32 MB chunks through two pinned buffers so that reading overlaps the
+ * copies to the device.  background = 1: returns at once; a loader thread
+ * reads, copies and computes segment min/max on its own stream, and the
+ * first execute that scans the table (or sdb_engine_sync_tables) waits for
+ * it and installs it -- the whole-table counterpart of the reference's
+ * background copy activated on first use (models/models.hpp:489-564).  A
+ * failed background load reports its error at that point. */
+int sdb_engine_load_dir(sdb_engine *eng, const char *dir, const char *name, uint64_t column_mask, int background);
+/* Waits for every background load and installs the tables. */
+int sdb_engine_sync_tables(sdb_engine *eng);
+
 /* Execute one plan; on success *out holds the result rows (host memory).
  * With plan_cache > 0 (and profile = 0) the second execution of the same plan
  * text prepares it as a one-plan batch (sdb_engine_batch_prepare: recorded

@@ -135,6 +135,8 @@ _SIGS = {
     "sdb_engine_destroy": (c_int, [c_void_p]),
     "sdb_engine_load_table": (c_int, [c_void_p, c_char_p, c_int, POINTER(c_void_p), c_uint64, c_int]),
     "sdb_engine_execute": (c_int, [c_void_p, c_char_p, POINTER(c_void_p)]),
+    "sdb_engine_load_dir": (c_int, [c_void_p, c_char_p, c_char_p, c_uint64, c_int]),
+    "sdb_engine_sync_tables": (c_int, [c_void_p]),
     "sdb_result_shape": (c_int, [c_void_p, POINTER(c_int), POINTER(c_uint64)]),
     "sdb_result_column": (c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_void_p)]),
     "sdb_result_write_res": (c_int, [c_void_p, c_char_p]),

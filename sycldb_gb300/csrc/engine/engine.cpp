@@ -24,6 +24,7 @@
 #include <cstring>
 #include <deque>
 #include <fstream>
+#include <future>
 #include <functional>
 #include <map>
 #include <memory>
@@ -679,6 +680,9 @@ struct Engine {
     uint64_t seg = kDefaultSegment;
     MemoryManager mm;
     std::map<std::string, std::unique_ptr<Table>> tables;
+    // Tables being loaded from column files in the background: installed by
+    // the first plan that scans them (activate).
+    std::map<std::string, std::future<std::unique_ptr<Table>>> pending;
     Profiler prof;
     double last_plan_ms = 0;
     cudaEvent_t plan_a = nullptr, plan_b = nullptr;
@@ -1511,6 +1515,144 @@ struct sdb_batch {
 
 namespace sdb {
 
+// ------------------------------------------------------------------ table installation
+// Replaces (or adds) table `name`: the old table's device buffers are freed
+// once the engine's stream is idle.
+void install_table(Engine &E, const std::string &name, std::unique_ptr<Table> t)
+{
+    auto old = E.tables.find(name);
+    if (old != E.tables.end()) {
+        SDB_CUDA(cudaStreamSynchronize(E.stream));
+        for (auto p : old->second->owned) cudaFree(p);
+        E.tables.erase(old);
+    }
+    E.tables[name] = std::move(t);
+}
+
+// Waits for a background load of `name`, if one is pending, and installs it
+// (Segment::activate_background_buffer, models/models.hpp:541-550, for a
+// whole table).
+void activate_table(Engine &E, const std::string &name)
+{
+    auto it = E.pending.find(name);
+    if (it == E.pending.end()) return;
+    auto fut = std::move(it->second);
+    E.pending.erase(it);
+    install_table(E, name, fut.get());  // rethrows the loader's error
+}
+
+// Reads table `name` from the reference's columnar files -- one file per
+// column, dir/<NAME><i> with the table name upper-cased, raw int32 in the
+// machine's byte order (Table::Table, models/models.hpp:1659-1708) -- into
+// new device buffers, and computes per-segment min/max.  Only the columns of
+// `mask` (bit i = column i) are read; the row count is the first read
+// column's; a missing file or one of another length leaves that column
+// unloaded, as the reference does.  File reads of 32 MB chunks alternate
+// between two pinned buffers so that reading overlaps the copies.
+std::unique_ptr<Table> load_columns(const std::string &dir, const std::string &name, int ncols, uint64_t mask,
+                                    uint64_t seg_rows, cudaStream_t s, std::vector<std::string> *warnings)
+{
+    constexpr size_t kChunk = 32u << 20;
+    std::string upper = base_name(name);
+    std::transform(upper.begin(), upper.end(), upper.begin(), [](unsigned char ch) { return (char)std::toupper(ch); });
+    std::string prefix = dir;
+    if (!prefix.empty() && prefix.back() != '/') prefix += '/';
+    auto t = std::make_unique<Table>();
+    t->name = name;
+    t->columns.resize(ncols);
+    bool nrows_set = false;
+    char *pin[2] = {nullptr, nullptr};
+    cudaEvent_t done[2] = {nullptr, nullptr};
+    auto cleanup = [&]() {
+        for (int b = 0; b < 2; b++) {
+            if (done[b]) cudaEventSynchronize(done[b]), cudaEventDestroy(done[b]);
+            if (pin[b]) cudaFreeHost(pin[b]);
+        }
+    };
+    std::vector<std::pair<int, int32_t *>> dev_cols;
+    try {
+        for (int b = 0; b < 2; b++) {
+            SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&pin[b]), kChunk, cudaHostAllocDefault));
+            SDB_CUDA(cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
+        }
+        int b = 0;
+        for (int c = 0; c < ncols && c < 64; c++) {
+            if (!((mask >> c) & 1u)) continue;
+            const std::string file = prefix + upper + std::to_string(c);
+            std::ifstream in(file, std::ios::binary | std::ios::ate);
+            if (!in) {
+                if (warnings) warnings->push_back("column file missing: " + file);
+                continue;
+            }
+            const uint64_t bytes = (uint64_t)in.tellg();
+            const uint64_t n = bytes / sizeof(int32_t);
+            if (!nrows_set) {
+                if (n == 0) throw Error(SDB_ERR_INVALID, "empty column file " + file);
+                t->nrows = n;
+                nrows_set = true;
+            }
+            if (n != t->nrows || bytes % sizeof(int32_t)) {
+                if (warnings)
+                    warnings->push_back("column length mismatch in " + file + ": expected " + std::to_string(t->nrows) +
+                                        ", got " + std::to_string(n));
+                continue;
+            }
+            in.seekg(0);
+            int32_t *d = nullptr;
+            SDB_CUDA(cudaMalloc(&d, bytes));
+            t->owned.push_back(d);
+            for (uint64_t off = 0; off < bytes; off += kChunk) {
+                const size_t len = (size_t)std::min<uint64_t>(kChunk, bytes - off);
+                SDB_CUDA(cudaEventSynchronize(done[b]));  // the buffer's previous copy is done
+                if (!in.read(pin[b], (std::streamsize)len)) throw Error(SDB_ERR_INVALID, "read failed: " + file);
+                SDB_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(d) + off, pin[b], len, cudaMemcpyHostToDevice, s));
+                SDB_CUDA(cudaEventRecord(done[b], s));
+                b ^= 1;
+            }
+            dev_cols.emplace_back(c, d);
+        }
+        if (!nrows_set) throw Error(SDB_ERR_INVALID, "no column file of table " + name + " under " + dir);
+        // Segment statistics (models/models.hpp:71-77), on the device.
+        auto sg = split_rows(t->nrows, seg_rows);
+        const size_t nmm = dev_cols.size() * sg.size() * 2;
+        int32_t *mm = nullptr;
+        SDB_CUDA(cudaMalloc(&mm, std::max<size_t>(nmm, 2) * sizeof(int32_t)));
+        size_t q = 0;
+        int st = SDB_OK;
+        for (auto &dc : dev_cols)
+            for (auto [start, cnt] : sg)
+                if (st == SDB_OK) st = sdb_min_max_i32(dc.second + start, cnt, mm + 2 * (q++), (sdb_stream_t)s);
+        std::vector<int32_t> host(nmm);
+        cudaError_t e1 = st == SDB_OK ? cudaMemcpyAsync(host.data(), mm, nmm * sizeof(int32_t), cudaMemcpyDeviceToHost, s)
+                                      : cudaSuccess;
+        cudaError_t e2 = cudaStreamSynchronize(s);
+        cudaFree(mm);
+        check(st);
+        if (e1 != cudaSuccess || e2 != cudaSuccess)
+            throw Error(SDB_ERR_CUDA, std::string("load_dir: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+        q = 0;
+        for (auto &dc : dev_cols) {
+            Column &col = t->columns[dc.first];
+            for (auto [start, cnt] : sg) {
+                Segment sgm;
+                sgm.data = dc.second + start;
+                sgm.nrows = cnt;
+                sgm.min = host[2 * q];
+                sgm.max = host[2 * q + 1];
+                col.segments.push_back(sgm);
+                q++;
+            }
+        }
+    } catch (...) {
+        cleanup();
+        cudaStreamSynchronize(s);
+        for (auto p : t->owned) cudaFree(p);
+        throw;
+    }
+    cleanup();
+    return t;
+}
+
 // execute_ddor_plan (executor/ddor_executor.cpp:22-245) up to the result
 // materialisation of save_result (executor/result_writer.cpp:12-68): every
 // device operation goes through Engine::dev.  The caller resets the arena.
@@ -1523,6 +1665,8 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
 
     std::deque<TransientTable> tts;
     std::vector<int> output_table(plan.rels.size(), -1);
+    for (const RelNode &rel : plan.rels)
+        if (rel.relOp == TABLE_SCAN) activate_table(E, rel.tables[1]);
     for (const RelNode &rel : plan.rels) {
         if (rel.relOp != TABLE_SCAN) continue;
         const std::string &name = rel.tables[1];
@@ -1676,6 +1820,7 @@ std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text
 void load_table(Engine &E, const char *name, int ncols, const int32_t *const *cols, uint64_t nrows, int on_device)
 {
     if (!name) throw Error(SDB_ERR_INVALID, "table name is NULL");
+    activate_table(E, name);  // a background load of the same name finishes first
     auto it = table_column_numbers().find(base_name(name));
     if (it == table_column_numbers().end()) throw Error(SDB_ERR_INVALID, std::string("unknown table ") + name);
     if (ncols != it->second)
@@ -2185,6 +2330,14 @@ int sdb_engine_destroy(sdb_engine *eng)
     sdb::Engine &E = eng->E;
     cudaStreamSynchronize(E.stream);
     sdb::plan_cache_clear(*eng);
+    for (auto &pl : E.pending) {  // finish background loads, then free them
+        try {
+            auto t = pl.second.get();
+            for (auto p : t->owned) cudaFree(p);
+        } catch (...) {
+        }
+    }
+    E.pending.clear();
     for (auto &t : E.tables)
         for (auto p : t.second->owned) cudaFree(p);
     E.tables.clear();
@@ -2203,6 +2356,59 @@ int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const in
     return sdb::guarded([&] {
         sdb::plan_cache_clear(*eng);
         sdb::load_table(eng->E, name, ncols, cols, nrows, on_device);
+    });
+}
+
+int sdb_engine_load_dir(sdb_engine *eng, const char *dir, const char *name, uint64_t column_mask, int background)
+{
+    if (!eng || !dir || !name) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_load_dir: NULL argument");
+    return sdb::guarded([&] {
+        sdb::Engine &E = eng->E;
+        const std::string tname = name;
+        auto it = sdb::table_column_numbers().find(sdb::base_name(tname));
+        if (it == sdb::table_column_numbers().end()) throw sdb::Error(SDB_ERR_INVALID, "unknown table " + tname);
+        const int ncols = it->second;
+        uint64_t mask = column_mask;
+        if (mask == 0)
+            for (int c : sdb::table_column_indices().at(sdb::base_name(tname))) mask |= 1ull << c;
+        if (ncols < 64 && (mask >> ncols))
+            throw sdb::Error(SDB_ERR_INVALID, "column_mask names columns beyond the table's " + std::to_string(ncols));
+        sdb::plan_cache_clear(*eng);
+        sdb::activate_table(E, tname);
+        const uint64_t seg = E.seg;
+        const std::string d = dir;
+        auto work = [d, tname, ncols, mask, seg](int device) {
+            cudaSetDevice(device);
+            cudaStream_t s = nullptr;
+            SDB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+            std::vector<std::string> warn;
+            std::unique_ptr<sdb::Table> t;
+            try {
+                t = sdb::load_columns(d, tname, ncols, mask, seg, s, &warn);
+            } catch (...) {
+                cudaStreamDestroy(s);
+                throw;
+            }
+            cudaStreamDestroy(s);
+            for (auto &w : warn) std::fprintf(stderr, "sycldb: %s\n", w.c_str());
+            return t;
+        };
+        int device = 0;
+        SDB_CUDA(cudaGetDevice(&device));
+        if (background)
+            E.pending[tname] = std::async(std::launch::async, work, device);
+        else
+            sdb::install_table(E, tname, work(device));
+    });
+}
+
+int sdb_engine_sync_tables(sdb_engine *eng)
+{
+    if (!eng) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_sync_tables: engine is NULL");
+    return sdb::guarded([&] {
+        std::vector<std::string> names;
+        for (auto &p : eng->E.pending) names.push_back(p.first);
+        for (auto &n : names) sdb::activate_table(eng->E, n);
     });
 }
 

@@ -146,6 +146,22 @@ class Engine:
         else:
             self._keep.pop(name, None)
 
+    def load_dir(self, directory: str, name: str, columns=None, background: bool = False):
+        """Registers table ``name`` from the reference's columnar files
+        (``directory/<NAME><i>``, raw int32); ``columns`` = column indices to
+        read (default: the reference loader's set).  With ``background`` the
+        call returns at once and the first plan that scans the table waits
+        for it."""
+        mask = 0
+        for c in columns or ():
+            mask |= 1 << c
+        capi.check(capi.lib().sdb_engine_load_dir(self._h, directory.encode(), name.encode(), mask,
+                                                  1 if background else 0))
+        self._keep.pop(name, None)
+
+    def sync_tables(self):
+        capi.check(capi.lib().sdb_engine_sync_tables(self._h))
+
     def execute(self, plan) -> Result:
         text = plan if isinstance(plan, str) else json.dumps(plan)
         L = capi.lib()

@@ -162,3 +162,16 @@ def gen_dims(sf: float, seed: int = SEED) -> Dict[str, Dict[int, np.ndarray]]:
         "part": gen_part(dim_rows("part", sf), seed),
         "ddate": gen_ddate(),
     }
+
+
+def write_columnar(directory: str, tables: Dict[str, Dict[int, np.ndarray]]):
+    """Writes tables in the reference's columnar layout: one raw int32 file
+    per column, ``directory/<NAME><i>`` with the table's base name
+    upper-cased (what ``Engine.load_dir`` and the reference's loader read)."""
+    import os
+
+    os.makedirs(directory, exist_ok=True)
+    for name, cols in tables.items():
+        base = name.split("@", 1)[0].upper()
+        for c, a in cols.items():
+            np.ascontiguousarray(a, dtype=np.int32).tofile(os.path.join(directory, "%s%d" % (base, c)))
