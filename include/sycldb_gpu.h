@@ -201,6 +201,18 @@ int sdb_count_flags(const uint8_t *flags, uint64_t n, uint64_t *out, sdb_stream_
  * (models/models.hpp:71-77). */
 int sdb_min_max_i32(const int32_t *col, uint64_t n, int32_t *minmax, sdb_stream_t stream);
 
+/* ORDER BY: perm[0..n) = the row ids 0..n-1 ordered by keys[0], then keys[1],
+ * ... (nkeys <= 16; key_types[k] 0 = int32 compared signed, 1 = uint64
+ * compared unsigned, the comparisons of the reference's sort_table,
+ * kernels/sort.hpp:7-103; descending[k] != 0 reverses key k).  Stable: equal
+ * rows keep their order.  n <= 2^31.  A radix sort: 4 passes per int32 key,
+ * 8 per uint64 key.  scratch: sdb_sort_scratch_bytes(n) bytes, 256-byte aligned.
+ * The reference's executor itself treats SORT as a pass-through
+ * (executor/ddor_executor.cpp:209-211). */
+size_t sdb_sort_scratch_bytes(uint64_t n);
+int sdb_sort_rows(const void *const *keys, const int *key_types, const int *descending, int nkeys, uint64_t n,
+                  uint32_t *perm, void *scratch, size_t scratch_bytes, sdb_stream_t stream);
+
 /* ------------------------------------------------------ fused operator chain */
 
 /* One pass over a segment that applies a KernelBundle's kernels in order with
@@ -372,7 +384,9 @@ typedef struct sdb_engine_config {
     int32_t profile;            /* 1: time every launch with CUDA events */
     sdb_stream_t stream;        /* NULL: the engine creates its own stream */
     int32_t plan_cache;         /* > 0: prepared plans kept (see sdb_engine_execute); 0: none */
-    int32_t pad;
+    int32_t order_by;           /* 1: sdb_engine_execute orders result rows by the plan's last SORT
+                                   collation on the device (sdb_sort_rows); 0: rows in the order the
+                                   reference gives them (its SORT is a pass-through) */
 } sdb_engine_config;
 
 /* Parses a plan and derives its execution order and group-by columns

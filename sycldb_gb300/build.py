@@ -22,7 +22,7 @@ OUT = os.path.join(PKG, "_build")
 LIB = os.path.join(OUT, "libsycldb_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_SOURCES = ["kernels.cu", "fused.cu"]
+CU_SOURCES = ["kernels.cu", "fused.cu", "sort.cu"]
 CPP_SOURCES = ["errors.cpp", os.path.join("engine", "engine.cpp"), os.path.join("engine", "server.cpp")]
 
 

@@ -57,7 +57,7 @@ class ChainDesc(ctypes.Structure):
 
 class EngineConfig(ctypes.Structure):
     _fields_ = [("arena_bytes", c_uint64), ("segment_rows", c_uint64), ("fuse", c_int32), ("profile", c_int32),
-                ("stream", c_void_p), ("plan_cache", c_int32), ("pad", c_int32)]
+                ("stream", c_void_p), ("plan_cache", c_int32), ("order_by", c_int32)]
 
 
 class BatchStats(ctypes.Structure):
@@ -110,6 +110,9 @@ _SIGS = {
     "sdb_gather_u64": (c_int, [_P, _P, _P, _P, c_uint64, _P]),
     "sdb_count_flags": (c_int, [_P, c_uint64, _P, _P]),
     "sdb_min_max_i32": (c_int, [_P, c_uint64, _P, _P]),
+    "sdb_sort_scratch_bytes": (c_size_t, [c_uint64]),
+    "sdb_sort_rows": (c_int, [POINTER(c_void_p), POINTER(c_int), POINTER(c_int), c_int, c_uint64, _P, _P, c_size_t,
+                              _P]),
     "sdb_fused_chain": (c_int, [POINTER(ChainDesc), _P]),
     "sdb_fused_chain_variant": (c_int, [POINTER(ChainDesc), c_int, _P]),
     "sdb_chain_tune_set": (c_int, [c_int, c_int, c_uint64, c_int]),

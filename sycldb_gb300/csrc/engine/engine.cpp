@@ -1442,6 +1442,7 @@ struct PendingSeg {
 struct PendingResult {
     std::vector<int> types;  // 0 int32, 1 uint64
     std::vector<PendingSeg> segs;
+    std::vector<std::pair<int, int>> order;  // ORDER BY: (result column, descending), first key first
 };
 
 }  // namespace sdb
@@ -1732,6 +1733,20 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
             cols.push_back(c);
         }
     for (Column *c : cols) pr.types.push_back(c->is_aggregate_result ? 1 : 0);
+    // ORDER BY: the collation of the plan's last SORT node, its fields being
+    // positions in the final table's columns
+    for (auto k = info.dag_order.rbegin(); k != info.dag_order.rend(); ++k) {
+        const RelNode &rel = plan.rels[*k];
+        if (rel.relOp != SORT || rel.collation.empty()) continue;
+        for (const CollationType &c : rel.collation) {
+            if (c.field < 0 || (size_t)c.field >= fin.current_columns.size() || !fin.current_columns[c.field])
+                throw Error(SDB_ERR_UNSUPPORTED, "ORDER BY field " + std::to_string(c.field) + " is not a result column");
+            const Column *col = fin.current_columns[c.field];
+            const int pos = (int)(std::find(cols.begin(), cols.end(), col) - cols.begin());
+            pr.order.emplace_back(pos, c.direction == 0 ? 1 : 0);
+        }
+        break;
+    }
     auto sg = fin.segs();
     for (size_t s = 0; s < sg.size(); s++) {
         const uint64_t cnt = sg[s].second;
@@ -1770,6 +1785,66 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
     return pr;
 }
 
+// ORDER BY on the device: the result rows of all segments are laid end to
+// end, sorted by the collation keys (sdb_sort_rows, stable) and gathered in
+// that order; pr then describes one segment of `total` rows.
+void sort_result(Engine &E, PendingResult &pr, std::vector<uint32_t> &counts, uint64_t total)
+{
+    const size_t ncols = pr.types.size();
+    cudaStream_t st = E.stream;
+    std::vector<void *> flat(ncols);
+    for (size_t c = 0; c < ncols; c++) {
+        const size_t w = pr.types[c] == 1 ? 8 : 4;
+        if (pr.segs.size() == 1) {
+            flat[c] = pr.segs[0].dev[c];
+            continue;
+        }
+        char *d = E.mm.alloc<char>(total * w);
+        uint64_t at = 0;
+        for (size_t s = 0; s < pr.segs.size(); s++) {
+            if (counts[s]) SDB_CUDA(cudaMemcpyAsync(d + at * w, pr.segs[s].dev[c], counts[s] * w, cudaMemcpyDeviceToDevice, st));
+            at += counts[s];
+        }
+        flat[c] = d;
+    }
+    std::vector<const void *> keys;
+    std::vector<int> types, desc;
+    for (auto &o : pr.order) {
+        keys.push_back(flat[o.first]);
+        types.push_back(pr.types[o.first]);
+        desc.push_back(o.second);
+    }
+    uint32_t *perm = E.mm.alloc<uint32_t>(total);
+    const size_t sb = sdb_sort_scratch_bytes(total);
+    void *scratch = E.mm.alloc<uint8_t>(sb);
+    E.dev("sort_rows", [&](cudaStream_t s) {
+        return sdb_sort_rows(keys.data(), types.data(), desc.data(), (int)keys.size(), total, perm, scratch, sb,
+                             (sdb_stream_t)s);
+    });
+    uint32_t *count = E.mm.alloc<uint32_t>(1);
+    const uint32_t t32 = (uint32_t)total;
+    SDB_CUDA(cudaMemcpyAsync(count, &t32, sizeof t32, cudaMemcpyHostToDevice, st));
+    PendingSeg one;
+    one.count = count;
+    one.cap = total;
+    for (size_t c = 0; c < ncols; c++) {
+        if (pr.types[c] == 1) {
+            uint64_t *d = E.mm.alloc<uint64_t>(total);
+            check(sdb_gather_u64(static_cast<const uint64_t *>(flat[c]), reinterpret_cast<const int32_t *>(perm), count, d,
+                                 total, (sdb_stream_t)st));
+            one.dev.push_back(d);
+        } else {
+            int32_t *d = E.mm.alloc<int32_t>(total);
+            check(sdb_gather_i32(static_cast<const int32_t *>(flat[c]), reinterpret_cast<const int32_t *>(perm), count, d,
+                                 total, (sdb_stream_t)st));
+            one.dev.push_back(d);
+        }
+    }
+    SDB_CUDA(cudaStreamSynchronize(st));  // t32 lives on this frame
+    pr.segs.assign(1, one);
+    counts.assign(1, (uint32_t)total);
+}
+
 std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text)
 {
     E.mm.reset(E.stream);
@@ -1794,6 +1869,7 @@ std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text
         else
             res->i32[ci].resize(total);
     }
+    if (E.cfg.order_by && !pr.order.empty() && total > 1) sort_result(E, pr, counts, total);
     uint64_t base = 0;
     for (size_t s = 0; s < pr.segs.size(); s++) {
         for (size_t ci = 0; ci < ncols; ci++) {
@@ -2417,8 +2493,9 @@ int sdb_engine_execute(sdb_engine *eng, const char *plan_json, sdb_result **out)
     if (!eng || !plan_json || !out) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_execute: NULL argument");
     *out = nullptr;
     return sdb::guarded([&] {
-        auto r = (eng->E.cfg.plan_cache > 0 && !eng->E.prof.on) ? sdb::execute_cached(*eng, plan_json)
-                                                                  : sdb::execute_plan(eng->E, plan_json);
+        auto r = (eng->E.cfg.plan_cache > 0 && !eng->E.prof.on && !eng->E.cfg.order_by)
+                     ? sdb::execute_cached(*eng, plan_json)
+                     : sdb::execute_plan(eng->E, plan_json);
         *out = r.release();
     });
 }

@@ -202,3 +202,31 @@ def test_plan_cache_replays_give_the_plain_results():
         ds2["lineorder"] = lo2
         for _ in range(3):
             assert eng.execute(pls[0]).canonical() == datasets.oracle_run(ds2, pls[0])
+
+
+def test_order_by_on_the_device():
+    """order_by: rows come out ordered by the plan's SORT collation (stable:
+    ties keep row order), also across segments and on uint64 sums."""
+    ds = datasets.dataset(0.05)
+    star = plans.plan_star(2, 11)  # SORT on (d_year, p_brand1), ascending
+    by_sum = json.loads(json.dumps(star))
+    by_sum["rels"][-1]["collation"] = [{"field": 2, "direction": "DESCENDING", "nulls": "LAST"},
+                                       {"field": 0, "direction": "ASCENDING", "nulls": "LAST"}]
+    b = plans.PlanBuilder()  # a large, multi-segment result
+    b.scan("lineorder")
+    b.filter(plans.search(11, 2, 3))
+    b.project([plans.col(5), plans.col(9)])
+    b.sort([1, 0])
+    wide = b.plan()
+    wide["rels"][-1]["collation"][0]["direction"] = "DESCENDING"
+    with Engine(arena_bytes=1 << 30, segment_rows=1 << 14) as plain:
+        load(plain, ds)
+        rows = {i: plain.execute(p).rows() for i, p in enumerate((star, by_sum, wide))}
+    with Engine(arena_bytes=1 << 30, segment_rows=1 << 14, order_by=True, plan_cache=2) as eng:
+        load(eng, ds)
+        for _ in range(2):
+            assert eng.execute(star).rows() == sorted(rows[0], key=lambda r: (r[0], r[1]))
+            assert eng.execute(by_sum).rows() == sorted(rows[1], key=lambda r: (-r[2], r[0]))
+            got = eng.execute(wide).rows()
+            assert len(got) > 1 << 15  # rows from many 16K-row segments
+            assert got == sorted(rows[2], key=lambda r: (-r[1], r[0]))
