@@ -148,3 +148,56 @@ def plan_star(region: int, category: int, year_lo: int = None, year_hi: int = No
     b.aggregate([0, 1], 2)
     b.sort([0, 1])
     return b.plan()
+
+
+def plan_customer_supplier_date(region: int, year_lo: int = 1992, year_hi: int = 1997, city_points=None,
+                                fact_tag=None) -> dict:
+    """SSB flight-3 shape: lineorder joined with customer (region filter, or
+    c_city in two points), supplier (same) and date (year range); group by
+    (customer nation or city, supplier nation or city, d_year); SUM(lo_revenue).
+    Three group-by keys, one from each dimension."""
+    b = PlanBuilder()
+    f = b.scan(_t("lineorder", fact_tag))
+    c = b.scan("customer")
+    if city_points:
+        c = b.filter(search_points(3, city_points[0], city_points[1]))
+    else:
+        c = b.filter(expr("==", col(5), lit(region)))
+    j1 = b.join(f, c, 2, 17 + 0)                           # customer -> 17..24
+    s = b.scan("supplier")
+    if city_points:
+        s = b.filter(search_points(3, city_points[0], city_points[1]))
+    else:
+        s = b.filter(expr("==", col(5), lit(region)))
+    j2 = b.join(j1, s, 4, 25 + 0)                          # supplier -> 25..31
+    d = b.scan("ddate")
+    d = b.filter(search(4, year_lo, year_hi))
+    b.join(j2, d, 5, 32 + 0)                               # ddate -> 32..48
+    key = 3 if city_points else 4                          # c/s_city or c/s_nation
+    b.project([col(17 + key), col(25 + key), col(32 + 4), col(12)])
+    b.aggregate([0, 1, 2], 3)
+    b.sort([2, 0, 1])
+    return b.plan()
+
+
+def plan_profit(region: int, mfgr_points=(0, 1), fact_tag=None) -> dict:
+    """SSB flight-4 shape: four joins -- customer (region, group by nation),
+    supplier (region, semi join), part (p_mfgr in two points, semi join), date
+    (group by year); SUM(lo_revenue - lo_supplycost)."""
+    b = PlanBuilder()
+    f = b.scan(_t("lineorder", fact_tag))
+    c = b.scan("customer")
+    c = b.filter(expr("==", col(5), lit(region)))
+    j1 = b.join(f, c, 2, 17 + 0)                           # customer -> 17..24
+    s = b.scan("supplier")
+    s = b.filter(expr("==", col(5), lit(region)))
+    j2 = b.join(j1, s, 4, 25 + 0, "semi")                  # supplier -> 25..31
+    p = b.scan("part")
+    p = b.filter(search_points(2, mfgr_points[0], mfgr_points[1]))
+    j3 = b.join(j2, p, 3, 32 + 0, "semi")                  # part -> 32..40
+    d = b.scan("ddate")
+    b.join(j3, d, 5, 41 + 0)                               # ddate -> 41..57
+    b.project([col(41 + 4), col(17 + 4), expr("-", col(12), col(13))])
+    b.aggregate([0, 1], 2)
+    b.sort([0, 1])
+    return b.plan()

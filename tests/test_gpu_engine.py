@@ -230,3 +230,20 @@ def test_order_by_on_the_device():
             got = eng.execute(wide).rows()
             assert len(got) > 1 << 15  # rows from many 16K-row segments
             assert got == sorted(rows[2], key=lambda r: (-r[1], r[0]))
+
+
+@pytest.mark.parametrize("fuse", [False, True])
+def test_more_ssb_shapes_match_the_oracle(fuse):
+    """Three group-by keys over three dimensions (SSB flight 3, with the
+    region filter and with OR-of-two-points city filters) and the four-join
+    profit shape (flight 4: revenue - supplycost, two semi joins)."""
+    ds = datasets.dataset(0.05)
+    cases = [plans.plan_customer_supplier_date(2), plans.plan_customer_supplier_date(0, 1992, 1993),
+             plans.plan_customer_supplier_date(0, 1992, 1998, city_points=(21, 27)),
+             plans.plan_profit(1), plans.plan_profit(3, (2, 4))]
+    with Engine(arena_bytes=1 << 30, fuse=fuse, segment_rows=1 << 16) as eng:
+        load(eng, ds)
+        for plan in cases:
+            got = eng.execute(plan).canonical()
+            assert got == datasets.oracle_run(ds, plan, 1 << 16), json.dumps(plan)
+            assert len(got) > 0
