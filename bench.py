@@ -510,7 +510,7 @@ def run_batched(args, rank, world, local, pg, stream, peak):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.1)
-    lat_b, dev_ms, chain_ms = [], [], []
+    lat_b, dev_ms, chain_ms, pre_ms, post_ms = [], [], [], [], []
     barrier(pg)
     t0 = time.perf_counter()
     for _ in range(args.batched_runs):
@@ -520,6 +520,8 @@ def run_batched(args, rank, world, local, pg, stream, peak):
         st = b.stats()
         dev_ms.append(st["last_run_ms"])
         chain_ms.append(st["last_chain_ms"])
+        pre_ms.append(st["last_pre_ms"])
+        post_ms.append(st["last_post_ms"])
     batch_s = max_over_ranks(pg, time.perf_counter() - t0)
     clk = clocks.stop()
     st = b.stats()
@@ -546,6 +548,8 @@ def run_batched(args, rank, world, local, pg, stream, peak):
             "note": "batched: every plan of a batch completes when the batch run returns (host wall clock "
                     "around sdb_batch_run incl. result unpacking); plain: each sdb_engine_execute alone"},
         "device_ms_per_batch": statistics.median(dev_ms),
+        "device_ms_phases": {"before_chains": statistics.median(pre_ms), "chains": statistics.median(chain_ms),
+                             "after_chains": statistics.median(post_ms)},
         "chain_batch": {"kernel": "k_batch (persistent, span work queue; semi + full + full probe, group-by)",
                         "ms": chain_med, "algorithmic_bytes": fact_bytes,
                         "achieved": achieved, "peak": peak, "unit": "GB/s",

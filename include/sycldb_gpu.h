@@ -486,6 +486,8 @@ typedef struct sdb_batch_stats {
     uint64_t host_bytes;      /* pinned staging */
     double last_run_ms;       /* device milliseconds of the last run */
     double last_chain_ms;     /* of it, the chain batch's launches (0: none) */
+    double last_pre_ms;       /* before the chain batch: zeroing, dimension filters and builds */
+    double last_post_ms;      /* after it: final flags, compaction, gathers, result copies */
 } sdb_batch_stats;
 
 int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int n_plans, int flags,

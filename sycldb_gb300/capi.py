@@ -63,7 +63,8 @@ class EngineConfig(ctypes.Structure):
 class BatchStats(ctypes.Structure):
     _fields_ = [("n_plans", c_int32), ("kernels_per_run", c_int32), ("graph", c_int32), ("chain_launches", c_int32),
                 ("batched_chains", c_int32), ("pad", c_int32), ("arena_bytes", c_uint64), ("zero_bytes", c_uint64),
-                ("host_bytes", c_uint64), ("last_run_ms", c_double), ("last_chain_ms", c_double)]
+                ("host_bytes", c_uint64), ("last_run_ms", c_double), ("last_chain_ms", c_double),
+                ("last_pre_ms", c_double), ("last_post_ms", c_double)]
 
 
 class ServerConfig(ctypes.Structure):

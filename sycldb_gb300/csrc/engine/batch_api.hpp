@@ -28,7 +28,7 @@ struct Error : std::runtime_error {
 struct BatchSize {
     uint64_t arena = 0;     // arena bytes
     uint64_t zero = 0;      // zeroed-region bytes
-    uint64_t staging = 0;   // pinned result staging bytes
+    uint64_t staging = 0;   // result region bytes (on the device, and its pinned mirror)
     std::vector<sdb_chain_desc> chains;  // the aggregating chains (addresses of the sizing pass)
 };
 
@@ -50,9 +50,10 @@ size_t batch_chain_bytes(const std::vector<sdb_chain_desc> &chains);
 
 // Records `plans` (sized by `z`, which must be the sum of their sizing passes
 // with the chains concatenated) against the device region dev[0, dev_bytes)
-// -- arena, then zeroed region, then chain-batch tables, each rounded up to
-// 256 bytes -- and the pinned region pinned[0, pinned_bytes) -- chain-batch
-// tables, then result staging -- and enqueues the whole batch on the slot's
+// -- arena, then zeroed region, then result region (every plan's count and
+// result columns), then chain-batch tables, each rounded up to 256 bytes --
+// and the pinned region pinned[0, pinned_bytes) -- chain-batch tables, then
+// the result region's mirror -- and enqueues the whole batch on the slot's
 // streams.  Returns the batch; its results are read with batch_take_result
 // once the work on ss.main has completed.
 sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string> &plans, const BatchSize &z,

@@ -208,6 +208,7 @@ public:
     uint64_t size() const { return size_; }
     uint64_t zsize() const { return zsize_; }
     char *zero_base() const { return zbase_; }
+    char *base() const { return base_; }
 
     template <typename T>
     T *alloc(uint64_t count)
@@ -675,6 +676,9 @@ struct Recorder {
 struct Engine {
     sdb_engine_config cfg{};
     Recorder *rec = nullptr;  // non-null: record device work, don't run it
+    // non-null: where result counts and gathered result columns go (a batch's
+    // contiguous result region, copied to the host in one piece)
+    MemoryManager *rmm = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
     uint64_t seg = kDefaultSegment;
@@ -1483,12 +1487,15 @@ struct sdb_batch {
         std::vector<size_t> col_off;
     };
     std::vector<std::vector<Stage>> stage;  // [plan][segment]
+    sdb::MemoryManager rmm;  // result region: counts and result columns of every plan
+    char *rbase = nullptr;   // its base; B.host mirrors it byte for byte
+    size_t rbytes = 0;
     cudaStream_t bs = nullptr;              // the stream a run goes on
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr, ev_in = nullptr;
     cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;  // around the chain batch
-    double last_chain_ms = 0;
+    double last_chain_ms = 0, last_pre_ms = 0, last_post_ms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int kernels = 0;
@@ -1752,8 +1759,9 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
         const uint64_t cnt = sg[s].second;
         PendingSeg o;
         o.cap = cnt;
+        MemoryManager &R = E.rmm ? *E.rmm : E.mm;
         int32_t *ids = E.mm.alloc<int32_t>(cnt);
-        uint32_t *count = E.mm.alloc<uint32_t>(1);
+        uint32_t *count = R.alloc<uint32_t>(1);
         o.count = count;
         size_t sb = sdb_compact_scratch_bytes(cnt);
         void *scratch = E.mm.alloc<uint8_t>(sb);
@@ -1765,14 +1773,14 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
         for (Column *c : cols) {
             const Segment &seg = c->segments[s];
             if (c->is_aggregate_result) {
-                uint64_t *d = E.mm.alloc<uint64_t>(cnt);
+                uint64_t *d = R.alloc<uint64_t>(cnt);
                 const uint64_t *src = seg.agg;
                 E.dev("gather", [src, ids, count, d, cnt](cudaStream_t st) {
                     return sdb_gather_u64(src, ids, count, d, cnt, (sdb_stream_t)st);
                 });
                 o.dev.push_back(d);
             } else {
-                int32_t *d = E.mm.alloc<int32_t>(cnt);
+                int32_t *d = R.alloc<int32_t>(cnt);
                 const int32_t *src = seg.data;
                 E.dev("gather", [src, ids, count, d, cnt](cudaStream_t st) {
                     return sdb_gather_i32(src, ids, count, d, cnt, (sdb_stream_t)st);
@@ -1975,26 +1983,29 @@ void load_table(Engine &E, const char *name, int ncols, const int32_t *const *co
 // ------------------------------------------------------------------ batches
 // Records `plans` into B.rec against arena `mm` (swapped into the engine for
 // the duration).
-void record_plans(Engine &E, sdb_batch &B, MemoryManager &mm, const std::vector<std::string> &plans)
+void record_plans(Engine &E, sdb_batch &B, MemoryManager &mm, MemoryManager &rmm,
+                  const std::vector<std::string> &plans)
 {
-    struct Swap {  // the engine records into B against mm until scope exit
+    struct Swap {  // the engine records into B against mm (results in rmm) until scope exit
         Engine &E;
         MemoryManager &mm;
-        Swap(Engine &e, MemoryManager &m, Recorder *r) : E(e), mm(m)
+        Swap(Engine &e, MemoryManager &m, MemoryManager &r, Recorder *rec) : E(e), mm(m)
         {
             E.mm.swap(mm);
-            E.rec = r;
+            E.rec = rec;
+            E.rmm = &r;
         }
         ~Swap()
         {
             E.mm.swap(mm);
             E.rec = nullptr;
+            E.rmm = nullptr;
         }
     };
     B.rec = Recorder();
     B.rec.batch_chains = !(B.flags & SDB_BATCH_NO_CHAIN_BATCH);
     B.pend.clear();
-    Swap guard(E, mm, &B.rec);
+    Swap guard(E, mm, rmm, &B.rec);
     for (const std::string &pt : plans) {
         B.rec.plans.emplace_back();
         B.pend.push_back(run_plan(E, pt));
@@ -2028,61 +2039,22 @@ void replay(sdb_batch &B, cudaStream_t main)
         if (B.ev_c1) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c1, main, rf));
     }
     phase(true);
+    // every plan's count and result columns, in one copy to the pinned mirror
+    if (B.rbytes) SDB_CUDA(cudaMemcpyAsync(B.host, B.rbase, B.rbytes, cudaMemcpyDeviceToHost, main));
 }
 
-// Pinned staging of a recorded batch: per plan and segment, the count and
-// every result column at full capacity.  Lays it out (B.stage) and returns
-// its size.
-size_t staging_bytes(sdb_batch &B)
+// Where each plan's count and result columns sit in the result region (and
+// so in its pinned mirror B.host).
+void layout_results(sdb_batch &B, const char *rbase)
 {
-    size_t off = 0;
     B.stage.assign(B.pend.size(), {});
-    for (size_t p = 0; p < B.pend.size(); p++) {
-        const PendingResult &pr = B.pend[p];
-        for (const PendingSeg &sg : pr.segs) {
+    for (size_t p = 0; p < B.pend.size(); p++)
+        for (const PendingSeg &sg : B.pend[p].segs) {
             sdb_batch::Stage st;
-            st.count_off = off;
-            off += 64;
-            for (size_t c = 0; c < pr.types.size(); c++) {
-                st.col_off.push_back(off);
-                off += (sg.cap * (pr.types[c] == 1 ? 8 : 4) + 63) & ~(size_t)63;
-            }
+            st.count_off = (size_t)(reinterpret_cast<const char *>(sg.count) - rbase);
+            for (void *d : sg.dev) st.col_off.push_back((size_t)(static_cast<const char *>(d) - rbase));
             B.stage[p].push_back(st);
         }
-    }
-    return off;
-}
-
-// Appends to every plan the copies of its results into B.host (laid out by
-// staging_bytes), after the plan's last kernel.
-void add_result_copies(sdb_batch &B)
-{
-    for (size_t p = 0; p < B.pend.size(); p++) {
-        PlanRecord &rp = B.rec.plans[p];
-        auto &ops = rp.after ? rp.post : rp.pre;
-        const PendingResult &pr = B.pend[p];
-        for (size_t s = 0; s < pr.segs.size(); s++) {
-            const PendingSeg &sg = pr.segs[s];
-            char *dst = B.host + B.stage[p][s].count_off;
-            const void *cnt = sg.count;
-            ops.push_back({"d2h", [dst, cnt](cudaStream_t st) {
-                               return cudaMemcpyAsync(dst, cnt, 4, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                                          ? SDB_OK
-                                          : sdb_set_error(SDB_ERR_CUDA, "batch result copy failed");
-                           }});
-            for (size_t c = 0; c < pr.types.size(); c++) {
-                char *d = B.host + B.stage[p][s].col_off[c];
-                const void *src = sg.dev[c];
-                const size_t bytes = sg.cap * (pr.types[c] == 1 ? 8 : 4);
-                if (!bytes) continue;
-                ops.push_back({"d2h", [d, src, bytes](cudaStream_t st) {
-                                   return cudaMemcpyAsync(d, src, bytes, cudaMemcpyDeviceToHost, st) == cudaSuccess
-                                              ? SDB_OK
-                                              : sdb_set_error(SDB_ERR_CUDA, "batch result copy failed");
-                               }});
-            }
-        }
-    }
 }
 
 // Plan p's result from the staging of a finished run.
@@ -2125,10 +2097,11 @@ sdb_result *unpack_result(const sdb_batch &B, size_t p)
 void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plans)
 {
     // sizing pass: addresses only
-    MemoryManager vm;
+    MemoryManager vm, vr;
     vm.init_virtual();
-    record_plans(E, B, vm, plans);
-    const uint64_t used = vm.used(), zused = vm.zused();
+    vr.init_virtual();
+    record_plans(E, B, vm, vr, plans);
+    const uint64_t used = vm.used(), zused = vm.zused(), rused = vr.used();
     const size_t cb_bytes = B.rec.chains.empty()
                                 ? 0
                                 : sdb_chain_batch_scratch_bytes(B.rec.chains.data(), (int)B.rec.chains.size());
@@ -2136,7 +2109,8 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
 
     // real pass against an arena of exactly that size
     B.mm.init_sized(used + cb_bytes + 256, zused, E.stream);
-    record_plans(E, B, B.mm, plans);
+    B.rmm.init_sized(rused, 256, E.stream);
+    record_plans(E, B, B.mm, B.rmm, plans);
     if (!B.rec.chains.empty()) {
         void *scratch = B.mm.alloc<uint8_t>(cb_bytes);
         check(sdb_chain_batch_create(B.rec.chains.data(), (int)B.rec.chains.size(), scratch, cb_bytes,
@@ -2144,9 +2118,11 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
         B.chain_groups = sdb_chain_batch_kernels(B.cb);
     }
 
-    B.host_bytes = std::max<size_t>(staging_bytes(B), 64);
+    B.rbase = B.rmm.base();
+    B.rbytes = B.rmm.used();
+    layout_results(B, B.rbase);
+    B.host_bytes = std::max<size_t>(B.rbytes, 64);
     SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&B.host), B.host_bytes, cudaHostAllocDefault));
-    add_result_copies(B);
 
     // streams and events; the plans' work is spread over up to 8 streams
     SDB_CUDA(cudaStreamCreateWithFlags(&B.bs, cudaStreamNonBlocking));
@@ -2206,6 +2182,9 @@ void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
     if (B.cb) {
         float cms = 0;
         B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_c0, B.ev_c1) == cudaSuccess ? cms : -1.0;
+        float pre = 0, post = 0;
+        B.last_pre_ms = cudaEventElapsedTime(&pre, B.ev_a, B.ev_c0) == cudaSuccess ? pre : -1.0;
+        B.last_post_ms = cudaEventElapsedTime(&post, B.ev_c1, B.ev_b) == cudaSuccess ? post : -1.0;
     }
     if (!out) return;
     for (size_t p = 0; p < B.pend.size(); p++) out[p] = unpack_result(B, p);
@@ -2271,13 +2250,14 @@ BatchSize batch_size(sdb_engine *eng, const std::vector<std::string> &plans)
 {
     Engine &E = eng->E;
     sdb_batch B;
-    MemoryManager vm;
+    MemoryManager vm, vr;
     vm.init_virtual();
-    record_plans(E, B, vm, plans);
+    vr.init_virtual();
+    record_plans(E, B, vm, vr, plans);
     BatchSize z;
     z.arena = vm.used();
     z.zero = vm.zused();
-    z.staging = staging_bytes(B);
+    z.staging = vr.used();
     z.chains = B.rec.chains;
     return z;
 }
@@ -2296,22 +2276,26 @@ sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string>
     B.eng = eng;
     B.owns = false;
     const uint64_t arena = (z.arena + 255) & ~uint64_t(255), zero = (z.zero + 255) & ~uint64_t(255);
+    const uint64_t results = (z.staging + 255) & ~uint64_t(255);
     const size_t cb_bytes = batch_chain_bytes(z.chains);
-    if (arena + zero + cb_bytes > dev_bytes) throw Error(SDB_ERR_INVALID, "batch region too small");
+    if (arena + zero + results + cb_bytes > dev_bytes) throw Error(SDB_ERR_INVALID, "batch region too small");
     B.mm.init_external(dev, arena, dev + arena, zero);
-    record_plans(E, B, B.mm, plans);
-    if (B.mm.used() != z.arena || B.mm.zused() != z.zero) throw Error(SDB_ERR_INVALID, "batch sizing mismatch");
-    const size_t stage = staging_bytes(B);
-    if (cb_bytes + stage > pinned_bytes) throw Error(SDB_ERR_INVALID, "batch staging too small");
+    B.rmm.init_external(dev + arena + zero, results, nullptr, 0);
+    record_plans(E, B, B.mm, B.rmm, plans);
+    if (B.mm.used() != z.arena || B.mm.zused() != z.zero || B.rmm.used() != z.staging)
+        throw Error(SDB_ERR_INVALID, "batch sizing mismatch");
+    if (cb_bytes + z.staging > pinned_bytes) throw Error(SDB_ERR_INVALID, "batch staging too small");
     B.host = pinned + cb_bytes;
-    B.host_bytes = stage;
-    add_result_copies(B);
+    B.host_bytes = z.staging;
+    B.rbase = dev + arena + zero;
+    B.rbytes = z.staging;
+    layout_results(B, B.rbase);
     B.side = ss.side;
     B.join = ss.join;
     B.fork = ss.fork;
     if (!B.rec.chains.empty())
-        check(sdb_chain_batch_create_async(B.rec.chains.data(), (int)B.rec.chains.size(), dev + arena + zero, cb_bytes,
-                                           pinned, cb_bytes, (sdb_stream_t)ss.main, &B.cb));
+        check(sdb_chain_batch_create_async(B.rec.chains.data(), (int)B.rec.chains.size(), dev + arena + zero + results,
+                                           cb_bytes, pinned, cb_bytes, (sdb_stream_t)ss.main, &B.cb));
     replay(B, ss.main);
     return Bp.release();
 }
@@ -2597,6 +2581,8 @@ int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
     info->host_bytes = b->host_bytes;
     info->last_run_ms = b->last_ms;
     info->last_chain_ms = b->last_chain_ms;
+    info->last_pre_ms = b->last_pre_ms;
+    info->last_post_ms = b->last_post_ms;
     return SDB_OK;
 }
 

@@ -105,7 +105,7 @@ struct Request {
     Clock::time_point arrival;
     bool sized = false;
     sdb::BatchSize size;
-    uint64_t dev_need = 0;  // arena + zeroed region, this plan alone
+    uint64_t dev_need = 0;  // arena + zeroed region + result region, this plan alone
 };
 
 struct Done {
@@ -188,7 +188,8 @@ struct sdb_server {
     {
         try {
             r.size = sdb::batch_size(eng, {r.plan});
-            r.dev_need = RegionPool::round(r.size.arena) + RegionPool::round(r.size.zero);
+            r.dev_need = RegionPool::round(r.size.arena) + RegionPool::round(r.size.zero) +
+                         RegionPool::round(r.size.staging);
             r.sized = true;
             return true;
         } catch (const sdb::Error &x) {
@@ -238,7 +239,8 @@ struct sdb_server {
                 plans.push_back(waiting[i].plan);
             }
             const uint64_t cb = sdb::batch_chain_bytes(z.chains);
-            const uint64_t dev_bytes = RegionPool::round(z.arena) + RegionPool::round(z.zero) + RegionPool::round(cb);
+            const uint64_t dev_bytes = RegionPool::round(z.arena) + RegionPool::round(z.zero) +
+                                       RegionPool::round(z.staging) + RegionPool::round(cb);
             const uint64_t pin_bytes = RegionPool::round(cb) + RegionPool::round(z.staging);
             uint64_t doff = 0, poff = 0;
             if (!dev_pool.alloc(dev_bytes, doff)) continue;
