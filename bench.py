@@ -522,8 +522,18 @@ def run_batched(args, rank, world, local, pg, stream, peak):
         chain_ms.append(st["last_chain_ms"])
         pre_ms.append(st["last_pre_ms"])
         post_ms.append(st["last_post_ms"])
-    batch_s = max_over_ranks(pg, time.perf_counter() - t0)
+    batch_s = max_over_ranks(pg, sum(lat_b))
     clk = clocks.stop()
+    # the same runs without the Python conversion of the results, and without
+    # unpacking at all: where the host time of a run goes
+    lat_native, lat_bare = [], []
+    for _ in range(max(3, args.batched_runs // 2)):
+        t = time.perf_counter()
+        b.run_native()
+        lat_native.append(time.perf_counter() - t)
+        t = time.perf_counter()
+        b.run(unpack=False)
+        lat_bare.append(time.perf_counter() - t)
     st = b.stats()
     b.close()
     eng.close()
@@ -545,6 +555,8 @@ def run_batched(args, rank, world, local, pg, stream, peak):
         "latency_ms": {
             "batched_p50": _pct(lat_b, 50) * 1e3, "batched_p99": _pct(lat_b, 99) * 1e3,
             "plain_p50": _pct(lat_plain, 50) * 1e3, "plain_p99": _pct(lat_plain, 99) * 1e3,
+            "batched_p50_native_results": _pct(lat_native, 50) * 1e3,
+            "batched_p50_no_unpack": _pct(lat_bare, 50) * 1e3,
             "note": "batched: every plan of a batch completes when the batch run returns (host wall clock "
                     "around sdb_batch_run incl. result unpacking); plain: each sdb_engine_execute alone"},
         "device_ms_per_batch": statistics.median(dev_ms),

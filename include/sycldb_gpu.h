@@ -498,6 +498,17 @@ int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int
 int sdb_batch_run(sdb_batch *batch, sdb_result **results);
 int sdb_batch_info(const sdb_batch *batch, sdb_batch_stats *info);
 void sdb_batch_free(sdb_batch *batch);
+/* Results without unpacking (for bindings that build their own arrays): after
+ * sdb_batch_run (results may be NULL), the batch's pinned result mirror
+ * (sdb_batch_host, `bytes` long, valid until the next run) holds for each
+ * plan and segment a uint32 row count at count_off and each result column
+ * (capacity rows; the first `count` are the result, in row order) at
+ * col_offs[c]; sdb_batch_layout gives a plan's column count and types (0 int32,
+ * 1 uint64) and segments. */
+int sdb_batch_layout(const sdb_batch *batch, int plan, int *ncols, int *types, int types_cap, int *nsegs);
+int sdb_batch_segment(const sdb_batch *batch, int plan, int seg, uint64_t *count_off, uint64_t *col_offs, int cap,
+                      uint64_t *capacity);
+const void *sdb_batch_host(const sdb_batch *batch, size_t *bytes);
 
 /* ----------------------------------------------------------------- server
  * Continuous batching of arriving plans over the engine's loaded tables.  No

@@ -151,6 +151,10 @@ _SIGS = {
     "sdb_batch_run": (c_int, [c_void_p, POINTER(c_void_p)]),
     "sdb_batch_info": (c_int, [c_void_p, POINTER(BatchStats)]),
     "sdb_batch_free": (None, [c_void_p]),
+    "sdb_batch_layout": (c_int, [c_void_p, c_int, POINTER(c_int), POINTER(c_int), c_int, POINTER(c_int)]),
+    "sdb_batch_segment": (c_int, [c_void_p, c_int, c_int, POINTER(c_uint64), POINTER(c_uint64), c_int,
+                                  POINTER(c_uint64)]),
+    "sdb_batch_host": (c_void_p, [c_void_p, POINTER(c_size_t)]),
     "sdb_server_create": (c_int, [c_void_p, POINTER(ServerConfig), POINTER(c_void_p)]),
     "sdb_server_submit": (c_int, [c_void_p, c_char_p, POINTER(c_int64)]),
     "sdb_server_next": (c_int, [c_void_p, c_int, POINTER(c_int64), POINTER(c_int), POINTER(c_void_p),

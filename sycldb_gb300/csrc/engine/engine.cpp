@@ -2586,6 +2586,37 @@ int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
     return SDB_OK;
 }
 
+int sdb_batch_layout(const sdb_batch *b, int plan, int *ncols, int *types, int types_cap, int *nsegs)
+{
+    if (!b || plan < 0 || (size_t)plan >= b->pend.size() || !ncols || !nsegs)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_batch_layout: bad argument");
+    const auto &pr = b->pend[plan];
+    *ncols = (int)pr.types.size();
+    *nsegs = (int)pr.segs.size();
+    for (int c = 0; c < *ncols && c < types_cap && types; c++) types[c] = pr.types[c];
+    return SDB_OK;
+}
+
+int sdb_batch_segment(const sdb_batch *b, int plan, int seg, uint64_t *count_off, uint64_t *col_offs, int cap,
+                      uint64_t *capacity)
+{
+    if (!b || plan < 0 || (size_t)plan >= b->pend.size() || seg < 0 || (size_t)seg >= b->pend[plan].segs.size() ||
+        !count_off || !capacity)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_batch_segment: bad argument");
+    const auto &st = b->stage[plan][seg];
+    *count_off = st.count_off;
+    *capacity = b->pend[plan].segs[seg].cap;
+    for (size_t c = 0; c < st.col_off.size() && (int)c < cap && col_offs; c++) col_offs[c] = st.col_off[c];
+    return SDB_OK;
+}
+
+const void *sdb_batch_host(const sdb_batch *b, size_t *bytes)
+{
+    if (!b) return nullptr;
+    if (bytes) *bytes = b->rbytes;
+    return b->host;
+}
+
 void sdb_batch_free(sdb_batch *b) { delete b; }
 
 }  // extern "C"

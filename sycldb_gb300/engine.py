@@ -219,15 +219,59 @@ class Batch:
         self._h = h
         self._engine = engine  # the batch reads the engine's tables
         self.n_plans = len(texts)
+        # where each plan's rows land in the pinned result mirror
+        size = ctypes.c_size_t()
+        ptr = L.sdb_batch_host(h, ctypes.byref(size))
+        self._mirror = (np.frombuffer((ctypes.c_char * size.value).from_address(ptr), dtype=np.uint8)
+                        if size.value else np.empty(0, np.uint8))
+        self._layout = []
+        for p in range(self.n_plans):
+            nc, ns = ctypes.c_int(), ctypes.c_int()
+            types = (ctypes.c_int * 64)()
+            capi.check(L.sdb_batch_layout(h, p, ctypes.byref(nc), types, 64, ctypes.byref(ns)))
+            dts = [np.uint64 if types[c] == 1 else np.int32 for c in range(nc.value)]
+            segs = []
+            for sg in range(ns.value):
+                co, cap = ctypes.c_uint64(), ctypes.c_uint64()
+                offs = (ctypes.c_uint64 * max(nc.value, 1))()
+                capi.check(L.sdb_batch_segment(h, p, sg, ctypes.byref(co), offs, nc.value, ctypes.byref(cap)))
+                segs.append((co.value, [offs[c] for c in range(nc.value)]))
+            self._layout.append((dts, segs))
 
     def run(self, unpack: bool = True) -> Optional[List[Result]]:
+        """Runs the batch once; returns one Result per plan (numpy copies of
+        the rows in the pinned result mirror) unless ``unpack`` is False."""
         L = capi.lib()
+        capi.check(L.sdb_batch_run(self._h, None))
         if not unpack:
-            capi.check(L.sdb_batch_run(self._h, None))
             return None
+        m = self._mirror
+        out = []
+        for dts, segs in self._layout:
+            parts = [[] for _ in dts]
+            for co, offs in segs:
+                cnt = int(m[co:co + 4].view(np.uint32)[0])
+                for c, dt in enumerate(dts):
+                    w = np.dtype(dt).itemsize
+                    parts[c].append(m[offs[c]:offs[c] + cnt * w].view(dt))
+            out.append(Result([np.concatenate(pc) if len(pc) > 1 else (pc[0].copy() if pc else np.empty(0, dt))
+                               for pc, dt in zip(parts, dts)]))
+        return out
+
+    def run_native(self) -> List[int]:
+        """Runs the batch with the results unpacked into native result
+        objects, as a C caller receives them, and returns each plan's row
+        count (the objects are freed; no numpy conversion)."""
+        L = capi.lib()
         out = (ctypes.c_void_p * self.n_plans)()
         capi.check(L.sdb_batch_run(self._h, out))
-        return [_take_result(ctypes.c_void_p(out[i])) for i in range(self.n_plans)]
+        rows = []
+        for i in range(self.n_plans):
+            nc, nr = ctypes.c_int(), ctypes.c_uint64()
+            L.sdb_result_shape(out[i], ctypes.byref(nc), ctypes.byref(nr))
+            rows.append(nr.value)
+            L.sdb_result_free(out[i])
+        return rows
 
     def stats(self) -> dict:
         st = capi.BatchStats()
