@@ -2126,7 +2126,7 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
 
     // streams and events; the plans' work is spread over up to 8 streams
     SDB_CUDA(cudaStreamCreateWithFlags(&B.bs, cudaStreamNonBlocking));
-    const size_t K = std::min<size_t>(std::max<size_t>(plans.size(), 1), 8);
+    const size_t K = std::min<size_t>(std::max<size_t>(plans.size(), 1), 16);
     for (size_t i = 0; i < K; i++) {
         cudaStream_t s;
         SDB_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
