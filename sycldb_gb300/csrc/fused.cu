@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <atomic>
+#include <mutex>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -384,12 +385,12 @@ __global__ void __launch_bounds__(kThreads, min_blocks_of(ITEMS)) k_chain(const 
 
 int num_sms()
 {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
+    static const int sms = [] {  // initialised once, thread-safe
+        int dev = 0, n = 0;
         cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = sdb::kSMs;
-    }
+        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = sdb::kSMs;
+        return n;
+    }();
     return sms;
 }
 
@@ -1184,11 +1185,11 @@ int launch_stages(const Launch &L, cudaStream_t s)
     auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
     const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
-    static bool attr = false;
-    if (!attr) {
+    static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
-        attr = true;
-    }
+        return true;
+    }();
+    (void)attr;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
@@ -1395,11 +1396,11 @@ int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, ui
     auto kern = k_batch<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
     const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
     const int smem = ring + (int)(bitmap_words * 4);
-    static int attr_set = 0;
-    if (!attr_set) {
+    static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
-        attr_set = 1;
-    }
+        return true;
+    }();
+    (void)attr;
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
@@ -1439,12 +1440,14 @@ struct BatchLauncher {
 // tells the shapes of one terminal apart (a star join starts with a semi
 // join, a date join with a range filter).
 constexpr int kOpClasses = 8;  // SDB_OP_* kinds 0..6, 7 = no op
-int g_tune[3][3][kOpClasses][40];
-bool g_tune_init = false;
+// entries are read and written from any thread (the request server launches
+// from its own): relaxed atomics, all -1 until set
+std::atomic<int> g_tune[3][3][kOpClasses][40];
+std::atomic<bool> g_tune_init{false};
 
 int op_class(const sdb_chain_desc &d) { return d.n_ops > 0 && d.ops[0].kind >= 0 && d.ops[0].kind < 7 ? d.ops[0].kind : 7; }
 
-int &tune_entry(int term, int nregs, int opc, uint64_t rows);
+std::atomic<int> &tune_entry(int term, int nregs, int opc, uint64_t rows);
 
 int reg_class(int nregs) { return nregs <= 2 ? 0 : (nregs <= 4 ? 1 : 2); }
 int rows_bucket(uint64_t n)
@@ -1454,12 +1457,16 @@ int rows_bucket(uint64_t n)
     return b;
 }
 
-int &tune_entry(int term, int nregs, int opc, uint64_t rows)
+std::atomic<int> &tune_entry(int term, int nregs, int opc, uint64_t rows)
 {
-    if (!g_tune_init) {
-        memset(g_tune, 0xff, sizeof g_tune);
-        g_tune_init = true;
-    }
+    static std::once_flag once;
+    std::call_once(once, [] {
+        for (auto &a : g_tune)
+            for (auto &b : a)
+                for (auto &c : b)
+                    for (auto &e : c) e.store(-1, std::memory_order_relaxed);
+        g_tune_init.store(true);
+    });
     return g_tune[term][reg_class(nregs)][opc][rows_bucket(rows)];
 }
 
@@ -1697,7 +1704,7 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
     std::vector<BatchPlan::G> groups;
     std::vector<const Family *> of;
     for (const Family &F : fams) {
-        int variant = g_tune_init ? tune_entry(F.term, F.nregs, F.opc, F.rows) : -1;
+        int variant = g_tune_init ? tune_entry(F.term, F.nregs, F.opc, F.rows).load(std::memory_order_relaxed) : -1;
         if (variant < 0) variant = kCompact2Variant;
         if (variant < kDenseVariant) {  // the general pass: chain by chain
             for (const Item &it : F.items) bp.singles.push_back(chains[it.index]);

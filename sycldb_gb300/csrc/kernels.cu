@@ -762,11 +762,11 @@ int sdb_groupby_sum(const int32_t *const *keys, const int32_t *mins, const int32
     cudaStream_t s = (cudaStream_t)stream;
     const size_t smem = (size_t)P * (sizeof(uint64_t) + sizeof(uint32_t));
     if (P <= 8192) {
-        static bool attr_set = false;
-        if (!attr_set) {
+        static const bool attr_set = [] {  // once, thread-safe
             cudaFuncSetAttribute(k_groupby<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 12);
-            attr_set = true;
-        }
+            return true;
+        }();
+        (void)attr_set;
         k_groupby<true><<<sdb::grid_for(n, kThreads, 2), kThreads, smem, s>>>(a);
     } else {
         k_groupby<false><<<sdb::grid_for(n, kThreads, 8), kThreads, 0, s>>>(a);
