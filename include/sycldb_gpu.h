@@ -201,6 +201,14 @@ int sdb_count_flags(const uint8_t *flags, uint64_t n, uint64_t *out, sdb_stream_
  * (models/models.hpp:71-77). */
 int sdb_min_max_i32(const int32_t *col, uint64_t n, int32_t *minmax, sdb_stream_t stream);
 
+/* The flagged rows of a small segment (n <= 65536, e.g. a group-by result)
+ * gathered from up to 8 columns in row order, in one launch: what
+ * sdb_compact_row_ids and one sdb_gather_* per column give together
+ * (dst[c][0..*count) = src[c][rows with flags != 0]).  src/dst/wide are HOST
+ * arrays of ncols entries; wide[c] = 1 for a uint64 column, 0 for int32. */
+int sdb_compact_gather(const uint8_t *flags, uint64_t n, int ncols, const void *const *src, const int *wide,
+                       void *const *dst, uint32_t *count, sdb_stream_t stream);
+
 /* ORDER BY: perm[0..n) = the row ids 0..n-1 ordered by keys[0], then keys[1],
  * ... (nkeys <= 16; key_types[k] 0 = int32 compared signed, 1 = uint64
  * compared unsigned, the comparisons of the reference's sort_table,

@@ -1760,6 +1760,34 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
         PendingSeg o;
         o.cap = cnt;
         MemoryManager &R = E.rmm ? *E.rmm : E.mm;
+        const uint8_t *fl0 = fin.flags + sg[s].first;
+        if (cnt <= 65536 && cols.size() <= 8) {  // small result: compaction and gathers in one launch
+            uint32_t *count = R.alloc<uint32_t>(1);
+            o.count = count;
+            std::vector<const void *> src;
+            std::vector<void *> dst;
+            std::vector<int> wide;
+            for (Column *c : cols) {
+                const Segment &seg = c->segments[s];
+                if (c->is_aggregate_result) {
+                    src.push_back(seg.agg);
+                    dst.push_back(R.alloc<uint64_t>(cnt));
+                    wide.push_back(1);
+                } else {
+                    src.push_back(seg.data);
+                    dst.push_back(R.alloc<int32_t>(cnt));
+                    wide.push_back(0);
+                }
+            }
+            o.dev = dst;
+            E.ensure_filled(fl0);
+            E.dev("compact_gather", [fl0, cnt, src, wide, dst, count](cudaStream_t st) {
+                return sdb_compact_gather(fl0, cnt, (int)src.size(), src.data(), wide.data(), dst.data(), count,
+                                          (sdb_stream_t)st);
+            });
+            pr.segs.push_back(o);
+            continue;
+        }
         int32_t *ids = E.mm.alloc<int32_t>(cnt);
         uint32_t *count = R.alloc<uint32_t>(1);
         o.count = count;

@@ -576,6 +576,62 @@ __global__ void __launch_bounds__(kThreads) k_gather(const T *src, const int32_t
     for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < c; i += stride) dst[i] = src[ids[i]];
 }
 
+// Ordered compaction and the gathers of every result column of a small
+// segment (a group-by result) in one block of 1024 threads: thread t owns
+// rows [t*per, (t+1)*per), counts its flagged rows, a block scan gives its
+// first output position, then it copies its rows' values in row order.
+constexpr uint32_t kSmallCompactMax = 65536;
+constexpr int kSmallCompactCols = 8;
+struct SmallCompact {
+    const uint8_t *flags;
+    uint32_t n;
+    int32_t ncols;
+    const void *src[kSmallCompactCols];
+    void *dst[kSmallCompactCols];
+    int32_t wide[kSmallCompactCols];  // 1: uint64 column
+    uint32_t *count;
+};
+
+__global__ void __launch_bounds__(1024) k_compact_gather_small(const __grid_constant__ SmallCompact a)
+{
+    __shared__ uint32_t s_warp[32];
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const uint32_t per = (a.n + 1023u) / 1024u;
+    const uint32_t b = min(threadIdx.x * per, a.n), e = min(b + per, a.n);
+    uint32_t cnt = 0;
+    for (uint32_t i = b; i < e; i++) cnt += a.flags[i] != 0;
+    uint32_t x = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= (uint32_t)o) x += y;
+    }
+    if (lane == 31) s_warp[warp] = x;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = s_warp[lane];
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += y;
+        }
+        s_warp[lane] = w;
+    }
+    __syncthreads();
+    uint32_t pos = x - cnt + (warp ? s_warp[warp - 1] : 0);
+    if (threadIdx.x == 1023) *a.count = pos + cnt;
+    for (uint32_t i = b; i < e; i++) {
+        if (!a.flags[i]) continue;
+        for (int c = 0; c < a.ncols; c++) {
+            if (a.wide[c])
+                static_cast<uint64_t *>(a.dst[c])[pos] = static_cast<const uint64_t *>(a.src[c])[i];
+            else
+                static_cast<int32_t *>(a.dst[c])[pos] = static_cast<const int32_t *>(a.src[c])[i];
+        }
+        pos++;
+    }
+}
+
 // ---------------------------------------------------------------- data gen
 __global__ void __launch_bounds__(kThreads) k_gen_uniform(int32_t *dst, uint64_t n, uint64_t row0, uint64_t key,
                                                           int32_t lo, int32_t hi)
@@ -903,6 +959,32 @@ int sdb_compact_row_ids_noalloc(const uint8_t *flags, uint64_t n, int32_t *ids, 
     // Every count the passes read is written first by k_compact_count, so the
     // array needs no clearing between calls.
     return sdb_compact_row_ids(flags, n, ids, count, scratch, sizeof(g_noalloc_compact_scratch), stream);
+}
+
+int sdb_compact_gather(const uint8_t *flags, uint64_t n, int ncols, const void *const *src, const int *wide,
+                       void *const *dst, uint32_t *count, sdb_stream_t stream)
+{
+    if (n > kSmallCompactMax) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: n=%llu exceeds %u",
+                                                   (unsigned long long)n, kSmallCompactMax);
+    if (ncols < 0 || ncols > kSmallCompactCols || (ncols && (!src || !wide || !dst)))
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: 0..%d columns", kSmallCompactCols);
+    if (!count || (n && !flags)) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: NULL flags or count");
+    if (!sdb::aligned(count, 4)) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: count misaligned");
+    SmallCompact a;
+    a.flags = flags;
+    a.n = (uint32_t)n;
+    a.ncols = ncols;
+    a.count = count;
+    for (int c = 0; c < ncols; c++) {
+        const size_t w = wide[c] ? 8 : 4;
+        if (!src[c] || !dst[c] || !sdb::aligned(src[c], w) || !sdb::aligned(dst[c], w))
+            return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: column %d NULL or misaligned", c);
+        a.src[c] = src[c];
+        a.dst[c] = dst[c];
+        a.wide[c] = wide[c] ? 1 : 0;
+    }
+    k_compact_gather_small<<<1, 1024, 0, (cudaStream_t)stream>>>(a);
+    return sdb_check_launch("sdb_compact_gather");
 }
 
 int sdb_gather_i32(const int32_t *src, const int32_t *ids, const uint32_t *count, int32_t *dst, uint64_t cap,

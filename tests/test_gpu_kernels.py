@@ -235,3 +235,28 @@ def test_min_max_and_generator_agree_with_host():
         mb, mm = zeros(2, np.int32)
         capi.check(L.sdb_min_max_i32(dev_cols[c].data_ptr(), n, mm, stream()))
         assert host(mb, mm, 2, np.int32).tolist() == list(O.min_max(host_cols[c]))
+
+
+@pytest.mark.parametrize("n", [0, 1, 1023, 1024, 1025, 7000, 65536])
+def test_compact_gather_equals_compaction_then_gathers(n):
+    """sdb_compact_gather = sdb_compact_row_ids + one gather per column."""
+    rng = np.random.default_rng(n + 5)
+    fl = kc.flags(rng, max(n, 1), 0.3, canonical=False)[:n]
+    a = rng.integers(-2**31, 2**31 - 1, max(n, 1), dtype=np.int64).astype(np.int32)[:n]
+    u = rng.integers(0, 2**63, max(n, 1), dtype=np.uint64)[:n]
+    b = rng.integers(-5, 5, max(n, 1)).astype(np.int32)[:n]
+    lib = L()
+    _, f = dev(fl if n else np.zeros(1, np.uint8))
+    srcs = [dev(x if n else np.zeros(1, x.dtype))[1] for x in (a, u, b)]
+    outs = [zeros(max(n, 1), x.dtype) for x in (a, u, b)]
+    cb, cnt = zeros(1, np.uint32)
+    src = (ctypes.c_void_p * 3)(*srcs)
+    dst = (ctypes.c_void_p * 3)(*[o[1] for o in outs])
+    wide = (ctypes.c_int * 3)(0, 1, 0)
+    capi.check(lib.sdb_compact_gather(f, n, 3, src, wide, dst, cnt, stream()))
+    c = int(host(cb, cnt, 1, np.uint32)[0])
+    sel = np.nonzero(fl)[0]
+    assert c == sel.size
+    for (buf, ptr), x in zip(outs, (a, u, b)):
+        assert np.array_equal(host(buf, ptr, c, x.dtype), x[sel])
+    assert lib.sdb_compact_gather(f, 65537, 3, src, wide, dst, cnt, stream()) == capi.SDB_ERR_INVALID
