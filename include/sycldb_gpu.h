@@ -308,8 +308,11 @@ int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream);
  * shared memory, more resident blocks).  6: as 5, and a warp's surviving rows
  * that do not fill a last group of 32 are carried (their column values) into
  * the next tile, so the one-row-per-lane ops run on full warps (chains whose
- * later ops write no column).  Shapes without a specialised pass fall back to
- * the general pass.  Default (and an unset tuning entry): 5. */
+ * later ops write no column).  7: as 6, and the rows that survive the first
+ * op after the compaction are compacted again, across lanes in registers,
+ * so the later ops and the terminal run on full warps.  Shapes without a
+ * specialised pass fall back to the general pass.  Default (and an unset
+ * tuning entry): 5. */
 int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream);
 /* Tuning table used by sdb_fused_chain: variant for chains with this
  * terminal (sdb_chain_terminal), register count and row count (bucketed by

@@ -1,6 +1,6 @@
 """Autotuner for the fused fact-side pass.
 
-The fused chain has six kernel variants (``sdb_fused_chain_variant``):
+The fused chain has eight kernel variants (``sdb_fused_chain_variant``):
 
   0/1/2  general interpreter, 4 / 8 / 16 rows per thread (items per thread)
   3      shape-specialised pass, every row through every op
@@ -8,6 +8,8 @@ The fused chain has six kernel variants (``sdb_fused_chain_variant``):
          3-stage cp.async copy ring (3 blocks of 256 threads per SM)
   5      as 4 with a 2-stage ring (5 blocks per SM)
   6      as 5, surviving rows that do not fill a warp carried into the next tile
+  7      as 6, and the rows that survive the first row-per-lane op compacted
+         again (across lanes, in registers) so the later ops run on full warps
 
 Block size is 256 threads throughout; the group-by tables are direct-address
 (the reference's HASH is the identity on its range), so there is no load
@@ -36,7 +38,7 @@ from . import capi, plans, ssb
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_TABLE = os.path.join(HERE, "tuning", "gb300.json")
-VARIANTS = (0, 1, 2, 3, 4, 5, 6)
+VARIANTS = (0, 1, 2, 3, 4, 5, 6, 7)
 TERMINALS = {"flags": 0, "sum": 1, "groupby": 2}
 
 OP_SEARCH_RANGE, OP_SEMI_PROBE = 1, 3  # SDB_OP_* kinds of a chain's first op

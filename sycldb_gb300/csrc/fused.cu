@@ -871,9 +871,98 @@ __device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint3
 // registers (`ce`) -- and runs them with the next tile's survivors, so the
 // row-per-lane phase runs full warps.  drain runs what is left (at the end of
 // a block's rows of a chain).
+// Second compaction level (CARRY 2): the rows that survive the first
+// row-per-lane op are moved, by warp shuffles, into a warp-wide group held in
+// registers (lane j: pending row j) and the remaining ops run only on full
+// groups of 32 -- for a star join, where ~4 % of the rows survive the part
+// probe, the date probe and the group-by then run on full warps.
+template <int NREGS>
+struct Level2 {
+    VRow<NREGS> r;   // lane j: pending row j
+    uint32_t n = 0;  // pending rows (warp-uniform)
+};
+
+// Row k (0-based, k < cnt) among the warp's live rows; every lane calls it
+// with its own k (k >= cnt: no row).
+template <int NREGS>
+__device__ __forceinline__ VRow<NREGS> take_row(const VRow<NREGS> &R, unsigned live, uint32_t k, uint32_t cnt)
+{
+    const int src = k < cnt ? (int)__fns(live, 0, (int)k + 1) : 0;
+    VRow<NREGS> o;
+    o.v0 = __shfl_sync(0xffffffffu, R.v0, src);
+    o.v1 = __shfl_sync(0xffffffffu, R.v1, src);
+    o.v2 = __shfl_sync(0xffffffffu, R.v2, src);
+    o.v3 = __shfl_sync(0xffffffffu, R.v3, src);
+#pragma unroll
+    for (int i = 0; i < NREGS; i++) o.reg[i] = __shfl_sync(0xffffffffu, R.reg[i], src);
+    o.live = k < cnt;
+    return o;
+}
+
 template <int TERM, int NREGS, int SPLIT, int... KS>
-__device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, const int4 &ce, const uint32_t *s_bits,
-                                            uint32_t *s_key, unsigned long long *s_sum, bool direct, uint64_t &acc)
+__device__ __forceinline__ void level2_run(const Launch &L, VRow<NREGS> &F, const uint32_t *s_bits, uint32_t *s_key,
+                                           unsigned long long *s_sum, bool direct, uint64_t &acc)
+{
+    constexpr int N = sizeof...(KS);
+    run_steps1<NREGS, SPLIT + 1, KS...>(L, F, s_bits, std::make_integer_sequence<int, N - SPLIT - 1>{});
+    finish_row<TERM>(L, F, s_key, s_sum, direct, acc);
+}
+
+// After the first row-per-lane op of a group: appends its live rows to the
+// level-2 rows and runs the remaining ops whenever 32 are pending.
+template <int TERM, int NREGS, int SPLIT, int... KS>
+__device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &R, Level2<NREGS> &Q,
+                                            const uint32_t *s_bits, uint32_t *s_key, unsigned long long *s_sum,
+                                            bool direct, uint64_t &acc)
+{
+    const uint32_t lane = threadIdx.x & 31u;
+    const unsigned live = __ballot_sync(0xffffffffu, R.live);
+    const uint32_t cnt = __popc(live);
+    if (cnt == 0) return;
+    const uint32_t n2 = Q.n;
+    {
+        const uint32_t k = lane >= n2 ? lane - n2 : 32u;
+        const VRow<NREGS> got = take_row(R, live, k, cnt);
+        if (lane >= n2 && k < cnt) Q.r = got;
+    }
+    if (n2 + cnt >= 32) {
+        VRow<NREGS> F = Q.r;
+        F.live = true;
+        level2_run<TERM, NREGS, SPLIT, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
+        const uint32_t used = 32 - n2;
+        const VRow<NREGS> got = take_row(R, live, lane + used, cnt);
+        if (lane < cnt - used) Q.r = got;
+        Q.n = cnt - used;
+    } else {
+        Q.n = n2 + cnt;
+    }
+}
+
+// Whether CARRY 2 uses the second level: there are ops after the first
+// row-per-lane op.
+template <int SPLIT, int... KS>
+__host__ __device__ constexpr bool use_level2(int carry)
+{
+    return carry == 2 && SPLIT + 1 < (int)sizeof...(KS);
+}
+
+// The first row-per-lane op and then the second level, for one group.
+template <int TERM, int NREGS, int SPLIT, int... KS>
+__device__ __forceinline__ void level2_group(const Launch &L, VRow<NREGS> &R, Level2<NREGS> &Q, const uint32_t *s_bits,
+                                             uint32_t *s_key, unsigned long long *s_sum, bool direct, uint64_t &acc)
+{
+    constexpr int kinds[] = {KS...};
+#pragma unroll
+    for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
+    step1<kinds[SPLIT]>(L.ops[SPLIT], R, s_bits);
+    level2_push<TERM, NREGS, SPLIT, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+}
+
+// Runs whatever the warp still holds (at the end of a block's rows of a chain).
+template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
+__device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, const int4 &ce, Level2<NREGS> &Q,
+                                            const uint32_t *s_bits, uint32_t *s_key, unsigned long long *s_sum,
+                                            bool direct, uint64_t &acc)
 {
     const uint32_t lane = threadIdx.x & 31u;
     if (carry) {
@@ -884,17 +973,28 @@ __device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, co
         R.v2 = e.z;
         R.v3 = e.w;
         R.live = lane < carry;
-        sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+        if constexpr (use_level2<SPLIT, KS...>(CARRY))
+            level2_group<TERM, NREGS, SPLIT, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+        else
+            sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
     }
     carry = 0;
+    if constexpr (use_level2<SPLIT, KS...>(CARRY)) {
+        if (Q.n) {
+            VRow<NREGS> F = Q.r;
+            F.live = lane < Q.n;
+            level2_run<TERM, NREGS, SPLIT, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
+        }
+        Q.n = 0;
+    }
     __syncwarp();
 }
 
-template <int TERM, int NREGS, int SPLIT, bool CARRY, int... KS>
+template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, const int4 *s_buf, int st, uint64_t tile,
                                           uint8_t *s_list, uint32_t *s_key, unsigned long long *s_sum,
                                           const uint32_t *s_bits, bool direct, uint64_t &acc, uint32_t &carry,
-                                          int4 &ce)
+                                          int4 &ce, Level2<NREGS> &Q)
 {
     constexpr int N = sizeof...(KS);
     constexpr bool kCompact = SPLIT <= N;
@@ -937,7 +1037,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
         __syncwarp();
         const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
-        if constexpr (CARRY) {
+        if constexpr (CARRY > 0) {
             // entries 0 .. carry-1 are the carried rows (entry j in lane j),
             // then this tile's survivors
             const uint32_t avail = carry + total;
@@ -961,7 +1061,10 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             uint32_t b = 0;
             for (; b + 32 <= avail; b += 32) {
                 VRow<NREGS> R = entry(b + lane);
-                sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+                if constexpr (use_level2<SPLIT, KS...>(CARRY))
+                    level2_group<TERM, NREGS, SPLIT, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+                else
+                    sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
             const uint32_t rem = avail - b;
             if (lane < rem && b + lane >= carry) {  // carry a survivor of this tile
@@ -1049,7 +1152,7 @@ __device__ __forceinline__ void block_flush(const Launch &L, uint32_t *s_key, un
     }
 }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(const __grid_constant__ Launch L)
 {
     constexpr int kStages = STAGES;
@@ -1061,6 +1164,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
     __shared__ uint64_t s_part[kThreads / 32];
     uint32_t carry = 0;  // rows the warp carries (warp-uniform)
     int4 ce = make_int4(0, 0, 0, 0);
+    Level2<NREGS> Q;
     const bool direct = L.P <= kDenseCap;
     uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
     group_table_reset<TERM>(s_key, s_sum);
@@ -1085,11 +1189,12 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
         issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, (st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
         tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
-                                                   carry, ce);
+                                                   carry, ce, Q);
         st = (st + 1) % kStages;
     }
     cp_async_wait<0>();
-    if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(L, carry, ce, s_bits, s_key, s_sum, direct, acc);
+    if constexpr (CARRY > 0)
+        drain_carry<TERM, NREGS, SPLIT, CARRY, KS...>(L, carry, ce, Q, s_bits, s_key, s_sum, direct, acc);
     block_flush<TERM>(L, s_key, s_sum, s_part, acc);
 }
 
@@ -1107,13 +1212,14 @@ struct Span {
 // new descriptor, resets its group table and re-stages the semi-join bitmap.
 // Within a span the tiles go through the same cp.async ring as the
 // single-chain pass.
-template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
     k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
             uint32_t *__restrict__ head)
 {
     uint32_t carry = 0;
     int4 ce = make_int4(0, 0, 0, 0);
+    Level2<NREGS> Q;
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
@@ -1169,17 +1275,18 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
             else cp_async_commit();
             cp_async_wait<kStages - 1>();
             tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum,
-                                                       s_bits, direct, acc, carry, ce);
+                                                       s_bits, direct, acc, carry, ce, Q);
             st = (st + 1) % kStages;
         }
         cp_async_wait<0>();
         // parked rows belong to this span's chain: run them before the next pull
-        if constexpr (CARRY) drain_carry<TERM, NREGS, SPLIT, KS...>(s_L, carry, ce, s_bits, s_key, s_sum, direct, acc);
+        if constexpr (CARRY > 0)
+            drain_carry<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, carry, ce, Q, s_bits, s_key, s_sum, direct, acc);
     }
     if (cur != ~0u) block_flush<TERM>(s_L, s_key, s_sum, s_part, acc);
 }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 int launch_stages(const Launch &L, cudaStream_t s)
 {
     auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
@@ -1202,15 +1309,16 @@ int launch_stages(const Launch &L, cudaStream_t s)
     return sdb_check_launch("sdb_fused_chain (dense)");
 }
 
-// Ring stages 3 or 2; rows carried between tiles only with compaction and a
-// 2-stage ring.
+// Ring stages 3 or 2; rows carried between tiles (carry 1; 2: and the second
+// compaction level) only with compaction and a 2-stage ring.
 template <int TERM, int NREGS, int SPLIT, int... KS>
-int launch(const Launch &L, int stages, bool carry, cudaStream_t s)
+int launch(const Launch &L, int stages, int carry, cudaStream_t s)
 {
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
-    if (stages >= 3) return launch_stages<TERM, NREGS, 3, SPLIT, false, KS...>(L, s);
-    if (kCompact && carry) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact, KS...>(L, s);
-    return launch_stages<TERM, NREGS, 2, SPLIT, false, KS...>(L, s);
+    if (stages >= 3) return launch_stages<TERM, NREGS, 3, SPLIT, 0, KS...>(L, s);
+    if (kCompact && carry == 2) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(L, s);
+    if (kCompact && carry == 1) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(L, s);
+    return launch_stages<TERM, NREGS, 2, SPLIT, 0, KS...>(L, s);
 }
 
 // Converts a checked chain into a dense launch.  Returns false when the chain
@@ -1371,7 +1479,7 @@ struct ShapeProbe {
 struct SingleLauncher {
     const Launch &D;
     int stages;
-    bool carry;
+    int carry;
     cudaStream_t s;
     template <int TERM, int NREGS, int SPLIT, int... KS>
     int run()
@@ -1380,16 +1488,16 @@ struct SingleLauncher {
     }
 };
 
-int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, bool carry, cudaStream_t s)
+int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages, int carry, cudaStream_t s)
 {
     Launch D;
     if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
-    SingleLauncher f{D, stages, carry && can_carry(D, term), s};
+    SingleLauncher f{D, stages, can_carry(D, term) ? carry : 0, s};
     return with_shape(D, term, compact, f);
 }
 
 // One launch of k_batch over the chains of one shape group.
-template <int TERM, int NREGS, int STAGES, int SPLIT, bool CARRY, int... KS>
+template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, uint32_t *head, uint32_t bitmap_words,
                  cudaStream_t s)
 {
@@ -1418,17 +1526,21 @@ struct BatchLauncher {
     uint32_t *head;
     uint32_t bitmap_words;
     int stages;
-    bool carry;
+    int carry;
     cudaStream_t s;
     template <int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
         constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
         if (stages >= 3)
-            return batch_stages<TERM, NREGS, 3, SPLIT, false, KS...>(launches, spans, n_spans, head, bitmap_words, s);
-        if (kCompact && carry)
-            return batch_stages<TERM, NREGS, 2, SPLIT, kCompact, KS...>(launches, spans, n_spans, head, bitmap_words, s);
-        return batch_stages<TERM, NREGS, 2, SPLIT, false, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+            return batch_stages<TERM, NREGS, 3, SPLIT, 0, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+        if (kCompact && carry == 2)
+            return batch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(launches, spans, n_spans, head,
+                                                                              bitmap_words, s);
+        if (kCompact && carry == 1)
+            return batch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(launches, spans, n_spans, head,
+                                                                              bitmap_words, s);
+        return batch_stages<TERM, NREGS, 2, SPLIT, 0, KS...>(launches, spans, n_spans, head, bitmap_words, s);
     }
 };
 
@@ -1476,9 +1588,11 @@ constexpr int kDenseVariant = 3;
 constexpr int kCompactVariant = 4;
 constexpr int kCompact2Variant = 5;  // as 4 with a 2-stage copy ring
 constexpr int kCarryVariant = 6;     // as 5, compacted rows carried across tiles
-constexpr int kMaxVariant = 6;
+constexpr int kLevel2Variant = 7;    // as 6, plus a second compaction after the first row-per-lane op
+constexpr int kMaxVariant = 7;
 
-int variant_stages(int v) { return (v == kCompact2Variant || v == kCarryVariant) ? 2 : 3; }
+int variant_stages(int v) { return (v == kCompact2Variant || v >= kCarryVariant) ? 2 : 3; }
+int variant_carry(int v) { return v == kLevel2Variant ? 2 : (v == kCarryVariant ? 1 : 0); }
 
 bool operand_ok(const sdb_operand &o, int &nregs, bool &vec, const char **why)
 {
@@ -1612,7 +1726,7 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
     }
     if (variant >= kDenseVariant) {
         const int st2 = dense::dispatch(L, nregs, term, variant != kDenseVariant, variant_stages(variant),
-                                        variant == kCarryVariant, s);
+                                        variant_carry(variant), s);
         if (st2 != SDB_ERR_UNSUPPORTED) return st2;
         variant = default_variant(nregs);
     }
@@ -1628,7 +1742,7 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
 struct sdb_chain_batch {
     struct Group {
         int term, compact, stages;
-        bool carry;
+        int carry;
         dense::Launch first;             // host copy, picks the instantiation
         const dense::Launch *launches;   // device
         const dense::Span *spans;        // device
@@ -1649,7 +1763,7 @@ namespace {
 struct BatchPlan {
     struct G {
         int term, compact, stages, shape;
-        bool carry = false;
+        int carry = 0;
         std::vector<dense::Launch> launches;
         std::vector<dense::Span> spans;
         uint32_t bitmap_words = 0;
@@ -1714,7 +1828,7 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         g.term = F.term;
         g.compact = variant != kDenseVariant;
         g.stages = variant_stages(variant);
-        g.carry = variant == kCarryVariant;
+        g.carry = variant_carry(variant);
         g.shape = F.shape;
         groups.push_back(g);
         of.push_back(&F);

@@ -132,7 +132,7 @@ def test_star_sf20_full_size():
     torch.cuda.empty_cache()
 
 
-@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5, 6, 7])
 def test_every_kernel_variant_matches_golden(variant):
     """The general pass at 4/8/16 rows per thread and the shape-specialised
     pass give the same rows."""
@@ -148,7 +148,7 @@ def test_every_kernel_variant_matches_golden(variant):
         capi.force_chain_variant(-1)
 
 
-@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6])
+@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6, 7])
 def test_reversed_search_range_is_empty(variant):
     """A SEARCH range whose low bound is above its high bound selects no row
     (the reference's `c >= lo` then `c <= hi`), in every fused variant."""
