@@ -510,7 +510,7 @@ def run_batched(args, rank, world, local, pg, stream, peak):
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.1)
-    lat_b, dev_ms, chain_ms, pre_ms, post_ms = [], [], [], [], []
+    lat_b, dev_ms, chain_ms, pre_ms, post_ms, build_ms = [], [], [], [], [], []
     barrier(pg)
     t0 = time.perf_counter()
     for _ in range(args.batched_runs):
@@ -522,6 +522,7 @@ def run_batched(args, rank, world, local, pg, stream, peak):
         chain_ms.append(st["last_chain_ms"])
         pre_ms.append(st["last_pre_ms"])
         post_ms.append(st["last_post_ms"])
+        build_ms.append(st["last_build_ms"])
     batch_s = max_over_ranks(pg, sum(lat_b))
     clk = clocks.stop()
     # the same runs without the Python conversion of the results, and without
@@ -560,14 +561,19 @@ def run_batched(args, rank, world, local, pg, stream, peak):
             "note": "batched: every plan of a batch completes when the batch run returns (host wall clock "
                     "around sdb_batch_run incl. result unpacking); plain: each sdb_engine_execute alone"},
         "device_ms_per_batch": statistics.median(dev_ms),
-        "device_ms_phases": {"before_chains": statistics.median(pre_ms), "chains": statistics.median(chain_ms),
-                             "after_chains": statistics.median(post_ms)},
+        "device_ms_phases": {"before_chains": statistics.median(pre_ms),
+                             "builds": statistics.median(build_ms), "chains": statistics.median(chain_ms),
+                             "after_chains": statistics.median(post_ms),
+                             "note": "before_chains: zeroing and unbatched work on 16 streams; builds: every "
+                                     "dimension filter + hash-table build of the batch in one launch; chains: "
+                                     "the fact-side chains; after_chains: compaction, gathers, result copy"},
         "chain_batch": {"kernel": "k_batch (persistent, span work queue; semi + full + full probe, group-by)",
                         "ms": chain_med, "algorithmic_bytes": fact_bytes,
                         "achieved": achieved, "peak": peak, "unit": "GB/s",
                         "frac": achieved / peak if achieved else None},
         "kernels_per_run": st["kernels_per_run"], "graph": bool(st["graph"]),
         "chain_launches": st["chain_launches"], "batched_chains": st["batched_chains"],
+        "batched_builds": st["batched_builds"],
         "arena_bytes": st["arena_bytes"], "bit_exact_vs_plain": exact,
         "plain_rounds": args.plain_rounds, "batched_runs": args.batched_runs, "clocks": clk,
     }

@@ -269,7 +269,14 @@ typedef struct sdb_chain_op {
 typedef enum sdb_chain_terminal {
     SDB_TERM_FLAGS = 0,   /* write the final flags to flags_out */
     SDB_TERM_SUM = 1,     /* *sum_out += sum of value over surviving rows (K7) */
-    SDB_TERM_GROUPBY = 2  /* dense group-by SUM into out_keys/out_sum/occ (K8) */
+    SDB_TERM_GROUPBY = 2, /* dense group-by SUM into out_keys/out_sum/occ (K8) */
+    /* Hash-table builds (Column::build_keys_hash_table / build_key_vals_hash_table,
+     * models/models.hpp:1413-1452, 1509-1548): every row of the segment writes
+     * its slot (build_key - ht_min) % ht_len of ht_out, live rows a hit and
+     * dead rows a miss, as K10/K12 (kernels/join.hpp:17-33, 60-93) do with
+     * the final flags. */
+    SDB_TERM_BUILD_KEYS = 3, /* uint8 ht_out[slot] = flag */
+    SDB_TERM_BUILD_KV = 4    /* flag: int32 ht_out[2 slot] = 1, [2 slot + 1] = build_val; else [2 slot] = 0 */
 } sdb_chain_terminal;
 
 typedef struct sdb_chain_desc {
@@ -290,6 +297,16 @@ typedef struct sdb_chain_desc {
     int32_t *out_keys[SDB_CHAIN_MAX_KEYS];
     uint64_t *out_sum;
     uint32_t *occ;
+    sdb_operand build_key;      /* BUILD_KEYS / BUILD_KV: the key of every row */
+    sdb_operand build_val;      /* BUILD_KV: the value of live rows */
+    void *ht_out;               /* BUILD: uint8[ht_len] (KEYS) or int32[2 ht_len] (KV) */
+    int32_t ht_min, ht_len;
+    int32_t ht_zeroed;          /* BUILD: 1 = ht_out is all zero before the chain runs and no other
+                                   build writes it meanwhile: a dead row's miss (a zero written over a
+                                   zero) is skipped, so dead rows cost no key load and no store.  With
+                                   duplicate keys the table is the one the reference's unordered
+                                   writes give when dead rows write first. */
+    int32_t pad2;
 } sdb_chain_desc;
 
 /* Launch one fused pass.  The descriptor is read on the host (copied into
@@ -334,7 +351,10 @@ int sdb_chain_registers(const sdb_chain_desc *chain);
  * turn.  Chains are grouped by the kernel instantiation they map to; each
  * group's (chain, tile range) spans go to one launch whose blocks pull spans
  * from a device work queue.  Chains without a batched instantiation are
- * launched one by one by sdb_chain_batch_launch.
+ * launched one by one by sdb_chain_batch_launch.  Hash-table builds
+ * (SDB_TERM_BUILD_*) go first, all of them in one persistent launch of the
+ * general pass, so the other chains may probe the tables they build; a build
+ * chain may not probe a table that another build chain of the batch writes.
  *
  * sdb_chain_batch_create checks every chain, writes the batch's tables into
  * `dev_scratch` (sdb_chain_batch_scratch_bytes(chains, n) bytes, 256-byte
@@ -354,6 +374,10 @@ int sdb_chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *dev
 int sdb_chain_batch_create_async(const sdb_chain_desc *chains, int n_chains, void *dev_scratch, size_t dev_bytes,
                                  void *host_staging, size_t host_bytes, sdb_stream_t stream, sdb_chain_batch **out);
 int sdb_chain_batch_launch(const sdb_chain_batch *batch, sdb_stream_t stream);
+/* One part of sdb_chain_batch_launch: part 0 launches the build chains (if
+ * any), part 1 the rest (memset included); part 0 then part 1 on one stream is
+ * sdb_chain_batch_launch.  Lets a caller time the two apart. */
+int sdb_chain_batch_launch_part(const sdb_chain_batch *batch, int part, sdb_stream_t stream);
 /* Kernel launches one sdb_chain_batch_launch makes (the memset excluded). */
 int sdb_chain_batch_kernels(const sdb_chain_batch *batch);
 void sdb_chain_batch_destroy(sdb_chain_batch *batch);
@@ -489,16 +513,17 @@ typedef struct sdb_batch_stats {
     int32_t n_plans;
     int32_t kernels_per_run;  /* library kernel launches one run makes */
     int32_t graph;            /* 1: runs are CUDA graph launches */
-    int32_t chain_launches;   /* launches of the chain batch (one per chain shape) */
-    int32_t batched_chains;   /* chains that went into the chain batch */
-    int32_t pad;
+    int32_t chain_launches;   /* kernel launches of the chain batch (one per chain shape, one for all builds) */
+    int32_t batched_chains;   /* aggregating chains that went into the chain batch */
+    int32_t batched_builds;   /* hash-table build chains that went into its build launch */
     uint64_t arena_bytes;     /* the batch's device arena */
     uint64_t zero_bytes;      /* of it, the region cleared on each run */
     uint64_t host_bytes;      /* pinned staging */
     double last_run_ms;       /* device milliseconds of the last run */
-    double last_chain_ms;     /* of it, the chain batch's launches (0: none) */
-    double last_pre_ms;       /* before the chain batch: zeroing, dimension filters and builds */
+    double last_chain_ms;     /* of it, the chain batch's aggregating chains (0: none) */
+    double last_pre_ms;       /* before the chain batch: zeroing and work no launch batched */
     double last_post_ms;      /* after it: final flags, compaction, gathers, result copies */
+    double last_build_ms;     /* the chain batch's hash-table builds (one launch; 0: none) */
 } sdb_batch_stats;
 
 int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int n_plans, int flags,

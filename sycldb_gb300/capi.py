@@ -27,7 +27,7 @@ MUL, DIV, ADD, SUB = range(4)
 
 SRC_COL, SRC_REG, SRC_LIT = range(3)
 OP_SELECT, OP_SEARCH_RANGE, OP_SEARCH_POINTS, OP_SEMI_PROBE, OP_FULL_PROBE, OP_BINOP, OP_FILL = range(7)
-TERM_FLAGS, TERM_SUM, TERM_GROUPBY = range(3)
+TERM_FLAGS, TERM_SUM, TERM_GROUPBY, TERM_BUILD_KEYS, TERM_BUILD_KV = range(5)
 CHAIN_MAX_OPS, CHAIN_MAX_REGS, CHAIN_MAX_KEYS = 16, 8, 4
 
 
@@ -52,7 +52,9 @@ class ChainDesc(ctypes.Structure):
                 ("terminal", c_int32), ("ops", ChainOp * CHAIN_MAX_OPS), ("value", Operand), ("sum_out", c_void_p),
                 ("n_keys", c_int32), ("pad", c_int32), ("keys", Operand * CHAIN_MAX_KEYS),
                 ("key_min", c_int32 * CHAIN_MAX_KEYS), ("key_max", c_int32 * CHAIN_MAX_KEYS), ("P", c_uint64),
-                ("out_keys", c_void_p * CHAIN_MAX_KEYS), ("out_sum", c_void_p), ("occ", c_void_p)]
+                ("out_keys", c_void_p * CHAIN_MAX_KEYS), ("out_sum", c_void_p), ("occ", c_void_p),
+                ("build_key", Operand), ("build_val", Operand), ("ht_out", c_void_p), ("ht_min", c_int32),
+                ("ht_len", c_int32), ("ht_zeroed", c_int32), ("pad2", c_int32)]
 
 
 class EngineConfig(ctypes.Structure):
@@ -62,9 +64,9 @@ class EngineConfig(ctypes.Structure):
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("n_plans", c_int32), ("kernels_per_run", c_int32), ("graph", c_int32), ("chain_launches", c_int32),
-                ("batched_chains", c_int32), ("pad", c_int32), ("arena_bytes", c_uint64), ("zero_bytes", c_uint64),
+                ("batched_chains", c_int32), ("batched_builds", c_int32), ("arena_bytes", c_uint64), ("zero_bytes", c_uint64),
                 ("host_bytes", c_uint64), ("last_run_ms", c_double), ("last_chain_ms", c_double),
-                ("last_pre_ms", c_double), ("last_post_ms", c_double)]
+                ("last_pre_ms", c_double), ("last_post_ms", c_double), ("last_build_ms", c_double)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -128,6 +130,7 @@ _SIGS = {
     "sdb_chain_batch_create_async": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, c_void_p, c_size_t, _P,
                                              POINTER(c_void_p)]),
     "sdb_chain_batch_launch": (c_int, [c_void_p, _P]),
+    "sdb_chain_batch_launch_part": (c_int, [c_void_p, c_int, _P]),
     "sdb_chain_batch_kernels": (c_int, [c_void_p]),
     "sdb_chain_batch_destroy": (None, [c_void_p]),
     "sdb_gen_uniform_host": (c_int32, [c_uint64, c_uint64, c_uint64, c_int32, c_int32]),

@@ -348,6 +348,7 @@ struct KernelData {
     int32_t *res = nullptr;            // fill / perform result, full-join value output
     void *ht = nullptr;
     int32_t ht_min = 0, ht_max = 0, ht_len = 0;
+    bool ht_fresh = false;  // builds: the table is still all zero (the first segment's build)
     uint64_t *agg_res = nullptr;
     std::vector<const int32_t *> keys;  // group-by
     std::vector<int32_t> mins, maxs;
@@ -464,14 +465,22 @@ struct Fuser {
         case KernelType::FillKernel:
         case KernelType::AggregateOperationKernel:
         case KernelType::GroupByAggregateKernel:
+        case KernelType::BuildKeysHTKernel:
+        case KernelType::BuildKeyValsHTKernel:
             return true;
         default:
             return false;
         }
     }
 
+    static bool is_build(int32_t terminal)
+    {
+        return terminal == SDB_TERM_BUILD_KEYS || terminal == SDB_TERM_BUILD_KV;
+    }
+
     // Builds a chain from ks[i..]; returns the index after the last kernel
-    // consumed, or i when no chain of two or more kernels could be formed.
+    // consumed, or i when no chain could be formed (two or more kernels, or a
+    // hash-table build on its own).
     static size_t build(const std::vector<const KernelData *> &ks, size_t i,
                         const std::set<const uint8_t *> &all_true, sdb_chain_desc &c)
     {
@@ -617,6 +626,20 @@ struct Fuser {
                     c.occ = k.occ;
                     terminal = true;
                     break;
+                case KernelType::BuildKeysHTKernel:
+                case KernelType::BuildKeyValsHTKernel:
+                    // K10 / K12 with the chain's flags; nothing after the build
+                    // reads them (the build side's table is consumed by the join)
+                    if (!cur) cur = k.in;
+                    c.terminal = k.type == KernelType::BuildKeysHTKernel ? SDB_TERM_BUILD_KEYS : SDB_TERM_BUILD_KV;
+                    c.build_key = operand(k.a);
+                    if (k.type == KernelType::BuildKeyValsHTKernel) c.build_val = operand(k.b);
+                    c.ht_out = k.ht;
+                    c.ht_min = k.ht_min;
+                    c.ht_len = k.ht_len;
+                    c.ht_zeroed = k.ht_fresh ? 1 : 0;
+                    terminal = true;
+                    break;
                 default:
                     goto done;
                 }
@@ -630,7 +653,7 @@ struct Fuser {
         }
     done:
         const size_t count = j - i;
-        if (count < 2) return i;
+        if (count < 1 || (count < 2 && !(terminal && is_build(c.terminal)))) return i;
         // The input flags are not read when they are an untouched all-true
         // buffer, or when the first op overwrites them (logic NONE).
         if (c.flags_in && all_true.count(c.flags_in)) c.flags_in = nullptr;
@@ -665,6 +688,9 @@ struct DevOp {
 struct PlanRecord {
     std::vector<DevOp> pre, post;
     bool after = false;  // the plan's batched chain has been recorded
+    // hash-table builds of the plan now in the batch's build launch: the last
+    // `builds` entries of Recorder::chains
+    size_t builds = 0;
 };
 
 struct Recorder {
@@ -703,6 +729,7 @@ struct Engine {
     {
         if (rec) {
             PlanRecord &pr = rec->plans.back();
+            if (!pr.after) unbatch_builds(pr);
             (pr.after ? pr.post : pr.pre).push_back({name, std::move(fn)});
             return;
         }
@@ -740,17 +767,53 @@ struct Engine {
         if (k.out) written(k.out);
     }
 
+    // A batch runs a plan's pre work, then every batched build (one launch),
+    // then the batched aggregating chains, then the post work.  A build can
+    // only stay in that launch while nothing of its plan recorded after it
+    // runs before the launch: a plan's later pre work moves its batched
+    // builds back into its pre work, in recording order.
+    void unbatch_builds(PlanRecord &pr)
+    {
+        if (!pr.builds) return;
+        std::vector<sdb_chain_desc> cs(rec->chains.end() - (std::ptrdiff_t)pr.builds, rec->chains.end());
+        rec->chains.resize(rec->chains.size() - pr.builds);
+        pr.builds = 0;
+        for (const sdb_chain_desc &c : cs)
+            pr.pre.push_back({"build_chain", [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); }});
+    }
+
+    // Whether a build chain can join the batch's build launch: it probes no
+    // table that launch writes, and writes no table another build of the
+    // launch writes (segments of one build side stay in order).
+    bool build_batchable(const sdb_chain_desc &c) const
+    {
+        for (const sdb_chain_desc &o : rec->chains) {
+            if (!Fuser::is_build(o.terminal)) continue;
+            if (o.ht_out == c.ht_out) return false;
+            for (int k = 0; k < c.n_ops; k++)
+                if ((c.ops[k].kind == SDB_OP_SEMI_PROBE || c.ops[k].kind == SDB_OP_FULL_PROBE) && c.ops[k].ht == o.ht_out)
+                    return false;
+        }
+        return true;
+    }
+
     void run_chain(const sdb_chain_desc &c)
     {
         if (c.flags_in) ensure_filled(c.flags_in);
         PlanRecord *pr = rec ? &rec->plans.back() : nullptr;
-        if (pr && rec->batch_chains && c.terminal != SDB_TERM_FLAGS && pr->post.empty()) {
+        const bool build = Fuser::is_build(c.terminal);
+        if (pr && rec->batch_chains && build && !pr->after && build_batchable(c)) {
+            // into the batch's build launch, ahead of every aggregating chain
+            rec->chains.push_back(c);
+            pr->builds++;
+        } else if (pr && rec->batch_chains && !build && c.terminal != SDB_TERM_FLAGS && pr->post.empty()) {
             // an aggregating chain goes into the batch's shared launch; the
             // plan's later work waits for it
             rec->chains.push_back(c);
             pr->after = true;
         } else {
-            dev("fused_chain", [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); });
+            dev(build ? "build_chain" : "fused_chain",
+                [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); });
         }
         if (c.flags_out) written(c.flags_out);
     }
@@ -1199,6 +1262,7 @@ public:
                 k.ht = ht;
                 k.ht_min = mn;
                 k.ht_len = len;
+                k.ht_fresh = s == 0;  // alloc_zero; later segments keep the reference's segment order
                 b.add_kernel(k);
                 hb.push_back(b);
             }
@@ -1246,6 +1310,7 @@ public:
                 k.ht = ht;
                 k.ht_min = mn;
                 k.ht_len = len;
+                k.ht_fresh = s == 0;  // alloc_zero; later segments keep the reference's segment order
                 b.add_kernel(k);
                 hb.push_back(b);
             }
@@ -1494,8 +1559,10 @@ struct sdb_batch {
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr, ev_in = nullptr;
-    cudaEvent_t ev_c0 = nullptr, ev_c1 = nullptr;  // around the chain batch
-    double last_chain_ms = 0, last_pre_ms = 0, last_post_ms = 0;
+    // around the chain batch: before its builds, between builds and
+    // aggregating chains, after them
+    cudaEvent_t ev_c0 = nullptr, ev_cb = nullptr, ev_c1 = nullptr;
+    double last_chain_ms = 0, last_pre_ms = 0, last_post_ms = 0, last_build_ms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int kernels = 0;
@@ -1514,7 +1581,7 @@ struct sdb_batch {
         if (graph) cudaGraphDestroy(graph);
         for (auto s : side) cudaStreamDestroy(s);
         for (auto e : join) cudaEventDestroy(e);
-        for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_c1})
+        for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_cb, ev_c1})
             if (e) cudaEventDestroy(e);
         if (bs) cudaStreamDestroy(bs);
         if (host) cudaFreeHost(host);
@@ -2063,7 +2130,9 @@ void replay(sdb_batch &B, cudaStream_t main)
         SDB_CUDA(cudaStreamIsCapturing(main, &cs));
         const unsigned rf = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
         if (B.ev_c0) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c0, main, rf));
-        check(sdb_chain_batch_launch(B.cb, (sdb_stream_t)main));
+        check(sdb_chain_batch_launch_part(B.cb, 0, (sdb_stream_t)main));  // builds
+        if (B.ev_cb) SDB_CUDA(cudaEventRecordWithFlags(B.ev_cb, main, rf));
+        check(sdb_chain_batch_launch_part(B.cb, 1, (sdb_stream_t)main));  // aggregating chains
         if (B.ev_c1) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c1, main, rf));
     }
     phase(true);
@@ -2168,6 +2237,7 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
     SDB_CUDA(cudaEventCreate(&B.ev_a));
     SDB_CUDA(cudaEventCreate(&B.ev_b));
     SDB_CUDA(cudaEventCreate(&B.ev_c0));
+    SDB_CUDA(cudaEventCreate(&B.ev_cb));
     SDB_CUDA(cudaEventCreate(&B.ev_c1));
     SDB_CUDA(cudaStreamSynchronize(E.stream));
 
@@ -2209,7 +2279,9 @@ void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
     B.last_ms = ms;
     if (B.cb) {
         float cms = 0;
-        B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_c0, B.ev_c1) == cudaSuccess ? cms : -1.0;
+        B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_cb, B.ev_c1) == cudaSuccess ? cms : -1.0;
+        float bms = 0;
+        B.last_build_ms = cudaEventElapsedTime(&bms, B.ev_c0, B.ev_cb) == cudaSuccess ? bms : -1.0;
         float pre = 0, post = 0;
         B.last_pre_ms = cudaEventElapsedTime(&pre, B.ev_a, B.ev_c0) == cudaSuccess ? pre : -1.0;
         B.last_post_ms = cudaEventElapsedTime(&post, B.ev_c1, B.ev_b) == cudaSuccess ? post : -1.0;
@@ -2602,8 +2674,10 @@ int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
     info->kernels_per_run = b->kernels;
     info->graph = b->exec ? 1 : 0;
     info->chain_launches = b->chain_groups;
-    info->batched_chains = (int32_t)b->rec.chains.size();
-    info->pad = 0;
+    int32_t builds = 0;
+    for (const sdb_chain_desc &c : b->rec.chains) builds += sdb::Fuser::is_build(c.terminal) ? 1 : 0;
+    info->batched_chains = (int32_t)b->rec.chains.size() - builds;
+    info->batched_builds = builds;
     info->arena_bytes = b->mm.size();
     info->zero_bytes = b->mm.zused();
     info->host_bytes = b->host_bytes;
@@ -2611,6 +2685,7 @@ int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
     info->last_chain_ms = b->last_chain_ms;
     info->last_pre_ms = b->last_pre_ms;
     info->last_post_ms = b->last_post_ms;
+    info->last_build_ms = b->last_build_ms;
     return SDB_OK;
 }
 

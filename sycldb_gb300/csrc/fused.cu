@@ -45,13 +45,30 @@ const int g_reader_registered = (sdb_errors_add_reader(&read_errors), 0);
 
 constexpr int kThreads = 256;
 
-enum Term { T_FLAGS = 0, T_SUM = 1, T_GROUP = 2 };
+// T_BUILD covers SDB_TERM_BUILD_KEYS and SDB_TERM_BUILD_KV (told apart at run time)
+enum Term { T_FLAGS = 0, T_SUM = 1, T_GROUP = 2, T_BUILD = 3 };
+
+// A selection of a column against literals as an interval test:
+// in = (a - lo <= span) | (a - lo2 <= span2) in unsigned 32-bit arithmetic,
+// negated when neg; combined into the flag with `logic` (SDB_NONE / AND / OR).
+struct RangeTest {
+    const int32_t *col;
+    int32_t lo, lo2;
+    uint32_t span, span2;
+    int32_t logic, neg;
+};
+constexpr int kRangeTests = 3;
 
 struct ChainLaunch {
     sdb_chain_desc d;
     int32_t dead_from;   // ops at index >= dead_from cannot revive a dead row
     int32_t vec;         // all column pointers 16-byte aligned, flags 4-byte aligned
     uint32_t mults[SDB_CHAIN_MAX_KEYS];
+    // builds whose ops are all selections of columns against literals: the
+    // ops as interval tests (n_tests >= 0), evaluated with every column of a
+    // tile loaded at once; -1: the general op-by-op pass
+    int32_t n_tests;
+    RangeTest tests[kRangeTests];
 };
 
 // Block tile: kThreads x ITEMS consecutive rows.  Thread t owns rows
@@ -95,15 +112,17 @@ __device__ __forceinline__ void reg_set(Tile<NREGS, ITEMS> &T, int idx, const in
 
 __device__ __forceinline__ uint64_t row_of(uint64_t base, int k) { return base + (uint64_t)k * kThreads; }
 
-// Operand values for the items of `need` (other items unspecified).
-template <int NREGS, int ITEMS>
+// Operand values for the items of `need` (other items unspecified).  Column
+// loads are evict-first (STREAM) for fact columns read once, plain for
+// dimension columns that several chains of a batch read.
+template <bool STREAM = true, int NREGS, int ITEMS>
 __device__ __forceinline__ void fetch(const sdb_operand &o, const Tile<NREGS, ITEMS> &T, uint32_t need,
                                       int32_t (&v)[ITEMS])
 {
     if (o.kind == SDB_SRC_COL) {
 #pragma unroll
         for (int k = 0; k < ITEMS; k++)
-            if ((need >> k) & 1u) v[k] = __ldcs(o.col + row_of(T.base, k));
+            if ((need >> k) & 1u) v[k] = STREAM ? __ldcs(o.col + row_of(T.base, k)) : __ldg(o.col + row_of(T.base, k));
     } else if (o.kind == SDB_SRC_REG) {
         reg_get(T, o.reg, v);
     } else {
@@ -134,7 +153,7 @@ __device__ __forceinline__ void store_masked(int32_t *col, uint64_t base, const 
 }
 
 // Evaluates the op list on a thread's items; on return T.live holds the flags.
-template <int NREGS, int ITEMS, class LC>
+template <bool STREAM = true, int NREGS, int ITEMS, class LC>
 __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
 {
     const sdb_chain_desc &d = Lc.d;
@@ -142,7 +161,7 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
         uint8_t f[ITEMS];
 #pragma unroll
         for (int k = 0; k < ITEMS; k++)
-            if ((T.valid >> k) & 1u) f[k] = __ldcs(d.flags_in + row_of(T.base, k));
+            if ((T.valid >> k) & 1u) f[k] = STREAM ? __ldcs(d.flags_in + row_of(T.base, k)) : __ldg(d.flags_in + row_of(T.base, k));
         T.live = 0;
 #pragma unroll
         for (int k = 0; k < ITEMS; k++)
@@ -159,8 +178,8 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
         switch (op.kind) {
         case SDB_OP_SELECT: {
             const uint32_t need = op.logic_op == SDB_AND ? T.live : T.valid;
-            fetch(op.a, T, need, a);
-            fetch(op.b, T, need, c);
+            fetch<STREAM>(op.a, T, need, a);
+            fetch<STREAM>(op.b, T, need, c);
             uint32_t m = 0;
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) m |= (uint32_t)sdb::compare(op.cmp_op, a[k], c[k]) << k;
@@ -170,7 +189,7 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
         case SDB_OP_SEARCH_RANGE:
         case SDB_OP_SEARCH_POINTS: {
             const uint32_t need = op.logic_op == SDB_AND ? T.live : T.valid;
-            fetch(op.a, T, need, a);
+            fetch<STREAM>(op.a, T, need, a);
             uint32_t m = 0;
             if (op.kind == SDB_OP_SEARCH_RANGE) {
 #pragma unroll
@@ -184,7 +203,7 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
         }
         case SDB_OP_SEMI_PROBE: {
             const uint32_t need = T.live;
-            fetch(op.a, T, need, a);
+            fetch<STREAM>(op.a, T, need, a);
             const uint8_t *ht = static_cast<const uint8_t *>(op.ht);
             uint8_t h[ITEMS];
 #pragma unroll
@@ -200,7 +219,7 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
         }
         case SDB_OP_FULL_PROBE: {
             const uint32_t need = T.live;
-            fetch(op.a, T, need, a);
+            fetch<STREAM>(op.a, T, need, a);
             const int2 *ht = static_cast<const int2 *>(op.ht);
             int2 e[ITEMS];
 #pragma unroll
@@ -222,8 +241,8 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
         }
         case SDB_OP_BINOP: {
             const uint32_t need = T.live;
-            fetch(op.a, T, need, a);
-            fetch(op.b, T, need, c);
+            fetch<STREAM>(op.a, T, need, a);
+            fetch<STREAM>(op.b, T, need, c);
 #pragma unroll
             for (int k = 0; k < ITEMS; k++) a[k] = sdb::binop(a[k], c[k], op.bin_op);
             reg_set(T, op.out_reg, a, need);
@@ -282,6 +301,157 @@ __device__ __forceinline__ bool smem_group_add(uint32_t *s_key, unsigned long lo
 // per thread at 256 threads per block).
 __host__ __device__ constexpr int min_blocks_of(int ITEMS) { return ITEMS <= 4 ? 4 : (ITEMS <= 8 ? 3 : 2); }
 
+// Hash-table build over a thread's items with the chain's final flags (K10 /
+// K12): each row of `rows` writes its slot, a live row a hit (and its value),
+// a dead row a miss.  `rows` is every valid row, or only the live ones when
+// the table is known to be zero (ht_zeroed: a miss would write a zero over a
+// zero).  A key outside the table is counted as an error and skipped, as in
+// the standalone builds.
+template <int ITEMS>
+__device__ __forceinline__ void build_store(const sdb_chain_desc &d, uint32_t rows, uint32_t live,
+                                            const int32_t (&key)[ITEMS], const int32_t (&val)[ITEMS])
+{
+    const bool kv = d.terminal == SDB_TERM_BUILD_KV;
+    const uint32_t len = (uint32_t)d.ht_len;  // > 0
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+        if (!((rows >> k) & 1u)) continue;
+        // (key - min) % len: a key inside the table is its own slot; the
+        // remainder only for the others
+        uint32_t h = (uint32_t)key[k] - (uint32_t)d.ht_min;
+        if (__builtin_expect(h >= len, 0)) {
+            const int64_t w = sdb::ht_slot(key[k], d.ht_len, d.ht_min);
+            if (w < 0 || w >= d.ht_len) {
+                atomicAdd(&g_errors, 1ull);
+                continue;
+            }
+            h = (uint32_t)w;
+        }
+        const bool hit = (live >> k) & 1u;
+        if (kv) {
+            int32_t *ht2 = static_cast<int32_t *>(d.ht_out) + 2 * (uint64_t)h;
+            if (hit)
+                *reinterpret_cast<int2 *>(ht2) = make_int2(1, val[k]);
+            else
+                ht2[0] = 0;
+        } else {
+            static_cast<uint8_t *>(d.ht_out)[h] = hit ? 1 : 0;
+        }
+    }
+}
+
+template <bool STREAM, int NREGS, int ITEMS>
+__device__ __forceinline__ void build_rows(const sdb_chain_desc &d, const Tile<NREGS, ITEMS> &T)
+{
+    int32_t key[ITEMS], val[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) val[k] = 0;
+    const uint32_t rows = d.ht_zeroed ? T.live : T.valid;
+    if (rows == 0) return;
+    fetch<STREAM>(d.build_key, T, rows, key);
+    if (d.terminal == SDB_TERM_BUILD_KV) fetch<STREAM>(d.build_val, T, T.live, val);
+    build_store(d, rows, T.live, key, val);
+}
+
+// A build chain in interval-test form (NT tests) over tiles t, t + stride,
+// ... < t_end (kThreads x ITEMS rows each).  Per tile and thread: the input
+// flags and every test's column are loaded before any is used (one memory
+// round trip instead of one per op), the key and the value with them (every
+// valid row writes), or after the tests for the live rows only (ht_zeroed),
+// so that a warp without a live row stops there.  The chain's parameters are
+// read once, before the tiles.
+template <bool STREAM, int ITEMS, int NT>
+__device__ __forceinline__ void build_tiles(const ChainLaunch &L, uint32_t t, uint32_t t_end, uint32_t stride)
+{
+    const sdb_chain_desc &d = L.d;
+    auto ld = [](const int32_t *p) { return STREAM ? __ldcs(p) : __ldg(p); };
+    const uint32_t n = (uint32_t)d.n;  // interval-test chains have fewer than 2^32 rows
+    const bool kv = d.terminal == SDB_TERM_BUILD_KV;
+    const bool zeroed = d.ht_zeroed != 0;
+    const uint8_t *fin = d.flags_in;
+    const int32_t *kcol = d.build_key.kind == SDB_SRC_COL ? d.build_key.col : nullptr;
+    const int32_t *vcol = d.build_val.kind == SDB_SRC_COL ? d.build_val.col : nullptr;
+    const int32_t klit = d.build_key.lit, vlit = d.build_val.lit;
+    const int32_t *tcol[NT > 0 ? NT : 1];
+    uint32_t tlo[NT > 0 ? NT : 1], tlo2[NT > 0 ? NT : 1], tspan[NT > 0 ? NT : 1], tspan2[NT > 0 ? NT : 1];
+    uint32_t tneg[NT > 0 ? NT : 1];
+    int32_t tlogic[NT > 0 ? NT : 1];
+#pragma unroll
+    for (int j = 0; j < NT; j++) {
+        tcol[j] = L.tests[j].col;
+        tlo[j] = (uint32_t)L.tests[j].lo;
+        tlo2[j] = (uint32_t)L.tests[j].lo2;
+        tspan[j] = L.tests[j].span;
+        tspan2[j] = L.tests[j].span2;
+        tneg[j] = (uint32_t)L.tests[j].neg;
+        tlogic[j] = L.tests[j].logic;
+    }
+    for (; t < t_end; t += stride) {
+        const uint32_t base = t * (uint32_t)(kThreads * ITEMS) + threadIdx.x;
+        uint32_t valid = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) valid |= (uint32_t)(base + (uint32_t)(k * kThreads) < n) << k;
+        int32_t x[NT > 0 ? NT : 1][ITEMS], key[ITEMS], val[ITEMS];
+        uint8_t f[ITEMS];
+        auto load_kv = [&](uint32_t rows) {
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                if (!((rows >> k) & 1u)) continue;
+                const uint32_t r = base + (uint32_t)(k * kThreads);
+                key[k] = kcol ? ld(kcol + r) : klit;
+                if (kv) val[k] = vcol ? ld(vcol + r) : vlit;
+            }
+        };
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            f[k] = 1;
+            key[k] = val[k] = 0;
+#pragma unroll
+            for (int j = 0; j < NT; j++) x[j][k] = 0;
+        }
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            if (!((valid >> k) & 1u)) continue;
+            const uint32_t r = base + (uint32_t)(k * kThreads);
+            if (fin) f[k] = STREAM ? __ldcs(fin + r) : __ldg(fin + r);
+#pragma unroll
+            for (int j = 0; j < NT; j++) x[j][k] = ld(tcol[j] + r);
+        }
+        if (!zeroed) load_kv(valid);
+        uint32_t live = 0;
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) live |= (uint32_t)(f[k] != 0) << k;
+        live &= valid;
+#pragma unroll
+        for (int j = 0; j < NT; j++) {
+            uint32_t m = 0;
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) {
+                const uint32_t a = (uint32_t)x[j][k];
+                m |= ((((a - tlo[j]) <= tspan[j]) | ((a - tlo2[j]) <= tspan2[j])) ^ tneg[j]) << k;
+            }
+            live = tlogic[j] == SDB_NONE ? (m & valid) : (tlogic[j] == SDB_AND ? (live & m) : ((live | m) & valid));
+        }
+        if (zeroed) {
+            if (live == 0) continue;
+            load_kv(live);
+        }
+        build_store(d, zeroed ? live : valid, live, key, val);
+    }
+}
+
+template <bool STREAM, int ITEMS>
+__device__ __forceinline__ void build_tiles_any(const ChainLaunch &L, uint32_t t, uint32_t t_end, uint32_t stride)
+{
+    switch (L.n_tests) {
+    case 0: build_tiles<STREAM, ITEMS, 0>(L, t, t_end, stride); break;
+    case 1: build_tiles<STREAM, ITEMS, 1>(L, t, t_end, stride); break;
+    case 2: build_tiles<STREAM, ITEMS, 2>(L, t, t_end, stride); break;
+    case 3: build_tiles<STREAM, ITEMS, 3>(L, t, t_end, stride); break;
+    default: build_tiles<STREAM, ITEMS, kRangeTests>(L, t, t_end, stride); break;
+    }
+}
+
 template <int TERM, int NREGS, int ITEMS>
 __global__ void __launch_bounds__(kThreads, min_blocks_of(ITEMS)) k_chain(const __grid_constant__ ChainLaunch L)
 {
@@ -298,6 +468,10 @@ __global__ void __launch_bounds__(kThreads, min_blocks_of(ITEMS)) k_chain(const 
     }
 
     constexpr uint64_t kTile = (uint64_t)kThreads * ITEMS;
+    if (TERM == T_BUILD && L.n_tests >= 0) {
+        build_tiles_any<true, ITEMS>(L, blockIdx.x, (uint32_t)((d.n + kTile - 1) / kTile), gridDim.x);
+        return;
+    }
     uint64_t acc = 0;
     Tile<NREGS, ITEMS> T;
 #pragma unroll
@@ -316,6 +490,10 @@ __global__ void __launch_bounds__(kThreads, min_blocks_of(ITEMS)) k_chain(const 
 #pragma unroll
             for (int k = 0; k < ITEMS; k++)
                 if ((T.valid >> k) & 1u) d.flags_out[row_of(T.base, k)] = (uint8_t)((T.live >> k) & 1u);
+        }
+        if (TERM == T_BUILD) {
+            build_rows<true>(d, T);
+            continue;
         }
         if (T.live == 0) continue;
         if (TERM == T_SUM) {
@@ -408,6 +586,105 @@ int launch_term(const ChainLaunch &L, cudaStream_t s)
     if (blocks == 0) blocks = 1;
     kern<<<(unsigned)blocks, kThreads, 0, s>>>(L);
     return sdb_check_launch("sdb_fused_chain");
+}
+
+// Hash-table builds: dimension tables are small, one tile shape serves.
+int launch_build(const ChainLaunch &L, int nregs, cudaStream_t s)
+{
+    if (nregs <= 2) return launch_term<T_BUILD, 2, 4>(L, s);
+    if (nregs <= 4) return launch_term<T_BUILD, 4, 4>(L, s);
+    return launch_term<T_BUILD, 8, 4>(L, s);
+}
+
+// The build chains of a batch in one persistent launch.  Tile t of the batch
+// (kThreads x kBuildItems rows) belongs to chain c with tile_start[c] <= t <
+// tile_start[c + 1] (no empty chains); block b takes the contiguous tiles
+// [b T / G, (b + 1) T / G), so it meets few chains, and copies a chain's
+// launch record into shared memory when it moves on to that chain.  Column
+// loads keep lines in L2: the chains of a batch often read the same
+// dimension columns.
+constexpr int kBuildItems = 8;
+
+template <int NREGS, bool GENERAL>  // GENERAL: some chain is not in interval-test form
+__global__ void __launch_bounds__(kThreads, GENERAL ? 2 : min_blocks_of(kBuildItems))
+    k_build_batch(const ChainLaunch *__restrict__ Ls, const uint32_t *__restrict__ tile_start, int n_chains)
+{
+    constexpr int ITEMS = kBuildItems;
+    constexpr uint64_t kTile = (uint64_t)kThreads * ITEMS;
+    __shared__ ChainLaunch sL;
+    const uint64_t total = tile_start[n_chains];
+    const uint32_t t0 = (uint32_t)(total * blockIdx.x / gridDim.x);
+    const uint32_t t1 = (uint32_t)(total * (blockIdx.x + 1) / gridDim.x);
+    int cur = -1;
+    Tile<NREGS, ITEMS> T;
+#pragma unroll
+    for (int r = 0; r < NREGS; r++)
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) T.reg[r][k] = 0;
+    // the block's tiles, one chain's run of them at a time
+    for (uint32_t t = t0; t < t1;) {
+        int lo = 0, hi = n_chains - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (tile_start[mid] <= t)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        if (lo != cur) {
+            __syncthreads();  // every thread is done with the previous record
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(Ls + lo);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sL);
+            for (uint32_t i = threadIdx.x; i < (uint32_t)(sizeof(ChainLaunch) / 4); i += kThreads) dst[i] = src[i];
+            __syncthreads();
+            cur = lo;
+        }
+        const uint32_t first = tile_start[lo];
+        const uint32_t end = min(t1, tile_start[lo + 1]);
+        if (!GENERAL || sL.n_tests >= 0) {
+            build_tiles_any<false, ITEMS>(sL, t - first, end - first, 1);
+            t = end;
+            continue;
+        }
+        const sdb_chain_desc &d = sL.d;
+        for (; t < end; t++) {
+            T.base = (uint64_t)(t - first) * kTile + threadIdx.x;
+            T.valid = 0;
+#pragma unroll
+            for (int k = 0; k < ITEMS; k++) T.valid |= (uint32_t)(row_of(T.base, k) < d.n) << k;
+            run_ops<false>(sL, T);
+            if (d.flags_out) {
+#pragma unroll
+                for (int k = 0; k < ITEMS; k++)
+                    if ((T.valid >> k) & 1u) d.flags_out[row_of(T.base, k)] = (uint8_t)((T.live >> k) & 1u);
+            }
+            build_rows<false>(d, T);
+        }
+    }
+}
+
+template <int NREGS, bool GENERAL>
+int launch_build_batch_t(const ChainLaunch *Ls, const uint32_t *tile_start, int n, uint32_t tiles, cudaStream_t s)
+{
+    auto kern = k_build_batch<NREGS, GENERAL>;
+    static const int per_sm = [&] {  // initialised once, thread-safe
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kThreads, 0) != cudaSuccess || v < 1) v = 1;
+        return v;
+    }();
+    const uint64_t blocks = std::max<uint64_t>(1, std::min<uint64_t>(tiles, (uint64_t)num_sms() * per_sm));
+    kern<<<(unsigned)blocks, kThreads, 0, s>>>(Ls, tile_start, n);
+    return sdb_check_launch("sdb_chain_batch_launch");
+}
+
+// nregs = 0: every chain is in interval-test form
+int launch_build_batch(const ChainLaunch *Ls, const uint32_t *tile_start, int n, uint32_t tiles, int nregs,
+                       cudaStream_t s)
+{
+    if (nregs == 0) return launch_build_batch_t<1, false>(Ls, tile_start, n, tiles, s);
+    if (nregs <= 2) return launch_build_batch_t<2, true>(Ls, tile_start, n, tiles, s);
+    if (nregs <= 4) return launch_build_batch_t<4, true>(Ls, tile_start, n, tiles, s);
+    return launch_build_batch_t<8, true>(Ls, tile_start, n, tiles, s);
 }
 
 // Variants: 0, 1, 2 = 4, 8, 16 rows per thread.  Chains needing up to 2
@@ -1610,6 +1887,64 @@ bool operand_ok(const sdb_operand &o, int &nregs, bool &vec, const char **why)
     return true;
 }
 
+// A build chain's ops as interval tests (RangeTest), or -1 when some op is
+// not a selection of a column against literals (or uses a code the general
+// pass treats specially) or there are more than kRangeTests.  Each test holds
+// for exactly the values the op's comparison holds for.
+int range_tests(const sdb_chain_desc &c, RangeTest *out)
+{
+    constexpr int32_t kMin = INT32_MIN, kMax = INT32_MAX;
+    if (c.n_ops > kRangeTests || c.n >= (1ull << 32) - 4096) return -1;
+    if ((c.build_key.kind != SDB_SRC_COL && c.build_key.kind != SDB_SRC_LIT) ||
+        (c.terminal == SDB_TERM_BUILD_KV && c.build_val.kind != SDB_SRC_COL && c.build_val.kind != SDB_SRC_LIT))
+        return -1;
+    for (int i = 0; i < c.n_ops; i++) {
+        const sdb_chain_op &o = c.ops[i];
+        RangeTest t{};
+        if (o.a.kind != SDB_SRC_COL || o.logic_op < SDB_NONE || o.logic_op > SDB_OR) return -1;
+        t.col = o.a.col;
+        t.logic = o.logic_op;
+        bool never = false;
+        if (o.kind == SDB_OP_SELECT) {
+            if (o.b.kind != SDB_SRC_LIT) return -1;
+            const int32_t v = o.b.lit;
+            switch (o.cmp_op) {
+            case SDB_EQ: t.lo = v; t.span = 0; break;
+            case SDB_NE: t.lo = v; t.span = 0; t.neg = 1; break;
+            case SDB_LT:
+                if (v == kMin) never = true;
+                else { t.lo = kMin; t.span = (uint32_t)(v - 1) - (uint32_t)kMin; }
+                break;
+            case SDB_LE: t.lo = kMin; t.span = (uint32_t)v - (uint32_t)kMin; break;
+            case SDB_GT:
+                if (v == kMax) never = true;
+                else { t.lo = v + 1; t.span = (uint32_t)kMax - (uint32_t)(v + 1); }
+                break;
+            case SDB_GE: t.lo = v; t.span = (uint32_t)kMax - (uint32_t)v; break;
+            default: return -1;
+            }
+            t.lo2 = t.lo;
+            t.span2 = t.span;
+        } else if (o.kind == SDB_OP_SEARCH_RANGE) {
+            if (o.lo > o.hi) never = true;
+            else { t.lo = t.lo2 = o.lo; t.span = t.span2 = (uint32_t)o.hi - (uint32_t)o.lo; }
+        } else if (o.kind == SDB_OP_SEARCH_POINTS) {
+            t.lo = o.lo;
+            t.lo2 = o.hi;
+            t.span = t.span2 = 0;
+        } else {
+            return -1;
+        }
+        if (never) {  // no value: the complement of every value
+            t.lo = t.lo2 = kMin;
+            t.span = t.span2 = 0xffffffffu;
+            t.neg = 1;
+        }
+        out[i] = t;
+    }
+    return c.n_ops;
+}
+
 }  // namespace
 
 // Checks a descriptor and fills the launch record; shared with the batched
@@ -1698,6 +2033,17 @@ int sdb_chain_prepare(const sdb_chain_desc *c, void *launch_out, size_t launch_b
         *term_out = T_GROUP;
         break;
     }
+    case SDB_TERM_BUILD_KEYS:
+    case SDB_TERM_BUILD_KV: {
+        const bool kv = c->terminal == SDB_TERM_BUILD_KV;
+        if (!c->ht_out || c->ht_len <= 0) { why = "a build needs ht_out and ht_len > 0"; goto bad; }
+        if (kv && !sdb::aligned(c->ht_out, 8)) { why = "key/value table must be 8-byte aligned"; goto bad; }
+        if (!operand_ok(c->build_key, nregs, vec, &why)) goto bad;
+        if (kv && !operand_ok(c->build_val, nregs, vec, &why)) goto bad;
+        *term_out = T_BUILD;
+        L.n_tests = range_tests(*c, L.tests);
+        break;
+    }
     default:
         why = "unknown terminal";
         goto bad;
@@ -1720,6 +2066,7 @@ static int fused_chain_impl(const sdb_chain_desc *chain, int variant, sdb_stream
     if (st != SDB_OK) return st;
     if (L.d.n == 0) return SDB_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    if (term == T_BUILD) return launch_build(L, nregs, s);
     if (variant < 0) {
         variant = tune_entry(term, nregs, op_class(L.d), L.d.n);
         if (variant < 0) variant = kCompact2Variant;  // shape-specialised pass when one exists
@@ -1754,6 +2101,12 @@ struct sdb_chain_batch {
     std::vector<sdb_chain_desc> singles;  // chains with no batched instantiation
     uint32_t *heads = nullptr;
     size_t n_heads = 0;
+    // hash-table builds, launched before everything else
+    const ChainLaunch *builds = nullptr;   // device
+    const uint32_t *build_tiles = nullptr; // device, n_builds + 1 tile offsets
+    int n_builds = 0;
+    uint32_t build_total = 0;
+    int build_nregs = 0;
 };
 
 namespace {
@@ -1770,6 +2123,9 @@ struct BatchPlan {
     };
     std::vector<G> groups;
     std::vector<sdb_chain_desc> singles;
+    std::vector<ChainLaunch> builds;
+    std::vector<uint32_t> build_tiles;  // builds.size() + 1 offsets
+    int build_nregs = 0;                // 0: every build in interval-test form
     size_t bytes = 0;
 };
 
@@ -1791,12 +2147,23 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         std::vector<Item> items;
     };
     std::vector<Family> fams;
+    uint64_t build_tiles = 0;
+    bp.build_tiles.assign(1, 0);
     for (int i = 0; i < n_chains; i++) {
         ChainLaunch L;
         int nregs = 1, term = 0;
         int st = sdb_chain_prepare(&chains[i], &L, sizeof L, &nregs, &term);
         if (st != SDB_OK) return st;
         if (L.d.n == 0) continue;
+        if (term == T_BUILD) {
+            constexpr uint64_t kBuildTile = (uint64_t)kThreads * kBuildItems;
+            build_tiles += (L.d.n + kBuildTile - 1) / kBuildTile;
+            if (build_tiles > 0xffffffffull) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch: build chains too large");
+            bp.builds.push_back(L);
+            bp.build_tiles.push_back((uint32_t)build_tiles);
+            if (L.n_tests < 0) bp.build_nregs = std::max(bp.build_nregs, nregs);
+            continue;
+        }
         Item it;
         it.index = i;
         dense::ShapeProbe probe;
@@ -1849,10 +2216,23 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
                 G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + S, it.tiles), 0});
         }
     }
+    // all builds run in one launch before the other chains: none may probe a
+    // table another build writes
+    for (const ChainLaunch &B : bp.builds)
+        for (int k = 0; k < B.d.n_ops; k++) {
+            const sdb_chain_op &o = B.d.ops[k];
+            if (o.kind != SDB_OP_SEMI_PROBE && o.kind != SDB_OP_FULL_PROBE) continue;
+            for (const ChainLaunch &W : bp.builds)
+                if (W.d.ht_out == o.ht)
+                    return sdb_set_error(SDB_ERR_INVALID,
+                                         "sdb_chain_batch: a build chain probes a table built in the same batch");
+        }
     bp.groups = std::move(groups);
     bp.bytes = round256(bp.groups.size() * sizeof(uint32_t));
     for (const auto &G : bp.groups)
         bp.bytes += round256(G.launches.size() * sizeof(dense::Launch)) + round256(G.spans.size() * sizeof(dense::Span));
+    if (!bp.builds.empty())
+        bp.bytes += round256(bp.builds.size() * sizeof(ChainLaunch)) + round256(bp.build_tiles.size() * sizeof(uint32_t));
     return SDB_OK;
 }
 
@@ -1915,6 +2295,17 @@ static int chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *
         b->groups.push_back(o);
     }
     b->singles = bp.singles;
+    if (!bp.builds.empty()) {
+        std::memcpy(host + off, bp.builds.data(), bp.builds.size() * sizeof(ChainLaunch));
+        b->builds = reinterpret_cast<const ChainLaunch *>(dev + off);
+        off += round256(bp.builds.size() * sizeof(ChainLaunch));
+        std::memcpy(host + off, bp.build_tiles.data(), bp.build_tiles.size() * sizeof(uint32_t));
+        b->build_tiles = reinterpret_cast<const uint32_t *>(dev + off);
+        off += round256(bp.build_tiles.size() * sizeof(uint32_t));
+        b->n_builds = (int)bp.builds.size();
+        b->build_total = bp.build_tiles.back();
+        b->build_nregs = bp.build_nregs;
+    }
     cudaStream_t s = (cudaStream_t)stream;
     if (bp.bytes) {
         cudaError_t e = cudaMemcpyAsync(dev_scratch, host, bp.bytes, cudaMemcpyHostToDevice, s);
@@ -1941,10 +2332,14 @@ int sdb_chain_batch_create_async(const sdb_chain_desc *chains, int n_chains, voi
     return chain_batch_create(chains, n_chains, dev_scratch, dev_bytes, host_staging, host_bytes, stream, out);
 }
 
-int sdb_chain_batch_launch(const sdb_chain_batch *b, sdb_stream_t stream)
+int sdb_chain_batch_launch_part(const sdb_chain_batch *b, int part, sdb_stream_t stream)
 {
     if (!b) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_launch: NULL batch");
+    if (part != 0 && part != 1) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_launch_part: part %d", part);
     cudaStream_t s = (cudaStream_t)stream;
+    if (part == 0)
+        return b->n_builds ? launch_build_batch(b->builds, b->build_tiles, b->n_builds, b->build_total, b->build_nregs, s)
+                           : SDB_OK;
     if (b->n_heads) {
         cudaError_t e = cudaMemsetAsync(b->heads, 0, b->n_heads * sizeof(uint32_t), s);
         if (e != cudaSuccess) return sdb_set_error(SDB_ERR_CUDA, "sdb_chain_batch_launch: %s", cudaGetErrorString(e));
@@ -1961,10 +2356,16 @@ int sdb_chain_batch_launch(const sdb_chain_batch *b, sdb_stream_t stream)
     return SDB_OK;
 }
 
+int sdb_chain_batch_launch(const sdb_chain_batch *b, sdb_stream_t stream)
+{
+    const int st = sdb_chain_batch_launch_part(b, 0, stream);
+    return st != SDB_OK ? st : sdb_chain_batch_launch_part(b, 1, stream);
+}
+
 int sdb_chain_batch_kernels(const sdb_chain_batch *b)
 {
     if (!b) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_batch_kernels: NULL batch");
-    return (int)(b->groups.size() + b->singles.size());
+    return (int)(b->groups.size() + b->singles.size()) + (b->n_builds ? 1 : 0);
 }
 
 void sdb_chain_batch_destroy(sdb_chain_batch *b) { delete b; }

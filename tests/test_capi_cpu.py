@@ -142,3 +142,43 @@ def test_misaligned_typed_pointers_are_rejected_on_the_host():
     d.terminal = capi.TERM_FLAGS
     d.flags_out = 0x2000
     assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID
+
+
+def test_build_chain_checks_need_no_device():
+    """Build terminals are checked on the host; a chain batch refuses a build
+    chain that probes a table another build chain of the batch writes (all
+    builds share one launch)."""
+    L = capi.lib()
+
+    def build(ht, probe_ht=None):
+        d = capi.ChainDesc()
+        d.n = 1000
+        d.terminal = capi.TERM_BUILD_KV
+        d.build_key.kind = capi.SRC_COL
+        d.build_key.col = 0x10000
+        d.build_val.kind = capi.SRC_COL
+        d.build_val.col = 0x20000
+        d.ht_out = ht
+        d.ht_min = 1
+        d.ht_len = 1000
+        if probe_ht:
+            d.n_ops = 1
+            d.ops[0].kind = capi.OP_SEMI_PROBE
+            d.ops[0].a.kind = capi.SRC_COL
+            d.ops[0].a.col = 0x30000
+            d.ops[0].lo, d.ops[0].hi = 0, 99
+            d.ops[0].ht = probe_ht
+        return d
+
+    d = build(0)
+    assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID
+    assert "ht_out" in capi.last_error()
+    d = build(0x40004)  # a key/value table must be 8-byte aligned
+    assert L.sdb_fused_chain(ctypes.byref(d), None) == capi.SDB_ERR_INVALID
+    ok = (capi.ChainDesc * 2)(build(0x40000), build(0x50000, probe_ht=0x60000))
+    assert L.sdb_chain_batch_scratch_bytes(ok, 2) > 0
+    bad = (capi.ChainDesc * 2)(build(0x40000), build(0x50000, probe_ht=0x40000))
+    assert L.sdb_chain_batch_scratch_bytes(bad, 2) == 0
+    h = ctypes.c_void_p()
+    assert L.sdb_chain_batch_create(bad, 2, 0x100000, 1 << 20, None, ctypes.byref(h)) == capi.SDB_ERR_INVALID
+    assert "built in the same batch" in capi.last_error()

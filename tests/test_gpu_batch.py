@@ -73,7 +73,8 @@ def test_batch_equals_each_plan_alone_and_the_oracle(tables, oracle_rows, eager,
         assert st["kernels_per_run"] > 0
         if chain_batch:
             assert st["batched_chains"] == len(pls)  # every plan ends in an aggregating chain
-            assert st["chain_launches"] == 3         # star, filter-sum and date-join shapes
+            assert st["batched_builds"] > 0          # dimension filters + builds in one launch
+            assert st["chain_launches"] == 4         # star, filter-sum and date-join shapes; the builds
         else:
             assert st["batched_chains"] == 0
 
@@ -141,7 +142,8 @@ def test_batched_form_full_size_equals_plain():
             got = [r.canonical() for r in b.run()]
             st = b.stats()
     assert got == alone
-    assert st["batched_chains"] == 64 and st["chain_launches"] == 1
+    # one launch for the 64 fact chains, one for the 192 dimension builds
+    assert st["batched_chains"] == 64 and st["batched_builds"] == 192 and st["chain_launches"] == 2
     groups = [len(r) for r in alone]
     assert max(groups) <= 280 and all(g <= p.max_groups for g, p in zip(groups, wl.params))
 
@@ -156,7 +158,7 @@ def test_batch_under_each_specialised_variant(tables, oracle_rows, variant):
         with make_engine(tables) as eng:
             with eng.batch(pls) as b:
                 got = [r.canonical() for r in b.run()]
-                assert b.stats()["chain_launches"] == 3
+                assert b.stats()["chain_launches"] == 4
             alone = [eng.execute(pl).canonical() for pl in pls]
     finally:
         capi.force_chain_variant(-1)
