@@ -508,6 +508,8 @@ typedef struct sdb_batch sdb_batch;
 
 #define SDB_BATCH_EAGER 1           /* replay the recorded launches on every run, no graph */
 #define SDB_BATCH_NO_CHAIN_BATCH 2  /* launch every fused chain on its own */
+#define SDB_BATCH_BUILDS_ONLY 4     /* batch only the hash-table builds (one launch); the aggregating
+                                       chains run on their own, with the tuned single-chain kernel */
 
 typedef struct sdb_batch_stats {
     int32_t n_plans;
@@ -521,7 +523,7 @@ typedef struct sdb_batch_stats {
     uint64_t host_bytes;      /* pinned staging */
     double last_run_ms;       /* device milliseconds of the last run */
     double last_chain_ms;     /* of it, the chain batch's aggregating chains (0: none) */
-    double last_pre_ms;       /* before the chain batch: zeroing and work no launch batched */
+    double last_pre_ms;       /* zeroing and the plans' unbatched work before the aggregating chains */
     double last_post_ms;      /* after it: final flags, compaction, gathers, result copies */
     double last_build_ms;     /* the chain batch's hash-table builds (one launch; 0: none) */
 } sdb_batch_stats;

@@ -82,6 +82,7 @@ class ServerStats(ctypes.Structure):
 
 SDB_BATCH_EAGER = 1
 SDB_BATCH_NO_CHAIN_BATCH = 2
+SDB_BATCH_BUILDS_ONLY = 4
 
 _P = c_void_p  # device pointers travel as integers
 _SIGS = {

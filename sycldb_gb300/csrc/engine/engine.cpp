@@ -685,18 +685,20 @@ struct DevOp {
     std::function<int(cudaStream_t)> fn;
 };
 
+// A batch runs every plan's `pre` work, then every batched hash-table build
+// (one launch), then every plan's `mid` work, then the batched aggregating
+// chains, then every plan's `post` work.
 struct PlanRecord {
-    std::vector<DevOp> pre, post;
-    bool after = false;  // the plan's batched chain has been recorded
-    // hash-table builds of the plan now in the batch's build launch: the last
-    // `builds` entries of Recorder::chains
-    size_t builds = 0;
+    std::vector<DevOp> pre, mid, post;
+    bool after = false;  // the plan's batched aggregating chain has been recorded
+    size_t builds = 0;   // the plan's builds in the batch's build launch
 };
 
 struct Recorder {
     std::vector<PlanRecord> plans;
     std::vector<sdb_chain_desc> chains;  // chains for sdb_chain_batch
-    bool batch_chains = true;
+    bool batch_chains = true;            // aggregating chains into the chain batch
+    bool batch_builds = true;            // hash-table builds into its build launch
 };
 
 struct Engine {
@@ -729,8 +731,7 @@ struct Engine {
     {
         if (rec) {
             PlanRecord &pr = rec->plans.back();
-            if (!pr.after) unbatch_builds(pr);
-            (pr.after ? pr.post : pr.pre).push_back({name, std::move(fn)});
+            (pr.after ? pr.post : (pr.builds ? pr.mid : pr.pre)).push_back({name, std::move(fn)});
             return;
         }
         cudaEvent_t a = nullptr;
@@ -767,20 +768,6 @@ struct Engine {
         if (k.out) written(k.out);
     }
 
-    // A batch runs a plan's pre work, then every batched build (one launch),
-    // then the batched aggregating chains, then the post work.  A build can
-    // only stay in that launch while nothing of its plan recorded after it
-    // runs before the launch: a plan's later pre work moves its batched
-    // builds back into its pre work, in recording order.
-    void unbatch_builds(PlanRecord &pr)
-    {
-        if (!pr.builds) return;
-        std::vector<sdb_chain_desc> cs(rec->chains.end() - (std::ptrdiff_t)pr.builds, rec->chains.end());
-        rec->chains.resize(rec->chains.size() - pr.builds);
-        pr.builds = 0;
-        for (const sdb_chain_desc &c : cs)
-            pr.pre.push_back({"build_chain", [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); }});
-    }
 
     // Whether a build chain can join the batch's build launch: it probes no
     // table that launch writes, and writes no table another build of the
@@ -802,8 +789,9 @@ struct Engine {
         if (c.flags_in) ensure_filled(c.flags_in);
         PlanRecord *pr = rec ? &rec->plans.back() : nullptr;
         const bool build = Fuser::is_build(c.terminal);
-        if (pr && rec->batch_chains && build && !pr->after && build_batchable(c)) {
-            // into the batch's build launch, ahead of every aggregating chain
+        if (pr && rec->batch_builds && build && !pr->after && pr->mid.empty() && build_batchable(c)) {
+            // into the batch's build launch, after the plan's pre work and
+            // before anything the plan records later (its mid work)
             rec->chains.push_back(c);
             pr->builds++;
         } else if (pr && rec->batch_chains && !build && c.terminal != SDB_TERM_FLAGS && pr->post.empty()) {
@@ -1559,9 +1547,9 @@ struct sdb_batch {
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr, ev_in = nullptr;
-    // around the chain batch: before its builds, between builds and
-    // aggregating chains, after them
-    cudaEvent_t ev_c0 = nullptr, ev_cb = nullptr, ev_c1 = nullptr;
+    // around the chain batch: before its builds, after them, before the
+    // aggregating chains (after the plans' mid work), after them
+    cudaEvent_t ev_c0 = nullptr, ev_cb = nullptr, ev_cm = nullptr, ev_c1 = nullptr;
     double last_chain_ms = 0, last_pre_ms = 0, last_post_ms = 0, last_build_ms = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1571,6 +1559,9 @@ struct sdb_batch {
     // false: streams, events, staging and arena belong to the caller (a
     // server slot), the batch runs once
     bool owns = true;
+    // false: no timing events around the chain batch (a prepared plan: one
+    // plan, where the event nodes would cost more than they tell)
+    bool timed = true;
 
     ~sdb_batch()
     {
@@ -1581,7 +1572,7 @@ struct sdb_batch {
         if (graph) cudaGraphDestroy(graph);
         for (auto s : side) cudaStreamDestroy(s);
         for (auto e : join) cudaEventDestroy(e);
-        for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_cb, ev_c1})
+        for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_cb, ev_cm, ev_c1})
             if (e) cudaEventDestroy(e);
         if (bs) cudaStreamDestroy(bs);
         if (host) cudaFreeHost(host);
@@ -2098,7 +2089,8 @@ void record_plans(Engine &E, sdb_batch &B, MemoryManager &mm, MemoryManager &rmm
         }
     };
     B.rec = Recorder();
-    B.rec.batch_chains = !(B.flags & SDB_BATCH_NO_CHAIN_BATCH);
+    B.rec.batch_chains = !(B.flags & (SDB_BATCH_NO_CHAIN_BATCH | SDB_BATCH_BUILDS_ONLY));
+    B.rec.batch_builds = !(B.flags & SDB_BATCH_NO_CHAIN_BATCH);
     B.pend.clear();
     Swap guard(E, mm, rmm, &B.rec);
     for (const std::string &pt : plans) {
@@ -2111,31 +2103,39 @@ void replay(sdb_batch &B, cudaStream_t main)
 {
     if (B.mm.zused()) SDB_CUDA(cudaMemsetAsync(B.mm.zero_base(), 0, B.mm.zused(), main));
     const size_t K = B.side.size();
-    auto phase = [&](bool post) {
+    // one phase: each plan's list on a side stream (plan p on p % K), joined
+    // back into main; nothing when every list is empty
+    auto phase = [&](std::vector<DevOp> PlanRecord::*list) {
+        bool any = false;
+        for (const PlanRecord &pr : B.rec.plans) any |= !(pr.*list).empty();
+        if (!any) return;
         SDB_CUDA(cudaEventRecord(B.fork, main));
         for (size_t i = 0; i < K; i++) SDB_CUDA(cudaStreamWaitEvent(B.side[i], B.fork, 0));
         for (size_t p = 0; p < B.rec.plans.size(); p++) {
             cudaStream_t s = B.side[p % K];
-            for (const DevOp &op : post ? B.rec.plans[p].post : B.rec.plans[p].pre) check(op.fn(s));
+            for (const DevOp &op : B.rec.plans[p].*list) check(op.fn(s));
         }
         for (size_t i = 0; i < K; i++) {
             SDB_CUDA(cudaEventRecord(B.join[i], B.side[i]));
             SDB_CUDA(cudaStreamWaitEvent(main, B.join[i], 0));
         }
     };
-    phase(false);
-    if (B.cb) {
-        // under capture, external records: they stay timing events in the graph
-        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-        SDB_CUDA(cudaStreamIsCapturing(main, &cs));
-        const unsigned rf = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
-        if (B.ev_c0) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c0, main, rf));
-        check(sdb_chain_batch_launch_part(B.cb, 0, (sdb_stream_t)main));  // builds
-        if (B.ev_cb) SDB_CUDA(cudaEventRecordWithFlags(B.ev_cb, main, rf));
-        check(sdb_chain_batch_launch_part(B.cb, 1, (sdb_stream_t)main));  // aggregating chains
-        if (B.ev_c1) SDB_CUDA(cudaEventRecordWithFlags(B.ev_c1, main, rf));
-    }
-    phase(true);
+    // under capture, external records: they stay timing events in the graph
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    SDB_CUDA(cudaStreamIsCapturing(main, &cs));
+    const unsigned rf = cs == cudaStreamCaptureStatusActive ? cudaEventRecordExternal : cudaEventRecordDefault;
+    auto mark = [&](cudaEvent_t e) {
+        if (B.cb && e && B.timed) SDB_CUDA(cudaEventRecordWithFlags(e, main, rf));
+    };
+    phase(&PlanRecord::pre);
+    mark(B.ev_c0);
+    if (B.cb) check(sdb_chain_batch_launch_part(B.cb, 0, (sdb_stream_t)main));  // builds
+    mark(B.ev_cb);
+    phase(&PlanRecord::mid);
+    mark(B.ev_cm);
+    if (B.cb) check(sdb_chain_batch_launch_part(B.cb, 1, (sdb_stream_t)main));  // aggregating chains
+    mark(B.ev_c1);
+    phase(&PlanRecord::post);
     // every plan's count and result columns, in one copy to the pinned mirror
     if (B.rbytes) SDB_CUDA(cudaMemcpyAsync(B.host, B.rbase, B.rbytes, cudaMemcpyDeviceToHost, main));
 }
@@ -2238,6 +2238,7 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
     SDB_CUDA(cudaEventCreate(&B.ev_b));
     SDB_CUDA(cudaEventCreate(&B.ev_c0));
     SDB_CUDA(cudaEventCreate(&B.ev_cb));
+    SDB_CUDA(cudaEventCreate(&B.ev_cm));
     SDB_CUDA(cudaEventCreate(&B.ev_c1));
     SDB_CUDA(cudaStreamSynchronize(E.stream));
 
@@ -2277,13 +2278,16 @@ void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
     float ms = 0;
     SDB_CUDA(cudaEventElapsedTime(&ms, B.ev_a, B.ev_b));
     B.last_ms = ms;
-    if (B.cb) {
+    if (B.cb && B.timed) {
         float cms = 0;
-        B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_cb, B.ev_c1) == cudaSuccess ? cms : -1.0;
+        B.last_chain_ms = cudaEventElapsedTime(&cms, B.ev_cm, B.ev_c1) == cudaSuccess ? cms : -1.0;
         float bms = 0;
         B.last_build_ms = cudaEventElapsedTime(&bms, B.ev_c0, B.ev_cb) == cudaSuccess ? bms : -1.0;
-        float pre = 0, post = 0;
-        B.last_pre_ms = cudaEventElapsedTime(&pre, B.ev_a, B.ev_c0) == cudaSuccess ? pre : -1.0;
+        float pre = 0, mid = 0, post = 0;
+        B.last_pre_ms = cudaEventElapsedTime(&pre, B.ev_a, B.ev_c0) == cudaSuccess &&
+                                cudaEventElapsedTime(&mid, B.ev_cb, B.ev_cm) == cudaSuccess
+                            ? pre + mid
+                            : -1.0;
         B.last_post_ms = cudaEventElapsedTime(&post, B.ev_c1, B.ev_b) == cudaSuccess ? post : -1.0;
     }
     if (!out) return;
@@ -2331,7 +2335,8 @@ std::unique_ptr<sdb_result> execute_cached(sdb_engine &eng, const std::string &t
         }
         auto B = std::make_unique<sdb_batch>();
         B->eng = &eng;
-        B->flags = SDB_BATCH_NO_CHAIN_BATCH;
+        B->flags = SDB_BATCH_BUILDS_ONLY;
+        B->timed = false;
         batch_prepare(E, *B, {text});
         c.batch = B.release();
     }
@@ -2644,7 +2649,7 @@ int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int
 {
     if (!eng || !out || n_plans < 1 || !plans_json)
         return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_batch_prepare: bad argument");
-    if (flags & ~(SDB_BATCH_EAGER | SDB_BATCH_NO_CHAIN_BATCH))
+    if (flags & ~(SDB_BATCH_EAGER | SDB_BATCH_NO_CHAIN_BATCH | SDB_BATCH_BUILDS_ONLY))
         return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_batch_prepare: unknown flags 0x%x", flags);
     *out = nullptr;
     std::vector<std::string> plans;

@@ -204,16 +204,20 @@ class Batch:
     """Many plans prepared once and run together (``sdb_engine_batch_*``).
 
     Each run replays every plan's recorded device work -- as one CUDA graph
-    unless ``eager`` -- with the plans' aggregating fused chains in one
-    persistent launch per chain shape (unless ``chain_batch`` is False), and
-    returns one ``Result`` per plan, each equal to what ``Engine.execute``
-    gives for that plan alone."""
+    unless ``eager`` -- with every plan's hash-table builds in one launch and
+    the plans' aggregating fused chains in one persistent launch per chain
+    shape (``chain_batch``: True; "builds": only the builds batched; False:
+    every chain on its own), and returns one ``Result`` per plan, each equal
+    to what ``Engine.execute`` gives for that plan alone."""
 
-    def __init__(self, engine: Engine, plans, eager: bool = False, chain_batch: bool = True):
+    def __init__(self, engine: Engine, plans, eager: bool = False, chain_batch=True):
         L = capi.lib()
         texts = [p if isinstance(p, str) else json.dumps(p) for p in plans]
         arr = (ctypes.c_char_p * len(texts))(*[t.encode() for t in texts])
-        flags = (capi.SDB_BATCH_EAGER if eager else 0) | (0 if chain_batch else capi.SDB_BATCH_NO_CHAIN_BATCH)
+        if chain_batch not in (True, False, "builds"):
+            raise ValueError("chain_batch must be True, False or 'builds'")
+        mode = {True: 0, False: capi.SDB_BATCH_NO_CHAIN_BATCH, "builds": capi.SDB_BATCH_BUILDS_ONLY}[chain_batch]
+        flags = (capi.SDB_BATCH_EAGER if eager else 0) | mode
         h = ctypes.c_void_p()
         capi.check(L.sdb_engine_batch_prepare(engine._h, arr, len(texts), flags, ctypes.byref(h)))
         self._h = h

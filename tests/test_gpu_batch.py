@@ -57,7 +57,7 @@ def make_engine(tables, **kw):
 
 
 @pytest.mark.parametrize("eager", [False, True])
-@pytest.mark.parametrize("chain_batch", [True, False])
+@pytest.mark.parametrize("chain_batch", [True, "builds", False])
 def test_batch_equals_each_plan_alone_and_the_oracle(tables, oracle_rows, eager, chain_batch):
     pls = small_plans()
     with make_engine(tables) as eng:
@@ -71,12 +71,14 @@ def test_batch_equals_each_plan_alone_and_the_oracle(tables, oracle_rows, eager,
         assert st["n_plans"] == len(pls)
         assert st["graph"] == (0 if eager else 1)
         assert st["kernels_per_run"] > 0
-        if chain_batch:
+        if chain_batch is True:
             assert st["batched_chains"] == len(pls)  # every plan ends in an aggregating chain
             assert st["batched_builds"] > 0          # dimension filters + builds in one launch
             assert st["chain_launches"] == 4         # star, filter-sum and date-join shapes; the builds
+        elif chain_batch == "builds":
+            assert st["batched_chains"] == 0 and st["batched_builds"] > 0 and st["chain_launches"] == 1
         else:
-            assert st["batched_chains"] == 0
+            assert st["batched_chains"] == 0 and st["batched_builds"] == 0
 
 
 def test_batch_with_several_segments_per_plan(tables, oracle_rows):
