@@ -104,3 +104,24 @@ def test_server_is_reusable_after_destroy(ds):
                 st, _, res, _ = srv.replay(pls, at)
             assert [r.canonical() for r in res] == alone
         assert eng.execute(pls[0]).canonical() == alone[0]  # the engine works again afterwards
+
+
+def test_large_chains_run_on_their_own_in_the_mix():
+    """A 9 M-row fact table: its aggregating chains are above the batch's
+    single-launch size (2^23 rows), so the server's batches launch them with
+    the single-chain kernel between the build launch and the chain batch.
+    Results stay those of each plan alone."""
+    big = datasets.dataset(1.5, fact_cols=(3, 4, 5, 8, 9, 11, 12))
+    assert big["lineorder"][5].size >= 1 << 23
+    pls, at = trace(3000, 48, seed=9)
+    with make_engine(big) as eng:
+        alone = [eng.execute(p).canonical() for p in pls]
+        with Server(eng, budget_bytes=8 << 30) as srv:
+            st, lat, res, wall = srv.replay(pls, at)
+            stats = srv.stats()
+        assert st == [capi.SDB_OK] * len(pls)
+        assert [r.canonical() for r in res] == alone
+        assert stats["batches"] < len(pls)
+        with eng.batch(pls[:12]) as b:
+            assert [r.canonical() for r in b.run()] == alone[:12]
+            assert b.stats()["batched_chains"] == 0  # every fact chain is large
