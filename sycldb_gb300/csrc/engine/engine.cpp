@@ -716,6 +716,26 @@ struct Engine {
     MemoryManager *rmm = nullptr;
     cudaStream_t stream = nullptr;
     bool own_stream = false;
+    // table loads: a second stream for segment statistics, the event that
+    // hands a copied column to it, and the statistics' device and pinned words
+    cudaStream_t aux = nullptr;
+    cudaEvent_t copied = nullptr;
+    int32_t *stats_dev = nullptr, *stats_host = nullptr;
+    size_t stats_cap = 0;
+
+    void stats_reserve(size_t words)
+    {
+        if (!copied) SDB_CUDA(cudaEventCreateWithFlags(&copied, cudaEventDisableTiming));
+        if (words <= stats_cap) return;
+        if (stats_dev) cudaFree(stats_dev);
+        if (stats_host) cudaFreeHost(stats_host);
+        stats_dev = stats_host = nullptr;
+        stats_cap = 0;
+        const size_t cap = std::max<size_t>(words, 1024);
+        SDB_CUDA(cudaMalloc(&stats_dev, cap * sizeof(int32_t)));
+        SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&stats_host), cap * sizeof(int32_t), cudaHostAllocDefault));
+        stats_cap = cap;
+    }
     uint64_t seg = kDefaultSegment;
     MemoryManager mm;
     std::map<std::string, std::unique_ptr<Table>> tables;
@@ -1995,7 +2015,10 @@ std::unique_ptr<sdb_result> execute_plan(Engine &E, const std::string &plan_text
     return res;
 }
 
-void load_table(Engine &E, const char *name, int ncols, const int32_t *const *cols, uint64_t nrows, int on_device)
+// Returns true when the table replaced one of the same name whose device
+// buffers it reuses column for column and whose per-segment min/max it
+// reproduces exactly: plans prepared against the old table then still hold.
+bool load_table(Engine &E, const char *name, int ncols, const int32_t *const *cols, uint64_t nrows, int on_device)
 {
     if (!name) throw Error(SDB_ERR_INVALID, "table name is NULL");
     activate_table(E, name);  // a background load of the same name finishes first
@@ -2007,11 +2030,23 @@ void load_table(Engine &E, const char *name, int ncols, const int32_t *const *co
     if (nrows == 0) throw Error(SDB_ERR_INVALID, "empty table");
     auto old = E.tables.find(name);
     std::vector<int32_t *> reuse;
+    // the old table's column layout and statistics, to tell whether it changed
+    bool comparable = false;
+    std::vector<const int32_t *> old_data(ncols, nullptr);
+    std::vector<std::pair<int32_t, int32_t>> old_stats;
     if (old != E.tables.end()) {
         SDB_CUDA(cudaStreamSynchronize(E.stream));
-        if (old->second->nrows == nrows) reuse = old->second->owned;
+        const Table &o = *old->second;
+        comparable = o.nrows == nrows && !on_device && (int)o.columns.size() == ncols;
+        if (comparable)
+            for (int c = 0; c < ncols; c++)
+                if (!o.columns[c].segments.empty()) {
+                    old_data[c] = o.columns[c].segments[0].data;
+                    for (const Segment &sg : o.columns[c].segments) old_stats.emplace_back(sg.min, sg.max);
+                }
+        if (o.nrows == nrows) reuse = o.owned;
         else
-            for (auto p : old->second->owned) cudaFree(p);
+            for (auto p : o.owned) cudaFree(p);
         E.tables.erase(old);
     }
     auto t = std::make_unique<Table>();
@@ -2033,45 +2068,52 @@ void load_table(Engine &E, const char *name, int ncols, const int32_t *const *co
                 SDB_CUDA(cudaMalloc(&d, nrows * sizeof(int32_t)));
             }
             t->owned.push_back(d);
-            SDB_CUDA(cudaMemcpyAsync(d, cols[c], nrows * sizeof(int32_t), cudaMemcpyHostToDevice, E.stream));
         }
         dev_cols.emplace_back(c, d);
     }
     for (; reuse_i < reuse.size(); reuse_i++) cudaFree(reuse[reuse_i]);
-    // Segment statistics (models/models.hpp:71-77), computed on the device.
-    int32_t *mm = nullptr;
+    // Segment statistics (models/models.hpp:71-77), computed on the device:
+    // a column's min/max run on the engine's second stream while the next
+    // column is still being copied on the first.
     const size_t nmm = dev_cols.size() * sg.size() * 2;
-    SDB_CUDA(cudaMalloc(&mm, std::max<size_t>(nmm, 2) * sizeof(int32_t)));
+    E.stats_reserve(nmm);
+    if (!E.aux) SDB_CUDA(cudaStreamCreateWithFlags(&E.aux, cudaStreamNonBlocking));
     size_t q = 0;
-    for (auto &dc : dev_cols)
+    for (auto &dc : dev_cols) {
+        if (!on_device)
+            SDB_CUDA(cudaMemcpyAsync(dc.second, cols[dc.first], nrows * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                     E.stream));
+        SDB_CUDA(cudaEventRecord(E.copied, E.stream));
+        SDB_CUDA(cudaStreamWaitEvent(E.aux, E.copied, 0));
         for (auto [start, cnt] : sg) {
-            int st = sdb_min_max_i32(dc.second + start, cnt, mm + 2 * q, (sdb_stream_t)E.stream);
-            if (st != SDB_OK) {
-                cudaFree(mm);
-                check(st);
-            }
+            check(sdb_min_max_i32(dc.second + start, cnt, E.stats_dev + 2 * q, (sdb_stream_t)E.aux));
             q++;
         }
-    std::vector<int32_t> host(nmm);
-    cudaError_t e1 = cudaMemcpyAsync(host.data(), mm, nmm * sizeof(int32_t), cudaMemcpyDeviceToHost, E.stream);
-    cudaError_t e2 = cudaStreamSynchronize(E.stream);
-    cudaFree(mm);
-    if (e1 != cudaSuccess || e2 != cudaSuccess)
-        throw Error(SDB_ERR_CUDA, std::string("load_table: ") + cudaGetErrorString(e1 != cudaSuccess ? e1 : e2));
+    }
+    if (nmm) SDB_CUDA(cudaMemcpyAsync(E.stats_host, E.stats_dev, nmm * sizeof(int32_t), cudaMemcpyDeviceToHost, E.aux));
+    SDB_CUDA(cudaStreamSynchronize(E.aux));
+    SDB_CUDA(cudaStreamSynchronize(E.stream));
     q = 0;
+    bool same = comparable;
+    size_t oq = 0;
+    for (int c = 0; c < ncols && same; c++) same = (cols[c] != nullptr) == (old_data[c] != nullptr);
     for (auto &dc : dev_cols) {
         Column &col = t->columns[dc.first];
+        if (same && old_data[dc.first] != dc.second) same = false;
         for (auto [start, cnt] : sg) {
             Segment s;
             s.data = dc.second + start;
             s.nrows = cnt;
-            s.min = host[2 * q];
-            s.max = host[2 * q + 1];
+            s.min = E.stats_host[2 * q];
+            s.max = E.stats_host[2 * q + 1];
+            if (same && (oq >= old_stats.size() || old_stats[oq] != std::make_pair(s.min, s.max))) same = false;
+            oq++;
             col.segments.push_back(s);
             q++;
         }
     }
     E.tables[name] = std::move(t);
+    return same && oq == old_stats.size();
 }
 
 // ------------------------------------------------------------------ batches
@@ -2517,6 +2559,10 @@ int sdb_engine_destroy(sdb_engine *eng)
     E.mm.release();
     if (E.plan_a) cudaEventDestroy(E.plan_a);
     if (E.plan_b) cudaEventDestroy(E.plan_b);
+    if (E.aux) cudaStreamDestroy(E.aux);
+    if (E.copied) cudaEventDestroy(E.copied);
+    if (E.stats_dev) cudaFree(E.stats_dev);
+    if (E.stats_host) cudaFreeHost(E.stats_host);
     if (E.own_stream) cudaStreamDestroy(E.stream);
     delete eng;
     return SDB_OK;
@@ -2527,8 +2573,16 @@ int sdb_engine_load_table(sdb_engine *eng, const char *name, int ncols, const in
 {
     if (!eng) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_load_table: engine is NULL");
     return sdb::guarded([&] {
-        sdb::plan_cache_clear(*eng);
-        sdb::load_table(eng->E, name, ncols, cols, nrows, on_device);
+        // prepared plans stay when the table comes back in the same buffers
+        // with the same statistics (a re-load of the same data)
+        bool same = false;
+        try {
+            same = sdb::load_table(eng->E, name, ncols, cols, nrows, on_device);
+        } catch (...) {
+            sdb::plan_cache_clear(*eng);
+            throw;
+        }
+        if (!same) sdb::plan_cache_clear(*eng);
     });
 }
 

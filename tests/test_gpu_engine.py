@@ -194,7 +194,8 @@ def test_plan_cache_replays_give_the_plain_results():
             for p, w in zip(pls, want):
                 assert eng.execute(p).canonical() == w
                 assert eng.last_plan_ms() > 0
-        # reloading a table drops the prepared plans: new data, new rows
+        # a reload into the same buffers with the same per-segment min/max
+        # keeps the prepared plans, which read the new contents
         lo = ds["lineorder"]
         lo2 = {c: (a[::-1].copy() if c == 12 else a) for c, a in lo.items()}  # revenue permuted
         eng.load_table("lineorder", lo2)
@@ -202,6 +203,14 @@ def test_plan_cache_replays_give_the_plain_results():
         ds2["lineorder"] = lo2
         for _ in range(3):
             assert eng.execute(pls[0]).canonical() == datasets.oracle_run(ds2, pls[0])
+        # statistics that change (wider brand range: another group-by size)
+        # drop them
+        part3 = {c: (a + 1000 if c == 4 else a) for c, a in ds["part"].items()}
+        eng.load_table("part", part3)
+        ds3 = dict(ds2)
+        ds3["part"] = part3
+        for _ in range(3):
+            assert eng.execute(pls[0]).canonical() == datasets.oracle_run(ds3, pls[0])
 
 
 def test_order_by_on_the_device():
