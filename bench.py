@@ -93,6 +93,9 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sf", type=float, default=SF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--unfused", action="store_true",
+                    help="operator at a time: one kernel per reference operator (K1-K16), no fused chains; "
+                         "the roofline is then over the step's summed kernel time")
     ap.add_argument("--e2e-steps", type=int, default=10, help="0 skips the host-buffer leg")
     ap.add_argument("--arena-gb", type=float, default=0.0, help="executor arena; 0 = the default budget")
     ap.add_argument("--batched-runs", type=int, default=20,
@@ -300,7 +303,8 @@ def run_ours(args, rank, world, local, pg):
 
     # (1) the plain path with every launch timed by CUDA events: the fused
     # kernel's time per launch (roofline) and the launches of one execution
-    peng = Engine(arena_bytes=arena, fuse=True, profile=True, stream=stream.cuda_stream)
+    fuse = not args.unfused
+    peng = Engine(arena_bytes=arena, fuse=fuse, profile=True, stream=stream.cuda_stream)
     peng.load_table("lineorder", fact)
     for t, c in dims.items():
         peng.load_table(t, c)
@@ -317,7 +321,10 @@ def run_ours(args, rank, world, local, pg):
     for _ in range(prof_steps):
         peng.execute(plan)
         st = peng.kernel_stats()
-        if "fused_chain" in st:
+        if not fuse:  # the whole step's kernels
+            fused_launches += 1
+            fused_ms += sum(v[1] for v in st.values())
+        elif "fused_chain" in st:
             fused_launches += st["fused_chain"][0]
             fused_ms += st["fused_chain"][1]
     pev1.record(stream)
@@ -330,7 +337,7 @@ def run_ours(args, rank, world, local, pg):
     # (2) the headline: the same plan through the engine with its plan cache
     # (from the second execution on, the prepared plan replays as one CUDA
     # graph: every kernel runs each step, only host-side planning is reused)
-    eng = Engine(arena_bytes=arena, fuse=True, plan_cache=4, stream=stream.cuda_stream)
+    eng = Engine(arena_bytes=arena, fuse=fuse, plan_cache=4, stream=stream.cuda_stream)
     eng.load_table("lineorder", fact)
     for t, c in dims.items():
         eng.load_table(t, c)
@@ -364,14 +371,15 @@ def run_ours(args, rank, world, local, pg):
     alg_bytes = 4 * len(cols) * n
     per_launch_ms = fused_ms / max(1, fused_launches)
     achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9 if fused_launches else None
-    traffic = profile_traffic() if (args.plan == "star" and sf == SF) else None
-    roof = {"kernel": kernel_name, "bound": "hbm",
+    traffic = profile_traffic() if (args.plan == "star" and sf == SF and fuse) else None
+    roof = {"kernel": kernel_name if fuse else "operator-at-a-time step (every K1-K16 launch of one execution)",
+            "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
             "launch_ms": per_launch_ms, "launches": fused_launches,
-            "timing": "CUDA events around each fused-pass launch on the executor stream, %d plain-path steps" %
-                      prof_steps}
+            "timing": "CUDA events around each %s on the executor stream, %d plain-path steps" %
+                      ("fused-pass launch" if fuse else "kernel launch, summed per step", prof_steps)}
 
     # e2e through the C ABI with host (pinned) buffers
     e2e = run_e2e(args, eng, plan, n, cols, sf, rank, stream, pg) if args.e2e_steps > 0 else None
@@ -388,7 +396,7 @@ def run_ours(args, rank, world, local, pg):
         "config": {"workload": workload_name(sf) if args.plan == "star" else "%s plan, SF%g (%d fact rows)" % (
                        args.plan, sf, n), "fact_rows_per_gpu": n, "groups": n_groups,
                    "l2": "inputs larger than L2 (%.2f GB of fact columns per step)" % (alg_bytes / 1e9),
-                   "segment_rows": 1 << 28, "fused": True, "parallelism": "replicas" if world > 1 else "1 GPU",
+                   "segment_rows": 1 << 28, "fused": fuse, "parallelism": "replicas" if world > 1 else "1 GPU",
                    "plan_cache": "on: steps 2.. replay the prepared plan as one CUDA graph (all kernels run)",
                    "plain_path_ms_per_step": plain_ms_per_step},
         "roofline": roof,

@@ -576,9 +576,11 @@ template <int TERM, int NREGS, int ITEMS>
 int launch_term(const ChainLaunch &L, cudaStream_t s)
 {
     auto kern = k_chain<TERM, NREGS, ITEMS>;
-    static int per_sm = 0;
-    if (per_sm == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, 0) != cudaSuccess || per_sm < 1))
-        per_sm = 1;
+    static const int per_sm = [&] {  // initialised once, thread-safe
+        int v = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, kern, kThreads, 0) != cudaSuccess || v < 1) v = 1;
+        return v;
+    }();
     const uint64_t tile = (uint64_t)kThreads * ITEMS;
     uint64_t blocks = (L.d.n + tile - 1) / tile;
     const uint64_t cap = (uint64_t)num_sms() * per_sm;

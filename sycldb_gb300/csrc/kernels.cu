@@ -326,29 +326,84 @@ __device__ __forceinline__ void claim_keys(const GroupArgs &a, int64_t h, uint64
 
 // Shared-memory privatised slot sums; a block's first touch of a slot also
 // runs the global first-writer exchange; sums flush once per touched slot.
+// One flagged row's slot update (K8): the first writer of a slot stores its
+// keys, the value goes into the slot's sum.
 template <bool SMEM>
+__device__ __forceinline__ void group_row(const GroupArgs &a, uint64_t r, uint64_t *s_sum, uint32_t *s_occ)
+{
+    const int64_t h = row_slot(a, r);
+    if (h < 0 || (uint64_t)h >= a.P) {
+        atomicAdd(&g_errors, 1ull);
+        return;
+    }
+    const unsigned long long v = (unsigned long long)sdb::widen(a.val[r]);
+    if (SMEM) {
+        if (atomicExch(&s_occ[h], 1u) == 0u) claim_keys(a, h, r);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&s_sum[h]), v);
+    } else {
+        if (a.occ[h] == 0u) claim_keys(a, h, r);
+        atomicAdd(reinterpret_cast<unsigned long long *>(&a.out_sum[h]), v);
+    }
+}
+
+// Grid-stride over 16-row groups: a thread reads its group's 16 flags with
+// one 16-byte load (VEC: the flags are 16-byte aligned); the warp then lists
+// its flagged rows in shared memory (a warp prefix sum of the lanes' counts)
+// and updates them one row per lane, so the key and value loads of up to 32
+// flagged rows are in flight together instead of one row after another.
+constexpr int kGroupList = 32 * 16;  // a warp's rows per iteration
+
+template <bool SMEM, bool VEC>
 __global__ void __launch_bounds__(kThreads) k_groupby(const GroupArgs a)
 {
     extern __shared__ uint64_t s_sum[];
     uint32_t *s_occ = reinterpret_cast<uint32_t *>(s_sum + (SMEM ? a.P : 0));
+    uint32_t *s_list = s_occ + (SMEM ? ((a.P + 1) & ~1ull) : 0);  // 8-byte aligned after the table
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    uint32_t *list = s_list + warp * kGroupList;
     if (SMEM) {
         for (uint64_t i = threadIdx.x; i < a.P; i += blockDim.x) { s_sum[i] = 0; s_occ[i] = 0; }
         __syncthreads();
     }
-    const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t r = tid; r < a.n; r += stride) {
-        if (!a.flags[r]) continue;
-        const int64_t h = row_slot(a, r);
-        if (h < 0 || (uint64_t)h >= a.P) { atomicAdd(&g_errors, 1ull); continue; }
-        const unsigned long long v = (unsigned long long)sdb::widen(a.val[r]);
-        if (SMEM) {
-            if (atomicExch(&s_occ[h], 1u) == 0u) claim_keys(a, h, r);
-            atomicAdd(reinterpret_cast<unsigned long long *>(&s_sum[h]), v);
-        } else {
-            if (a.occ[h] == 0u) claim_keys(a, h, r);
-            atomicAdd(reinterpret_cast<unsigned long long *>(&a.out_sum[h]), v);
+    const uint64_t groups = (a.n + 15) / 16;
+    const uint64_t wstride = (uint64_t)gridDim.x * (kThreads / 32);
+    // warp-uniform walk over chunks of 32 groups (512 rows)
+    for (uint64_t c = (uint64_t)blockIdx.x * (kThreads / 32) + warp; c * 32 < groups; c += wstride) {
+        const uint64_t gi = c * 32 + lane;
+        const uint64_t r0 = gi * 16;
+        uint32_t m = 0;  // bit b: row r0 + b is flagged
+        if (gi < groups) {
+            if (VEC && r0 + 16 <= a.n) {
+                const uint4 q = __ldcs(reinterpret_cast<const uint4 *>(a.flags + r0));
+                const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+                for (int j = 0; j < 4; j++)
+#pragma unroll
+                    for (int b = 0; b < 4; b++) m |= (uint32_t)(((w[j] >> (8 * b)) & 0xffu) != 0) << (4 * j + b);
+            } else {
+                for (int b = 0; b < 16 && r0 + b < a.n; b++) m |= (uint32_t)(a.flags[r0 + b] != 0) << b;
+            }
         }
+        // this lane's rows go to list[pos .. pos + popc(m))
+        const uint32_t cnt = __popc(m);
+        uint32_t pos = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, pos, o);
+            if (lane >= (uint32_t)o) pos += y;
+        }
+        const uint32_t total = __shfl_sync(0xffffffffu, pos, 31);
+        pos -= cnt;
+        if (total == 0) continue;
+        while (m) {
+            const int b = __ffs(m) - 1;
+            m &= m - 1;
+            list[pos++] = lane * 16 + (uint32_t)b;
+        }
+        __syncwarp();
+        const uint64_t base = c * 32 * 16;
+        for (uint32_t i = lane; i < total; i += 32) group_row<SMEM>(a, base + list[i], s_sum, s_occ);
+        __syncwarp();
     }
     if (SMEM) {
         __syncthreads();
@@ -816,16 +871,33 @@ int sdb_groupby_sum(const int32_t *const *keys, const int32_t *mins, const int32
     a.g = g; a.val = val; a.flags = flags; a.n = n; a.P = P; a.out_sum = out_sum; a.occ = occ;
     if (n == 0) return SDB_OK;
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t smem = (size_t)P * (sizeof(uint64_t) + sizeof(uint32_t));
+    // the slot table (P <= 8192: 12 B per slot, the occupancy words padded to
+    // 8 bytes) and every warp's row list
+    const size_t list_bytes = (size_t)(kThreads / 32) * kGroupList * sizeof(uint32_t);
+    const size_t smem = (P <= 8192 ? (size_t)P * sizeof(uint64_t) + ((P + 1) & ~1ull) * sizeof(uint32_t) : 0) + list_bytes;
+    const uint64_t groups = (n + 15) / 16;
+    const bool vec = sdb::aligned(flags, 16);
+    static const bool attr_set = [] {  // once, thread-safe
+        const int most = 8192 * 12 + (kThreads / 32) * kGroupList * 4;
+        cudaFuncSetAttribute(k_groupby<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        cudaFuncSetAttribute(k_groupby<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, most);
+        return true;
+    }();
+    (void)attr_set;
+    // a block per 32 x 8 groups, capped at the resident blocks
+    const uint64_t want = (groups + 32 * (kThreads / 32) - 1) / (32 * (kThreads / 32));
     if (P <= 8192) {
-        static const bool attr_set = [] {  // once, thread-safe
-            cudaFuncSetAttribute(k_groupby<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 8192 * 12);
-            return true;
-        }();
-        (void)attr_set;
-        k_groupby<true><<<sdb::grid_for(n, kThreads, 2), kThreads, smem, s>>>(a);
+        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)sdb::kSMs * 2));
+        if (vec)
+            k_groupby<true, true><<<blocks, kThreads, smem, s>>>(a);
+        else
+            k_groupby<true, false><<<blocks, kThreads, smem, s>>>(a);
     } else {
-        k_groupby<false><<<sdb::grid_for(n, kThreads, 8), kThreads, 0, s>>>(a);
+        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)sdb::kSMs * 8));
+        if (vec)
+            k_groupby<false, true><<<blocks, kThreads, smem, s>>>(a);
+        else
+            k_groupby<false, false><<<blocks, kThreads, smem, s>>>(a);
     }
     return sdb_check_launch("sdb_groupby_sum");
 }
