@@ -260,3 +260,43 @@ def test_compact_gather_equals_compaction_then_gathers(n):
     for (buf, ptr), x in zip(outs, (a, u, b)):
         assert np.array_equal(host(buf, ptr, c, x.dtype), x[sel])
     assert lib.sdb_compact_gather(f, 65537, 3, src, wide, dst, cnt, stream()) == capi.SDB_ERR_INVALID
+
+
+@pytest.mark.parametrize("P_ranges", [(7, 1000), (7, 3000)])  # 7,000 slots (shared table), 21,000 (global)
+@pytest.mark.parametrize("n", [1, 17, 4097, 1_000_003])
+@pytest.mark.parametrize("pad", [0, 1])
+@pytest.mark.parametrize("p", [0.008, 0.6])
+def test_groupby_sum_sparse_and_dense_flags_vs_oracle(P_ranges, n, pad, p):
+    """K8 over both slot tables (shared memory up to 8192 slots, global
+    beyond), with 16-byte aligned and unaligned flags, sparse and dense."""
+    rng = np.random.default_rng(n + 31 * P_ranges[1] + pad)
+    r0, r1 = P_ranges
+    k0 = rng.integers(1992, 1992 + r0, n).astype(np.int32)
+    k1 = rng.integers(0, r1, n).astype(np.int32)
+    val = rng.integers(-2**31, 2**31 - 1, n, dtype=np.int64).astype(np.int32)
+    fl = kc.flags(rng, n, p, canonical=False)
+    P = r0 * r1
+    mins = np.array([1992, 0], np.int32)
+    maxs = np.array([1992 + r0 - 1, r1 - 1], np.int32)
+    want_keys = [np.zeros(P, np.int32), np.zeros(P, np.int32)]
+    want_sum = np.zeros(P, np.uint64)
+    want_occ = np.zeros(P, np.uint32)
+    O.groupby_sum([k0, k1], mins, maxs, val, fl, P, want_keys, want_sum, want_occ)
+    lib = L()
+    keys = [dev(k)[1] for k in (k0, k1)]
+    _, v = dev(val)
+    _, f = dev(fl, 1 if pad else 0)  # one byte off: the unaligned flag path
+    okb = [zeros(P, np.int32) for _ in range(2)]
+    sb, sp = zeros(P, np.uint64)
+    ob, op = zeros(P, np.uint32)
+    kp = (ctypes.c_void_p * 2)(*keys)
+    okp = (ctypes.c_void_p * 2)(*[o[1] for o in okb])
+    mn = (ctypes.c_int32 * 2)(*mins.tolist())
+    mx = (ctypes.c_int32 * 2)(*maxs.tolist())
+    capi.check(lib.sdb_groupby_sum(kp, mn, mx, 2, v, f, n, P, okp, sp, op, stream()))
+    occ = host(ob, op, P, np.uint32)
+    assert np.array_equal(occ != 0, want_occ != 0)
+    assert np.array_equal(host(sb, sp, P, np.uint64), want_sum)
+    live = want_occ != 0
+    for (b, ptr), w in zip(okb, want_keys):
+        assert np.array_equal(host(b, ptr, P, np.int32)[live], w[live])
