@@ -208,6 +208,11 @@ int sdb_min_max_i32(const int32_t *col, uint64_t n, int32_t *minmax, sdb_stream_
  * arrays of ncols entries; wide[c] = 1 for a uint64 column, 0 for int32. */
 int sdb_compact_gather(const uint8_t *flags, uint64_t n, int ncols, const void *const *src, const int *wide,
                        void *const *dst, uint32_t *count, sdb_stream_t stream);
+/* Same, the flag of row i being occ[i] != 0: a group-by result compacted
+ * straight from its occupancy words (K8's occ), what sdb_occ_to_flags (K9)
+ * followed by sdb_compact_gather gives (transient_table.hpp:1544-1558). */
+int sdb_compact_gather_occ(const uint32_t *occ, uint64_t n, int ncols, const void *const *src, const int *wide,
+                           void *const *dst, uint32_t *count, sdb_stream_t stream);
 
 /* ORDER BY: perm[0..n) = the row ids 0..n-1 ordered by keys[0], then keys[1],
  * ... (nkeys <= 16; key_types[k] 0 = int32 compared signed, 1 = uint64

@@ -116,6 +116,8 @@ _SIGS = {
     "sdb_min_max_i32": (c_int, [_P, c_uint64, _P, _P]),
     "sdb_compact_gather": (c_int, [_P, c_uint64, c_int, POINTER(c_void_p), POINTER(c_int), POINTER(c_void_p), _P,
                                    _P]),
+    "sdb_compact_gather_occ": (c_int, [_P, c_uint64, c_int, POINTER(c_void_p), POINTER(c_int), POINTER(c_void_p), _P,
+                                       _P]),
     "sdb_sort_scratch_bytes": (c_size_t, [c_uint64]),
     "sdb_sort_rows": (c_int, [POINTER(c_void_p), POINTER(c_int), POINTER(c_int), c_int, c_uint64, _P, _P, c_size_t,
                               _P]),

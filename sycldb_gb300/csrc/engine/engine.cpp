@@ -751,6 +751,11 @@ struct Engine {
     // pass that treats the buffer as all-true never pays for it.
     std::set<const uint8_t *> all_true;
     std::map<const uint8_t *, uint64_t> unfilled;
+    // Segment flag buffers of a group-by result still to be derived from its
+    // occupancy words (transient_table.hpp:1544-1558): the conversion runs
+    // when a kernel reads the buffer, and the final compaction reads the
+    // words directly instead.
+    std::map<const uint8_t *, std::pair<const uint32_t *, uint64_t>> from_occ;
 
     // Every device operation of a plan goes through here: run now on the
     // engine's stream, or recorded for a batch.
@@ -769,6 +774,15 @@ struct Engine {
 
     void ensure_filled(const uint8_t *p)
     {
+        auto oc = from_occ.find(p);
+        if (oc != from_occ.end()) {
+            uint8_t *q = const_cast<uint8_t *>(p);
+            const uint32_t *occ = oc->second.first;
+            const uint64_t n = oc->second.second;
+            dev("occ_to_flags", [occ, q, n](cudaStream_t s) { return sdb_occ_to_flags(occ, q, n, (sdb_stream_t)s); });
+            from_occ.erase(oc);
+            return;
+        }
         auto it = unfilled.find(p);
         if (it == unfilled.end()) return;
         uint8_t *q = const_cast<uint8_t *>(p);
@@ -781,6 +795,7 @@ struct Engine {
     {
         all_true.erase(p);
         unfilled.erase(p);
+        from_occ.erase(p);
     }
 
     void run_kernel(const KernelData &k)
@@ -1219,8 +1234,8 @@ public:
         add_pending_kernels(bundles);
         execute_pending_kernels();
         uint8_t *new_flags = E.mm.alloc<uint8_t>(P);
-        E.dev("occ_to_flags",
-              [temp_flags, new_flags, P](cudaStream_t s) { return sdb_occ_to_flags(temp_flags, new_flags, P, (sdb_stream_t)s); });
+        for (auto [start, cnt] : split_rows(P, E.seg))  // K9, deferred to the first reader
+            E.from_occ[new_flags + start] = {temp_flags + start, cnt};
         flags = new_flags;
         flags_secondary = nullptr;
         nrows = P;
@@ -1756,6 +1771,7 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
     ExecutionInfo info = parse_execution_info(plan);
     E.all_true.clear();
     E.unfilled.clear();
+    E.from_occ.clear();
 
     std::deque<TransientTable> tts;
     std::vector<int> output_table(plan.rels.size(), -1);
@@ -1866,11 +1882,20 @@ PendingResult run_plan(Engine &E, const std::string &plan_text)
                 }
             }
             o.dev = dst;
-            E.ensure_filled(fl0);
-            E.dev("compact_gather", [fl0, cnt, src, wide, dst, count](cudaStream_t st) {
-                return sdb_compact_gather(fl0, cnt, (int)src.size(), src.data(), wide.data(), dst.data(), count,
-                                          (sdb_stream_t)st);
-            });
+            auto oc = E.from_occ.find(fl0);
+            if (oc != E.from_occ.end()) {  // a group-by result: straight from its occupancy words
+                const uint32_t *occ = oc->second.first;
+                E.dev("compact_gather", [occ, cnt, src, wide, dst, count](cudaStream_t st) {
+                    return sdb_compact_gather_occ(occ, cnt, (int)src.size(), src.data(), wide.data(), dst.data(), count,
+                                                  (sdb_stream_t)st);
+                });
+            } else {
+                E.ensure_filled(fl0);
+                E.dev("compact_gather", [fl0, cnt, src, wide, dst, count](cudaStream_t st) {
+                    return sdb_compact_gather(fl0, cnt, (int)src.size(), src.data(), wide.data(), dst.data(), count,
+                                              (sdb_stream_t)st);
+                });
+            }
             pr.segs.push_back(o);
             continue;
         }

@@ -638,7 +638,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(const T *src, const int32_t
 constexpr uint32_t kSmallCompactMax = 65536;
 constexpr int kSmallCompactCols = 8;
 struct SmallCompact {
-    const uint8_t *flags;
+    const void *flags;  // uint8 flags, or uint32 occupancy words (flag = word != 0)
     uint32_t n;
     int32_t ncols;
     const void *src[kSmallCompactCols];
@@ -647,14 +647,16 @@ struct SmallCompact {
     uint32_t *count;
 };
 
+template <typename F>
 __global__ void __launch_bounds__(1024) k_compact_gather_small(const __grid_constant__ SmallCompact a)
 {
+    const F *flags = static_cast<const F *>(a.flags);
     __shared__ uint32_t s_warp[32];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const uint32_t per = (a.n + 1023u) / 1024u;
     const uint32_t b = min(threadIdx.x * per, a.n), e = min(b + per, a.n);
     uint32_t cnt = 0;
-    for (uint32_t i = b; i < e; i++) cnt += a.flags[i] != 0;
+    for (uint32_t i = b; i < e; i++) cnt += flags[i] != 0;
     uint32_t x = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -676,7 +678,7 @@ __global__ void __launch_bounds__(1024) k_compact_gather_small(const __grid_cons
     uint32_t pos = x - cnt + (warp ? s_warp[warp - 1] : 0);
     if (threadIdx.x == 1023) *a.count = pos + cnt;
     for (uint32_t i = b; i < e; i++) {
-        if (!a.flags[i]) continue;
+        if (!flags[i]) continue;
         for (int c = 0; c < a.ncols; c++) {
             if (a.wide[c])
                 static_cast<uint64_t *>(a.dst[c])[pos] = static_cast<const uint64_t *>(a.src[c])[i];
@@ -1033,14 +1035,15 @@ int sdb_compact_row_ids_noalloc(const uint8_t *flags, uint64_t n, int32_t *ids, 
     return sdb_compact_row_ids(flags, n, ids, count, scratch, sizeof(g_noalloc_compact_scratch), stream);
 }
 
-int sdb_compact_gather(const uint8_t *flags, uint64_t n, int ncols, const void *const *src, const int *wide,
-                       void *const *dst, uint32_t *count, sdb_stream_t stream)
+static int compact_gather(const void *flags, bool occ, uint64_t n, int ncols, const void *const *src, const int *wide,
+                          void *const *dst, uint32_t *count, sdb_stream_t stream)
 {
     if (n > kSmallCompactMax) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: n=%llu exceeds %u",
                                                    (unsigned long long)n, kSmallCompactMax);
     if (ncols < 0 || ncols > kSmallCompactCols || (ncols && (!src || !wide || !dst)))
         return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: 0..%d columns", kSmallCompactCols);
     if (!count || (n && !flags)) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: NULL flags or count");
+    if (occ && !sdb::aligned(flags, 4)) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather_occ: occ misaligned");
     if (!sdb::aligned(count, 4)) return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_gather: count misaligned");
     SmallCompact a;
     a.flags = flags;
@@ -1055,8 +1058,23 @@ int sdb_compact_gather(const uint8_t *flags, uint64_t n, int ncols, const void *
         a.dst[c] = dst[c];
         a.wide[c] = wide[c] ? 1 : 0;
     }
-    k_compact_gather_small<<<1, 1024, 0, (cudaStream_t)stream>>>(a);
+    if (occ)
+        k_compact_gather_small<uint32_t><<<1, 1024, 0, (cudaStream_t)stream>>>(a);
+    else
+        k_compact_gather_small<uint8_t><<<1, 1024, 0, (cudaStream_t)stream>>>(a);
     return sdb_check_launch("sdb_compact_gather");
+}
+
+int sdb_compact_gather(const uint8_t *flags, uint64_t n, int ncols, const void *const *src, const int *wide,
+                       void *const *dst, uint32_t *count, sdb_stream_t stream)
+{
+    return compact_gather(flags, false, n, ncols, src, wide, dst, count, stream);
+}
+
+int sdb_compact_gather_occ(const uint32_t *occ, uint64_t n, int ncols, const void *const *src, const int *wide,
+                           void *const *dst, uint32_t *count, sdb_stream_t stream)
+{
+    return compact_gather(occ, true, n, ncols, src, wide, dst, count, stream);
 }
 
 int sdb_gather_i32(const int32_t *src, const int32_t *ids, const uint32_t *count, int32_t *dst, uint64_t cap,

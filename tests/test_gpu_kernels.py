@@ -300,3 +300,27 @@ def test_groupby_sum_sparse_and_dense_flags_vs_oracle(P_ranges, n, pad, p):
     live = want_occ != 0
     for (b, ptr), w in zip(okb, want_keys):
         assert np.array_equal(host(b, ptr, P, np.int32)[live], w[live])
+
+
+@pytest.mark.parametrize("n", [0, 1, 1023, 7000, 65536])
+def test_compact_gather_occ_equals_occ_to_flags_then_compact_gather(n):
+    """sdb_compact_gather_occ = sdb_occ_to_flags + sdb_compact_gather."""
+    rng = np.random.default_rng(n + 77)
+    m = max(n, 1)
+    occ = np.where(rng.random(m) < 0.04, rng.integers(1, 5, m), 0).astype(np.uint32)[:n]
+    a = rng.integers(-2**31, 2**31 - 1, m, dtype=np.int64).astype(np.int32)[:n]
+    u = rng.integers(0, 2**63, m, dtype=np.uint64)[:n]
+    lib = L()
+    _, op = dev(occ if n else np.zeros(1, np.uint32))
+    srcs = [dev(x if n else np.zeros(1, x.dtype))[1] for x in (a, u)]
+    outs = [zeros(m, x.dtype) for x in (a, u)]
+    cb, cnt = zeros(1, np.uint32)
+    src = (ctypes.c_void_p * 2)(*srcs)
+    dst = (ctypes.c_void_p * 2)(*[o[1] for o in outs])
+    wide = (ctypes.c_int * 2)(0, 1)
+    capi.check(lib.sdb_compact_gather_occ(op, n, 2, src, wide, dst, cnt, stream()))
+    c = int(host(cb, cnt, 1, np.uint32)[0])
+    sel = np.nonzero(occ)[0]
+    assert c == sel.size
+    for (buf, ptr), x in zip(outs, (a, u)):
+        assert np.array_equal(host(buf, ptr, c, x.dtype), x[sel])
