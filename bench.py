@@ -39,6 +39,7 @@ prints the line.
 from __future__ import annotations
 
 import argparse
+import ctypes
 import json
 import os
 import statistics
@@ -93,6 +94,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sf", type=float, default=SF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-widened", action="store_true",
+                    help="skip the widened rows (flight-3 / flight-4 shapes, device ORDER BY, columnar loader)")
     ap.add_argument("--unfused", action="store_true",
                     help="operator at a time: one kernel per reference operator (K1-K16), no fused chains; "
                          "the roofline is then over the step's summed kernel time")
@@ -388,6 +391,7 @@ def run_ours(args, rank, world, local, pg):
     torch.cuda.empty_cache()
     batched = run_batched(args, rank, world, local, pg, stream, peak) if args.batched_runs > 0 else None
     served = run_served(args, rank, world, local, pg, stream) if args.served_rates.strip() else None
+    widened = run_widened(args, rank, stream, peak) if not args.no_widened else None
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -403,6 +407,7 @@ def run_ours(args, rank, world, local, pg):
         "e2e": e2e,
         "batched": batched,
         "served": served,
+        "widened": widened,
         "gpu_launches": launches,
         "gpu_launches_note": "kernels of one execution (%d, counted on the plain path) x steps; the graph replays "
                              "the same kernels" % int(round(launches_per_step)),
@@ -481,6 +486,126 @@ def _pct(xs, q):
         return None
     k = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
     return xs[k]
+
+
+def run_widened(args, rank, stream, peak):
+    """The rows beyond the headline shape, measured the same way: the SSB
+    flight-3 (three joins, three group-by keys) and flight-4 (four joins,
+    revenue - supplycost) shapes at SF20 -- rows/s through the prepared plan
+    and the fused kernel's roofline over its fact columns --, ORDER BY on the
+    device (sdb_sort_rows throughput) and the columnar file loader."""
+    import shutil
+    import tempfile
+
+    import numpy as np
+    import torch
+
+    from sycldb_gb300 import capi, plans, ssb
+    from sycldb_gb300.engine import Engine
+
+    out = {}
+    sf = SF
+    n = ssb.fact_rows(sf)
+    dims = ssb.gen_dims(sf)
+    shapes = {
+        "flight3_customer_supplier_date": (plans.plan_customer_supplier_date(2), (2, 4, 5, 12)),
+        "flight4_profit": (plans.plan_profit(1), (2, 3, 4, 5, 12, 13)),
+    }
+    fact = ssb.gen_lineorder_device(n, sorted({c for _, cs in shapes.values() for c in cs}), sf, salt=rank)
+    torch.cuda.synchronize()
+
+    def loaded(**kw):
+        e = Engine(fuse=True, stream=stream.cuda_stream, **kw)
+        e.load_table("lineorder", fact)
+        for t, c in dims.items():
+            e.load_table(t, c)
+        return e
+
+    for name, (plan, cs) in shapes.items():
+        peng = loaded(profile=True)
+        for _ in range(3):
+            res = peng.execute(plan)
+        kms, kn = 0.0, 0
+        for _ in range(10):
+            peng.execute(plan)
+            st = peng.kernel_stats()
+            if "fused_chain" in st:
+                kn += st["fused_chain"][0]
+                kms += st["fused_chain"][1]
+        peng.close()
+        eng = loaded(plan_cache=4)
+        for _ in range(3):
+            eng.execute(plan)
+        steps = 20
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            eng.execute(plan)
+        e1.record(stream)
+        e1.synchronize()
+        eng.close()
+        ms = e0.elapsed_time(e1) / steps
+        per = kms / max(1, kn)
+        alg = 4 * len(cs) * n
+        out[name] = {"rows_per_s": n / (ms / 1e3), "ms_per_step": ms, "groups": res.nrows,
+                     "fact_columns": list(cs), "fused_kernel_ms": per,
+                     "roofline_frac": (alg / (per / 1e3) / 1e9 / peak) if kn else None,
+                     "note": "prepared plan, CUDA events over %d steps; kernel: the general fused pass, its "
+                             "algorithmic bytes %d B per fact row" % (steps, 4 * len(cs))}
+    del fact
+    torch.cuda.empty_cache()
+
+    # ORDER BY: a stable radix sort of row ids by (int32 asc, uint64 desc)
+    m = 1 << 24
+    g = torch.Generator(device="cuda").manual_seed(7)
+    k0 = torch.randint(-2**31, 2**31 - 1, (m,), dtype=torch.int32, device="cuda", generator=g)
+    k1 = torch.randint(0, 2**62, (m,), dtype=torch.int64, device="cuda", generator=g)
+    perm = torch.empty(m, dtype=torch.int32, device="cuda")
+    L = capi.lib()
+    sb = L.sdb_sort_scratch_bytes(m)
+    scratch = torch.empty(sb + 256, dtype=torch.uint8, device="cuda")
+    sp = (scratch.data_ptr() + 255) // 256 * 256
+    keys = (ctypes.c_void_p * 2)(k0.data_ptr(), k1.data_ptr())
+    types = (ctypes.c_int * 2)(0, 1)
+    desc = (ctypes.c_int * 2)(0, 1)
+    for _ in range(2):
+        capi.check(L.sdb_sort_rows(keys, types, desc, 2, m, perm.data_ptr(), sp, sb, stream.cuda_stream))
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(5):
+        capi.check(L.sdb_sort_rows(keys, types, desc, 2, m, perm.data_ptr(), sp, sb, stream.cuda_stream))
+    e1.record(stream)
+    e1.synchronize()
+    sms = e0.elapsed_time(e1) / 5
+    out["order_by_sort"] = {"rows": m, "keys": "int32 ascending, uint64 descending (12 passes of 8 bits)",
+                            "ms": sms, "rows_per_s": m / (sms / 1e3)}
+    del k0, k1, perm, scratch
+
+    # the columnar loader: the reference's file layout, just written (so in
+    # the page cache), read into device columns with min/max
+    lsf = 2.0
+    ln = ssb.fact_rows(lsf)
+    lcols = ssb.QUERY_COLUMNS["star"]
+    d = tempfile.mkdtemp(prefix="sdb_cols_")
+    try:
+        ssb.write_columnar(d, {"lineorder": ssb.gen_lineorder_host(ln, lcols, lsf)})
+        with Engine(fuse=True, stream=stream.cuda_stream) as eng:
+            times = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                eng.load_dir(d, "lineorder", columns=list(lcols), background=False)
+                torch.cuda.synchronize()
+                times.append(time.perf_counter() - t0)
+        best = min(times)
+        nbytes = 4 * len(lcols) * ln
+        out["load_dir"] = {"bytes": nbytes, "s": best, "gbs": nbytes / best / 1e9,
+                           "note": "%d lineorder columns of %d rows from files in the page cache, 32 MB "
+                                   "double-buffered pinned chunks, min/max on the device; best of 3" %
+                                   (len(lcols), ln)}
+    finally:
+        shutil.rmtree(d, ignore_errors=True)
+    return out
 
 
 def run_batched(args, rank, world, local, pg, stream, peak):

@@ -759,6 +759,7 @@ struct Launch {
     uint32_t *occ;
     const uint8_t *bitmap_ht;  // semi-join table staged as a bitmap (NULL: none)
     uint32_t bitmap_len;       // its entries
+    int32_t nregs;             // registers the chain uses (an instantiation needs NREGS >= nregs)
 };
 
 // Largest semi-join table staged as a shared-memory bitmap (32 KB of bits).
@@ -1605,8 +1606,9 @@ int launch(const Launch &L, int stages, int carry, cudaStream_t s)
 bool convert(const ChainLaunch &C, int nregs, Launch &D)
 {
     const sdb_chain_desc &c = C.d;
-    if (c.n_ops > kMaxOps || nregs > 2) return false;
+    if (c.n_ops > kMaxOps || nregs > 4) return false;
     std::memset(&D, 0, sizeof D);
+    D.nregs = nregs;
     D.n = c.n;
     D.flags_in = c.flags_in;
     D.flags_out = c.flags_out;
@@ -1715,23 +1717,32 @@ int with_shape(const Launch &D, int term, int compact, F &f)
     for (int i = 0; i < D.n_ops; i++) k[i] = D.ops[i].kind;
     const int n = D.n_ops;
     const bool c1 = compact && can_compact(D, term, 1);
+    // r2: the chain fits the 2-register instantiations (the three-full-probe
+    // one has 4)
+    const bool r2 = D.nregs <= 2;
     // star join: semi + full + full -> group-by (SSB flight 2)
-    if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_FULL_PROBE)
+    if (r2 && term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE &&
+        k[2] == SDB_OP_FULL_PROBE)
         return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>()
                   : f.template run<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
     // full + full -> group-by
-    if (term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
+    if (r2 && term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
         return f.template run<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+    // three full probes -> three-key group-by (SSB flight 3: customer, supplier, date)
+    if (D.nregs <= 4 && term == T_GROUP && n == 3 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE &&
+        k[2] == SDB_OP_FULL_PROBE)
+        return f.template run<T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
     // range filter + one join + projection -> group-by
-    if (term == T_GROUP && n == 3 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_FULL_PROBE && k[2] == SDB_OP_BINOP)
+    if (r2 && term == T_GROUP && n == 3 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_FULL_PROBE &&
+        k[2] == SDB_OP_BINOP)
         return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>()
                   : f.template run<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
     // filter-project-sum (SSB flight 1)
-    if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE && k[2] == SDB_OP_SELECT &&
-        k[3] == SDB_OP_BINOP)
+    if (r2 && term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
+        k[2] == SDB_OP_SELECT && k[3] == SDB_OP_BINOP)
         return c1 ? f.template run<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>()
                   : f.template run<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>();
-    if (term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
+    if (r2 && term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
         k[2] == SDB_OP_SEARCH_RANGE && k[3] == SDB_OP_BINOP)
         return c1 ? f.template run<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>()
                   : f.template run<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>();
