@@ -530,8 +530,8 @@ def run_widened(args, rank, stream, peak):
         peng = loaded(profile=True)
         for _ in range(3):
             res = peng.execute(plan)
-        kms, kn = 0.0, 0
-        for _ in range(10):
+        kms, kn, prof_steps = 0.0, 0, 10
+        for _ in range(prof_steps):
             peng.execute(plan)
             st = peng.kernel_stats()
             if "fused_chain" in st:
@@ -551,13 +551,15 @@ def run_widened(args, rank, stream, peak):
         e1.synchronize()
         eng.close()
         ms = e0.elapsed_time(e1) / steps
-        per = kms / max(1, kn)
+        per = kms / prof_steps  # fused-pass time of one execution
         alg = 4 * len(cs) * n
         out[name] = {"rows_per_s": n / (ms / 1e3), "ms_per_step": ms, "groups": res.nrows,
-                     "fact_columns": list(cs), "fused_kernel_ms": per,
+                     "fact_columns": list(cs), "fused_ms_per_execution": per,
+                     "fused_launches_per_execution": kn / prof_steps,
                      "roofline_frac": (alg / (per / 1e3) / 1e9 / peak) if kn else None,
-                     "note": "prepared plan, CUDA events over %d steps; kernel: the general fused pass, its "
-                             "algorithmic bytes %d B per fact row" % (steps, 4 * len(cs))}
+                     "note": "prepared plan, CUDA events over %d steps; roofline: %d B per fact row (every "
+                             "referenced fact column once) over the fused passes' time per execution" %
+                             (steps, 4 * len(cs))}
     del fact
     torch.cuda.empty_cache()
 

@@ -348,6 +348,10 @@ int sdb_chain_tune_set_op(int terminal, int nregs, int first_op, uint64_t rows, 
 int sdb_chain_tune_get_op(int terminal, int nregs, int first_op, uint64_t rows);
 /* Registers (1..8) a chain needs, or a negative status if it is invalid. */
 int sdb_chain_registers(const sdb_chain_desc *chain);
+/* 1 when the chain has a shape-specialised instantiation (variants 3-7), 0
+ * when only the general pass runs it, or a negative status if it is invalid.
+ * Host-only. */
+int sdb_chain_specialised(const sdb_chain_desc *chain);
 
 /* ------------------------------------------------------------ chain batches
  * Many fused chains in one persistent launch per chain shape.  No counterpart

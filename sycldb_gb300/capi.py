@@ -128,6 +128,7 @@ _SIGS = {
     "sdb_chain_tune_set_op": (c_int, [c_int, c_int, c_int, c_uint64, c_int]),
     "sdb_chain_tune_get_op": (c_int, [c_int, c_int, c_int, c_uint64]),
     "sdb_chain_registers": (c_int, [POINTER(ChainDesc)]),
+    "sdb_chain_specialised": (c_int, [POINTER(ChainDesc)]),
     "sdb_chain_batch_scratch_bytes": (c_size_t, [POINTER(ChainDesc), c_int]),
     "sdb_chain_batch_create": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
     "sdb_chain_batch_create_async": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, c_void_p, c_size_t, _P,

@@ -489,9 +489,11 @@ struct Fuser {
     // consumed, or i when no chain could be formed (two or more kernels, or a
     // hash-table build on its own).
     static size_t build(const std::vector<const KernelData *> &ks, size_t i,
-                        const std::set<const uint8_t *> &all_true, sdb_chain_desc &c)
+                        const std::set<const uint8_t *> &all_true, sdb_chain_desc &c,
+                        const uint8_t **final_flags = nullptr)
     {
         std::memset(&c, 0, sizeof c);
+        if (final_flags) *final_flags = nullptr;
         const KernelData &first = *ks[i];
         const uint8_t *cur = nullptr;
         std::unordered_map<const int32_t *, int> regmap;  // column produced in-chain -> register
@@ -679,7 +681,60 @@ struct Fuser {
             c.flags_out = nullptr;
         }
         if (!terminal && !c.flags_out) return i;
+        if (final_flags) *final_flags = cur;
         return j;
+    }
+
+    // Distinct columns a chain reads (the specialised pass stages up to 4).
+    static int columns(const sdb_chain_desc &c)
+    {
+        std::set<const int32_t *> cols;
+        auto add = [&](const sdb_operand &o) {
+            if (o.kind == SDB_SRC_COL) cols.insert(o.col);
+        };
+        for (int k = 0; k < c.n_ops; k++) {
+            if (c.ops[k].kind != SDB_OP_FILL) add(c.ops[k].a);
+            if (c.ops[k].kind == SDB_OP_SELECT || c.ops[k].kind == SDB_OP_BINOP) add(c.ops[k].b);
+        }
+        if (c.terminal == SDB_TERM_SUM || c.terminal == SDB_TERM_GROUPBY) add(c.value);
+        for (int q = 0; q < c.n_keys && c.terminal == SDB_TERM_GROUPBY; q++) add(c.keys[q]);
+        return (int)cols.size();
+    }
+
+    // An aggregating chain that reads more columns than the specialised pass
+    // stages, split in two specialised passes: its flag-only ops (semi
+    // probes, AND selections of columns against literals) first, writing the
+    // flags to `scratch` (the chain's own final flag buffer, which nothing
+    // reads after an aggregation), then the rest reading them.  Every op of
+    // such a chain ANDs into the row's flag and the flag-only ops use no
+    // register, so the order of the two groups does not change any live
+    // row's registers or the aggregate.  False (a, b untouched) when the
+    // chain does not qualify or either half has no specialised pass.
+    static bool split(const sdb_chain_desc &c, uint8_t *scratch, sdb_chain_desc &a, sdb_chain_desc &b)
+    {
+        if ((c.terminal != SDB_TERM_SUM && c.terminal != SDB_TERM_GROUPBY) || !scratch) return false;
+        if (columns(c) <= 4 || sdb_chain_specialised(&c) == 1) return false;
+        sdb_chain_desc A = c, B = c;
+        A.n_ops = B.n_ops = 0;
+        for (int k = 0; k < c.n_ops; k++) {
+            const sdb_chain_op &o = c.ops[k];
+            const bool sel = o.kind == SDB_OP_SELECT || o.kind == SDB_OP_SEARCH_RANGE || o.kind == SDB_OP_SEARCH_POINTS;
+            if (sel && (o.logic_op != SDB_AND || o.a.kind != SDB_SRC_COL ||
+                        (o.kind == SDB_OP_SELECT && o.b.kind == SDB_SRC_REG)))
+                return false;  // a NONE / OR selection or one over a register: order matters
+            if (sel || (o.kind == SDB_OP_SEMI_PROBE && o.a.kind == SDB_SRC_COL))
+                A.ops[A.n_ops++] = o;
+            else
+                B.ops[B.n_ops++] = o;
+        }
+        if (A.n_ops == 0 || B.n_ops == 0) return false;
+        A.terminal = SDB_TERM_FLAGS;
+        A.flags_out = scratch;
+        B.flags_in = scratch;
+        if (sdb_chain_specialised(&A) != 1 || sdb_chain_specialised(&B) != 1) return false;
+        a = A;
+        b = B;
+        return true;
     }
 };
 
@@ -856,9 +911,16 @@ struct Engine {
         while (i < ks.size()) {
             if (cfg.fuse && Fuser::fusable(ks[i]->type)) {
                 sdb_chain_desc c;
-                size_t j = Fuser::build(ks, i, all_true, c);
+                const uint8_t *last = nullptr;
+                size_t j = Fuser::build(ks, i, all_true, c, &last);
                 if (j > i) {
-                    run_chain(c);
+                    sdb_chain_desc a, b;
+                    if (Fuser::split(c, const_cast<uint8_t *>(last), a, b)) {
+                        run_chain(a);
+                        run_chain(b);
+                    } else {
+                        run_chain(c);
+                    }
                     i = j;
                     continue;
                 }

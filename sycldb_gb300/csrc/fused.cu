@@ -1717,14 +1717,21 @@ int with_shape(const Launch &D, int term, int compact, F &f)
     for (int i = 0; i < D.n_ops; i++) k[i] = D.ops[i].kind;
     const int n = D.n_ops;
     const bool c1 = compact && can_compact(D, term, 1);
-    // r2: the chain fits the 2-register instantiations (the three-full-probe
-    // one has 4)
+    // r2: the chain fits the 2-register instantiations (the flight-3 and
+    // flight-4 ones have 4)
     const bool r2 = D.nregs <= 2;
     // star join: semi + full + full -> group-by (SSB flight 2)
     if (r2 && term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE &&
         k[2] == SDB_OP_FULL_PROBE)
         return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>()
                   : f.template run<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+    // two semi probes -> flags (the flag-only front of a chain split in two)
+    if (r2 && term == T_FLAGS && n == 2 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_SEMI_PROBE)
+        return f.template run<T_FLAGS, 2, 3, SDB_OP_SEMI_PROBE, SDB_OP_SEMI_PROBE>();
+    // full + full + projection -> group-by (SSB flight 4 after its semi joins)
+    if (D.nregs <= 4 && term == T_GROUP && n == 3 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE &&
+        k[2] == SDB_OP_BINOP)
+        return f.template run<T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
     // full + full -> group-by
     if (r2 && term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
         return f.template run<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
@@ -2432,6 +2439,19 @@ int sdb_chain_registers(const sdb_chain_desc *chain)
     int nregs = 1, term = 0;
     int st = sdb_chain_prepare(chain, &L, sizeof L, &nregs, &term);
     return st != SDB_OK ? st : nregs;
+}
+
+int sdb_chain_specialised(const sdb_chain_desc *chain)
+{
+    ChainLaunch L;
+    int nregs = 1, term = 0;
+    int st = sdb_chain_prepare(chain, &L, sizeof L, &nregs, &term);
+    if (st != SDB_OK) return st;
+    if (term == T_BUILD) return 0;
+    dense::Launch D;
+    if (!dense::convert(L, nregs, D)) return 0;
+    dense::ShapeProbe probe;
+    return dense::with_shape(D, term, 1, probe) == SDB_OK ? 1 : 0;
 }
 
 }  // extern "C"

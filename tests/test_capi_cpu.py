@@ -182,3 +182,29 @@ def test_build_chain_checks_need_no_device():
     h = ctypes.c_void_p()
     assert L.sdb_chain_batch_create(bad, 2, 0x100000, 1 << 20, None, ctypes.byref(h)) == capi.SDB_ERR_INVALID
     assert "built in the same batch" in capi.last_error()
+
+
+def test_chain_specialised_is_a_host_query():
+    """sdb_chain_specialised: 1 for a chain with a shape-specialised pass, 0
+    for one only the general pass runs, a negative status when invalid."""
+    L = capi.lib()
+
+    def semi(o, col, ht):
+        o.kind = capi.OP_SEMI_PROBE
+        o.a.kind = capi.SRC_COL
+        o.a.col = col
+        o.lo, o.hi, o.ht = 1, 1000, ht
+
+    d = capi.ChainDesc()
+    d.n = 1000
+    d.n_ops = 2
+    semi(d.ops[0], 0x10000, 0x20000)
+    semi(d.ops[1], 0x30000, 0x40000)
+    d.terminal = capi.TERM_FLAGS
+    d.flags_out = 0x50000
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
+    d.n_ops = 1  # one semi probe alone: no specialised shape
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 0
+    d.n_ops = 2
+    d.flags_out = 0  # a flags chain without flags_out is invalid
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == capi.SDB_ERR_INVALID
