@@ -256,3 +256,40 @@ def test_more_ssb_shapes_match_the_oracle(fuse):
             got = eng.execute(plan).canonical()
             assert got == datasets.oracle_run(ds, plan, 1 << 16), json.dumps(plan)
             assert len(got) > 0
+
+
+def test_wide_chains_split_only_when_order_does_not_matter():
+    """An aggregating chain over more than four fact columns runs as two
+    specialised passes when its flag-only ops can go first (the profit
+    shape); with a fact filter whose ops combine with OR (order matters) it
+    stays one pass.  Both give the oracle's rows, on every variant."""
+    ds = datasets.dataset(0.05)
+    b = plans.PlanBuilder()  # profit shape plus an OR fact filter in front
+    f = b.scan("lineorder")
+    f = b.filter(plans.OR(plans.expr("<", plans.col(8), plans.lit(20)), plans.search(11, 8, 10)))
+    c = b.scan("customer")
+    c = b.filter(plans.expr("==", plans.col(5), plans.lit(1)))
+    j1 = b.join(f, c, 2, 17 + 0)
+    s = b.scan("supplier")
+    s = b.filter(plans.expr("==", plans.col(5), plans.lit(1)))
+    j2 = b.join(j1, s, 4, 25 + 0, "semi")
+    p = b.scan("part")
+    p = b.filter(plans.search_points(2, 0, 1))
+    j3 = b.join(j2, p, 3, 32 + 0, "semi")
+    d = b.scan("ddate")
+    b.join(j3, d, 5, 41 + 0)
+    b.project([plans.col(41 + 4), plans.col(17 + 4), plans.expr("-", plans.col(12), plans.col(13))])
+    b.aggregate([0, 1], 2)
+    with_or = b.plan()
+    cases = [plans.plan_profit(1), plans.plan_profit(2, (1, 3)), with_or]
+    want = [datasets.oracle_run(ds, p) for p in cases]
+    try:
+        for variant in (-1, 0, 5, 7):
+            capi.force_chain_variant(variant)
+            with Engine(arena_bytes=1 << 30) as eng:
+                load(eng, ds)
+                for plan, w in zip(cases, want):
+                    assert eng.execute(plan).canonical() == w, (variant, json.dumps(plan))
+    finally:
+        capi.force_chain_variant(-1)
+    assert all(len(w) > 0 for w in want)
