@@ -169,3 +169,22 @@ def test_batch_under_each_specialised_variant(tables, oracle_rows, variant):
         capi.force_chain_variant(-1)
     assert got == oracle_rows
     assert alone == oracle_rows
+
+
+@pytest.mark.parametrize("chain_batch", [True, "builds", False])
+def test_batch_with_split_and_three_key_chains(chain_batch):
+    """Flight-4 plans (their chains split in two passes: the flags pass runs
+    before the chain batch) and flight-3 plans (three full probes, three
+    keys) in one batch: each plan's rows as alone."""
+    ds = datasets.dataset(0.05)
+    pls = [plans.plan_profit(1), plans.plan_customer_supplier_date(2), plans.plan_profit(3, (2, 4)),
+           plans.plan_customer_supplier_date(0, 1992, 1993), plans.plan_star(1, 3)]
+    with Engine(arena_bytes=1 << 30) as eng:
+        for name, cols in ds.items():
+            eng.load_table(name, cols)
+        alone = [eng.execute(p).canonical() for p in pls]
+        with eng.batch(pls, chain_batch=chain_batch) as b:
+            for _ in range(2):
+                assert [r.canonical() for r in b.run()] == alone
+    assert alone[0] == datasets.oracle_run(ds, pls[0])
+    assert all(len(a) > 0 for a in alone)
