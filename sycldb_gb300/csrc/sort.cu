@@ -11,11 +11,13 @@
 // Each key becomes one or two 32-bit words whose unsigned order is the key's
 // order: an int32 with its sign bit flipped, a uint64 as its low then its high
 // word, and every bit inverted for a descending key.  Words are sorted from
-// the last key's low word to the first key's high word, 8 bits per pass, each
-// pass a stable counting sort of 256-row blocks: per block digit counts
-// (digit-major, so that one exclusive scan gives every block's first slot per
-// digit), the scan, then a scatter in which a row's place among equal digits
-// of its block comes from a warp match and per-warp counts.
+// the last key's low word to the first key's high word.  Each word is
+// gathered once through the current order into a word array, then sorted 8
+// bits per pass with (word, row id) pairs carried along, each pass a stable
+// counting sort of 256-row blocks: per block digit counts (digit-major, so
+// that one exclusive scan gives every block's first slot per digit), the
+// scan, then a scatter in which a row's place among equal digits of its
+// block comes from a warp match and per-warp counts.
 #include <algorithm>
 #include <cstdint>
 #include <utility>
@@ -47,21 +49,32 @@ __device__ __forceinline__ uint32_t key_word(const SortPass &p, uint32_t row)
     return p.desc ? ~w : w;
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_radix_count(const SortPass p, const uint32_t *__restrict__ perm,
+// word[i] = the pass's key word of row perm[i] (one gather per word).
+__global__ void k_gather_word(const SortPass p, const uint32_t *__restrict__ perm, uint32_t n,
+                              uint32_t *__restrict__ word)
+{
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        word[i] = key_word(p, perm[i]);
+}
+
+__global__ void __launch_bounds__(kSortThreads) k_radix_count(const uint32_t *__restrict__ word, int shift,
                                                                  uint32_t n, uint32_t *__restrict__ hist, uint32_t nb)
 {
     __shared__ uint32_t cnt[256];
     cnt[threadIdx.x] = 0;
     __syncthreads();
     const uint32_t i = blockIdx.x * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(key_word(p, perm[i]) >> p.shift) & 255u], 1u);
+    if (i < n) atomicAdd(&cnt[(word[i] >> shift) & 255u], 1u);
     __syncthreads();
     hist[threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
 }
 
-__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const SortPass p, const uint32_t *__restrict__ perm,
+// Moves (word, row id) pair i to its slot of this digit pass.
+__global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *__restrict__ word,
+                                                                   const uint32_t *__restrict__ perm, int shift,
                                                                    uint32_t n, const uint32_t *__restrict__ offs,
-                                                                   uint32_t nb, uint32_t *__restrict__ out)
+                                                                   uint32_t nb, uint32_t *__restrict__ word_out,
+                                                                   uint32_t *__restrict__ perm_out)
 {
     __shared__ uint32_t wcnt[kSortThreads / 32][256];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -70,10 +83,11 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const SortPass p
     const uint32_t i = blockIdx.x * kSortThreads + threadIdx.x;
     const bool valid = i < n;
     const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    uint32_t row = 0, d = 0, below = 0;
+    uint32_t w = 0, row = 0, d = 0, below = 0;
     if (valid) {
+        w = word[i];
         row = perm[i];
-        d = (key_word(p, row) >> p.shift) & 255u;
+        d = (w >> shift) & 255u;
         const unsigned peers = __match_any_sync(vmask, d);
         below = __popc(peers & ((1u << lane) - 1u));
         if (below == 0) wcnt[warp][d] = __popc(peers);  // the lowest lane of each digit group
@@ -81,8 +95,10 @@ __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const SortPass p
     __syncthreads();
     if (valid) {
         uint32_t before = below;
-        for (uint32_t w = 0; w < warp; w++) before += wcnt[w][d];
-        out[offs[d * nb + blockIdx.x] + before] = row;
+        for (uint32_t q = 0; q < warp; q++) before += wcnt[q][d];
+        const uint32_t at = offs[d * nb + blockIdx.x] + before;
+        word_out[at] = w;
+        perm_out[at] = row;
     }
 }
 
@@ -154,7 +170,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_add(uint32_t *a, uint32_t
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 struct Scratch {
-    uint32_t *perm_b, *hist, *sums;
+    uint32_t *perm_b, *word_a, *word_b, *hist, *sums;
 };
 
 size_t scratch_layout(uint64_t n, char *base, Scratch *s)
@@ -170,6 +186,8 @@ size_t scratch_layout(uint64_t n, char *base, Scratch *s)
     };
     Scratch t;
     t.perm_b = take(std::max<uint64_t>(n, 1) * 4);
+    t.word_a = take(std::max<uint64_t>(n, 1) * 4);
+    t.word_b = take(std::max<uint64_t>(n, 1) * 4);
     t.hist = take(std::max<uint64_t>(m, 1) * 4);
     t.sums = take(std::max<uint64_t>(nsum, 1) * 4);
     if (s) *s = t;
@@ -212,22 +230,26 @@ int sdb_sort_rows(const void *const *keys, const int *key_types, const int *desc
     uint32_t *cur = perm, *nxt = sc.perm_b;
     for (int k = nkeys - 1; k >= 0; k--) {
         const int words = key_types[k] ? 2 : 1;
-        for (int w = 0; w < words; w++)
+        for (int w = 0; w < words; w++) {
+            const SortPass p{keys[k], key_types[k], w, descending[k] ? 1 : 0, 0};
+            uint32_t *wc = sc.word_a, *wn = sc.word_b;
+            k_gather_word<<<std::min<uint32_t>((n32 + 255) / 256, 4096), 256, 0, s>>>(p, cur, n32, wc);
+            sdb_count_launches(1);
             for (int shift = 0; shift < 32; shift += 8) {
-                SortPass p{keys[k], key_types[k], w, descending[k] ? 1 : 0, shift};
-                k_radix_count<<<nb, kSortThreads, 0, s>>>(p, cur, n32, sc.hist, nb);
+                k_radix_count<<<nb, kSortThreads, 0, s>>>(wc, shift, n32, sc.hist, nb);
                 k_scan_local<<<nsum, kScanThreads, 0, s>>>(sc.hist, m, sc.sums);
                 k_scan_sums<<<1, kScanThreads, 0, s>>>(sc.sums, nsum);
                 k_scan_add<<<nsum, kScanThreads, 0, s>>>(sc.hist, m, sc.sums);
-                k_radix_scatter<<<nb, kSortThreads, 0, s>>>(p, cur, n32, sc.hist, nb, nxt);
+                k_radix_scatter<<<nb, kSortThreads, 0, s>>>(wc, cur, shift, n32, sc.hist, nb, wn, nxt);
                 sdb_count_launches(4);  // the four launches before the checked one
                 st = sdb_check_launch("sdb_sort_rows");
                 if (st != SDB_OK) return st;
                 std::swap(cur, nxt);
+                std::swap(wc, wn);
             }
+        }
     }
-    // an even number of passes per key word set leaves the result in perm;
-    // every key has 4 or 8 passes, so it always ends there
+    // four passes per word leave the result in perm
     return SDB_OK;
 }
 
