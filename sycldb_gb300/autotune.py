@@ -57,14 +57,23 @@ def rows_bucket(n: int) -> int:
 
 
 def load(table: dict) -> int:
-    """Puts every entry of a tuning table into the library; returns how many."""
+    """Puts every entry of a tuning table into the library; returns how many.
+    A measured bucket's choice also holds for the unmeasured buckets above
+    it, up to the next measured one (the largest: up to the table's end), so
+    sizes between and beyond the measured ones take their nearest smaller
+    neighbour's variant instead of the library default."""
     L = capi.lib()
-    k = 0
-    for e in table.get("entries", []):
-        capi.check(L.sdb_chain_tune_set_op(TERMINALS[e["terminal"]], e["nregs"], e.get("first_op", -1),
-                                           1 << e["rows_bucket"], e["variant"]))
-        k += 1
-    return k
+    entries = table.get("entries", [])
+    by_key = {}
+    for e in entries:
+        by_key.setdefault((e["terminal"], e["nregs"], e.get("first_op", -1)), []).append(e)
+    for (term, nregs, first_op), es in by_key.items():
+        es = sorted(es, key=lambda e: e["rows_bucket"])
+        for i, e in enumerate(es):
+            hi = es[i + 1]["rows_bucket"] if i + 1 < len(es) else 40
+            for b in range(e["rows_bucket"], hi):
+                capi.check(L.sdb_chain_tune_set_op(TERMINALS[term], nregs, first_op, 1 << b, e["variant"]))
+    return len(entries)
 
 
 def load_default(path: Optional[str] = None) -> Optional[dict]:

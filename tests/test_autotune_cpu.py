@@ -45,3 +45,25 @@ def test_first_op_keys_are_separate():
     finally:
         capi.force_chain_variant(-1)
         autotune.load_default()
+
+
+def test_measured_buckets_cover_the_sizes_above_them(tmp_path):
+    """A measured bucket's variant holds up to the next measured bucket of
+    the same key, and the largest one's for every size above it."""
+    L = capi.lib()
+    table = {"entries": [{"terminal": "groupby", "nregs": 2, "first_op": 3, "rows_bucket": 22, "variant": 5},
+                         {"terminal": "groupby", "nregs": 2, "first_op": 3, "rows_bucket": 24, "variant": 7},
+                         {"terminal": "groupby", "nregs": 2, "first_op": 1, "rows_bucket": 26, "variant": 6}]}
+    p = tmp_path / "t.json"
+    p.write_text(json.dumps(table))
+    try:
+        capi.force_chain_variant(-1)
+        autotune.load_default(str(p))
+        assert L.sdb_chain_tune_get_op(2, 2, 3, 1 << 22) == 5
+        assert L.sdb_chain_tune_get_op(2, 2, 3, 1 << 23) == 5   # between 22 and 24
+        assert L.sdb_chain_tune_get_op(2, 2, 3, 1 << 24) == 7
+        assert L.sdb_chain_tune_get_op(2, 2, 3, 1 << 28) == 7   # beyond the largest measured size
+        assert L.sdb_chain_tune_get_op(2, 2, 1, 1 << 30) == 6   # another first op keeps its own
+    finally:
+        capi.force_chain_variant(-1)
+        autotune.load_default()
