@@ -607,8 +607,9 @@ def run_widened(args, rank, stream, peak):
         best = min(times)
         nbytes = 4 * len(lcols) * ln
         out["load_dir"] = {"bytes": nbytes, "s": best, "gbs": nbytes / best / 1e9,
-                           "note": "%d lineorder columns of %d rows from files in the page cache, 32 MB "
-                                   "double-buffered pinned chunks, min/max on the device; best of 3" %
+                           "note": "%d lineorder columns of %d rows from files in the page cache, 8 MB chunks "
+                                   "read by 4 threads (two pinned buffers each), min/max on the device; "
+                                   "best of 3" %
                                    (len(lcols), ln)}
     finally:
         shutil.rmtree(d, ignore_errors=True)

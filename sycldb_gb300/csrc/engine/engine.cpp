@@ -35,6 +35,14 @@
 #include <unordered_map>
 #include <vector>
 
+#include <fcntl.h>
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include <atomic>
+#include <mutex>
+#include <thread>
+
 #include <cuda_runtime.h>
 
 #include "batch_api.hpp"
@@ -1718,12 +1726,13 @@ void activate_table(Engine &E, const std::string &name)
 // new device buffers, and computes per-segment min/max.  Only the columns of
 // `mask` (bit i = column i) are read; the row count is the first read
 // column's; a missing file or one of another length leaves that column
-// unloaded, as the reference does.  File reads of 32 MB chunks alternate
-// between two pinned buffers so that reading overlaps the copies.
+// unloaded, as the reference does.  The files are read in 8 MB chunks by
+// several threads, each alternating between two pinned buffers so that its
+// reads overlap its copies; the chunks go to the device on one stream.
 std::unique_ptr<Table> load_columns(const std::string &dir, const std::string &name, int ncols, uint64_t mask,
                                     uint64_t seg_rows, cudaStream_t s, std::vector<std::string> *warnings)
 {
-    constexpr size_t kChunk = 32u << 20;
+    constexpr size_t kChunk = 8u << 20;
     std::string upper = base_name(name);
     std::transform(upper.begin(), upper.end(), upper.begin(), [](unsigned char ch) { return (char)std::toupper(ch); });
     std::string prefix = dir;
@@ -1732,57 +1741,120 @@ std::unique_ptr<Table> load_columns(const std::string &dir, const std::string &n
     t->name = name;
     t->columns.resize(ncols);
     bool nrows_set = false;
-    char *pin[2] = {nullptr, nullptr};
-    cudaEvent_t done[2] = {nullptr, nullptr};
-    auto cleanup = [&]() {
-        for (int b = 0; b < 2; b++) {
-            if (done[b]) cudaEventSynchronize(done[b]), cudaEventDestroy(done[b]);
-            if (pin[b]) cudaFreeHost(pin[b]);
-        }
+    int device = 0;
+    SDB_CUDA(cudaGetDevice(&device));
+    struct Job {
+        int fd;
+        uint64_t off;
+        size_t len;
+        char *dst;
+    };
+    std::vector<int> fds;
+    std::vector<Job> jobs;
+    auto close_fds = [&]() {
+        for (int fd : fds) close(fd);
+        fds.clear();
     };
     std::vector<std::pair<int, int32_t *>> dev_cols;
     try {
-        for (int b = 0; b < 2; b++) {
-            SDB_CUDA(cudaHostAlloc(reinterpret_cast<void **>(&pin[b]), kChunk, cudaHostAllocDefault));
-            SDB_CUDA(cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming));
-        }
-        int b = 0;
         for (int c = 0; c < ncols && c < 64; c++) {
             if (!((mask >> c) & 1u)) continue;
             const std::string file = prefix + upper + std::to_string(c);
-            std::ifstream in(file, std::ios::binary | std::ios::ate);
-            if (!in) {
+            const int fd = open(file.c_str(), O_RDONLY);
+            if (fd < 0) {
                 if (warnings) warnings->push_back("column file missing: " + file);
                 continue;
             }
-            const uint64_t bytes = (uint64_t)in.tellg();
+            struct stat stt;
+            if (fstat(fd, &stt) != 0) {
+                close(fd);
+                throw Error(SDB_ERR_INVALID, "cannot stat " + file);
+            }
+            const uint64_t bytes = (uint64_t)stt.st_size;
             const uint64_t n = bytes / sizeof(int32_t);
             if (!nrows_set) {
-                if (n == 0) throw Error(SDB_ERR_INVALID, "empty column file " + file);
+                if (n == 0) {
+                    close(fd);
+                    throw Error(SDB_ERR_INVALID, "empty column file " + file);
+                }
                 t->nrows = n;
                 nrows_set = true;
             }
             if (n != t->nrows || bytes % sizeof(int32_t)) {
+                close(fd);
                 if (warnings)
                     warnings->push_back("column length mismatch in " + file + ": expected " + std::to_string(t->nrows) +
                                         ", got " + std::to_string(n));
                 continue;
             }
-            in.seekg(0);
+            fds.push_back(fd);
             int32_t *d = nullptr;
             SDB_CUDA(cudaMalloc(&d, bytes));
             t->owned.push_back(d);
-            for (uint64_t off = 0; off < bytes; off += kChunk) {
-                const size_t len = (size_t)std::min<uint64_t>(kChunk, bytes - off);
-                SDB_CUDA(cudaEventSynchronize(done[b]));  // the buffer's previous copy is done
-                if (!in.read(pin[b], (std::streamsize)len)) throw Error(SDB_ERR_INVALID, "read failed: " + file);
-                SDB_CUDA(cudaMemcpyAsync(reinterpret_cast<char *>(d) + off, pin[b], len, cudaMemcpyHostToDevice, s));
-                SDB_CUDA(cudaEventRecord(done[b], s));
-                b ^= 1;
-            }
+            for (uint64_t off = 0; off < bytes; off += kChunk)
+                jobs.push_back({fd, off, (size_t)std::min<uint64_t>(kChunk, bytes - off), reinterpret_cast<char *>(d) + off});
             dev_cols.emplace_back(c, d);
         }
         if (!nrows_set) throw Error(SDB_ERR_INVALID, "no column file of table " + name + " under " + dir);
+        // readers: each takes the next chunk, reads it into one of its two
+        // pinned buffers (once that buffer's previous copy is done) and
+        // queues the copy
+        const unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+        const size_t nthreads = std::max<size_t>(1, std::min<size_t>({(size_t)4, (size_t)hw, jobs.size()}));
+        std::atomic<size_t> next{0};
+        std::mutex err_mu;
+        std::string err;
+        auto reader = [&]() {
+            char *pin[2] = {nullptr, nullptr};
+            cudaEvent_t done[2] = {nullptr, nullptr};
+            auto fail = [&](const std::string &m) {
+                std::lock_guard<std::mutex> g(err_mu);
+                if (err.empty()) err = m;
+            };
+            bool ok = cudaSetDevice(device) == cudaSuccess;
+            for (int b = 0; b < 2 && ok; b++)
+                ok = cudaHostAlloc(reinterpret_cast<void **>(&pin[b]), kChunk, cudaHostAllocDefault) == cudaSuccess &&
+                     cudaEventCreateWithFlags(&done[b], cudaEventDisableTiming) == cudaSuccess;
+            if (!ok) fail("load_dir: pinned staging or event");
+            int b = 0;
+            for (size_t j = next++; ok && j < jobs.size(); j = next++) {
+                {
+                    std::lock_guard<std::mutex> g(err_mu);
+                    if (!err.empty()) break;
+                }
+                const Job &jb = jobs[j];
+                if (cudaEventSynchronize(done[b]) != cudaSuccess) {  // the buffer's previous copy is done
+                    fail("load_dir: copy failed");
+                    break;
+                }
+                size_t got = 0;
+                while (got < jb.len) {
+                    const ssize_t r = pread(jb.fd, pin[b] + got, jb.len - got, (off_t)(jb.off + got));
+                    if (r <= 0) break;
+                    got += (size_t)r;
+                }
+                if (got != jb.len) {
+                    fail("load_dir: read failed");
+                    break;
+                }
+                if (cudaMemcpyAsync(jb.dst, pin[b], jb.len, cudaMemcpyHostToDevice, s) != cudaSuccess ||
+                    cudaEventRecord(done[b], s) != cudaSuccess) {
+                    fail("load_dir: copy failed");
+                    break;
+                }
+                b ^= 1;
+            }
+            for (int q = 0; q < 2; q++) {
+                if (done[q]) cudaEventSynchronize(done[q]), cudaEventDestroy(done[q]);
+                if (pin[q]) cudaFreeHost(pin[q]);
+            }
+        };
+        std::vector<std::thread> pool;
+        for (size_t i = 1; i < nthreads; i++) pool.emplace_back(reader);
+        reader();
+        for (auto &th : pool) th.join();
+        close_fds();
+        if (!err.empty()) throw Error(SDB_ERR_INVALID, err);
         // Segment statistics (models/models.hpp:71-77), on the device.
         auto sg = split_rows(t->nrows, seg_rows);
         const size_t nmm = dev_cols.size() * sg.size() * 2;
@@ -1815,12 +1887,11 @@ std::unique_ptr<Table> load_columns(const std::string &dir, const std::string &n
             }
         }
     } catch (...) {
-        cleanup();
+        close_fds();
         cudaStreamSynchronize(s);
         for (auto p : t->owned) cudaFree(p);
         throw;
     }
-    cleanup();
     return t;
 }
 
