@@ -29,6 +29,13 @@ to result rows in host memory.
              server (continuous batching, 60 GB admission budget) and through
              the plain one-at-a-time path: queries/s and p50/p99 latency per
              arrival rate, results compared request by request
+  widened    the SSB flight-3 and flight-4 shapes at SF20 (rows/s, fused-pass
+             roofline), device ORDER BY throughput and the columnar loader
+             (--no-widened skips it)
+  gpu_launches  kernels of the prepared plan's graph x steps
+
+--unfused measures the operator-at-a-time path (one kernel per reference
+operator) instead of the fused one.
 
 --impl reference times the reference path's CPU restatement (the oracle port:
 the reference itself needs AdaptiveCpp, oneDPL and Thrift and cannot be built
