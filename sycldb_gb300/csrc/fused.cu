@@ -770,9 +770,9 @@ constexpr uint32_t kDenseCap = 512;
 
 // Tile rows are staged in shared memory by cp.async: thread t's four rows
 // (tile + 4t .. 4t + 3) of every chain column arrive as one 16-byte copy per
-// column into a kStages-deep ring, issued kStages - 1 tiles ahead.  Each
-// thread reads back only what it copied, so no block barrier is needed.
-constexpr int kMaxStages = 3;
+// column into a ring of STAGES (2 or 3) stages, issued STAGES - 1 tiles
+// ahead.  Each thread reads back only what it copied, so no block barrier is
+// needed.
 
 __device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint32_t src_bytes)
 {
@@ -1882,7 +1882,7 @@ std::atomic<int> &tune_entry(int term, int nregs, int opc, uint64_t rows)
 int default_variant(int nregs) { return nregs <= 4 ? 1 : 0; }
 
 constexpr int kDenseVariant = 3;
-constexpr int kCompactVariant = 4;
+[[maybe_unused]] constexpr int kCompactVariant = 4;  // compacted, 3-stage ring
 constexpr int kCompact2Variant = 5;  // as 4 with a 2-stage copy ring
 constexpr int kCarryVariant = 6;     // as 5, compacted rows carried across tiles
 constexpr int kLevel2Variant = 7;    // as 6, plus a second compaction after the first row-per-lane op

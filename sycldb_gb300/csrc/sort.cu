@@ -34,7 +34,6 @@ struct SortPass {
     int wide;         // 1: uint64 column
     int hi;           // uint64: high word
     int desc;
-    int shift;
 };
 
 __device__ __forceinline__ uint32_t key_word(const SortPass &p, uint32_t row)
@@ -231,7 +230,7 @@ int sdb_sort_rows(const void *const *keys, const int *key_types, const int *desc
     for (int k = nkeys - 1; k >= 0; k--) {
         const int words = key_types[k] ? 2 : 1;
         for (int w = 0; w < words; w++) {
-            const SortPass p{keys[k], key_types[k], w, descending[k] ? 1 : 0, 0};
+            const SortPass p{keys[k], key_types[k], w, descending[k] ? 1 : 0};
             uint32_t *wc = sc.word_a, *wn = sc.word_b;
             k_gather_word<<<std::min<uint32_t>((n32 + 255) / 256, 4096), 256, 0, s>>>(p, cur, n32, wc);
             sdb_count_launches(1);
