@@ -208,3 +208,37 @@ def test_chain_specialised_is_a_host_query():
     d.n_ops = 2
     d.flags_out = 0  # a flags chain without flags_out is invalid
     assert L.sdb_chain_specialised(ctypes.byref(d)) == capi.SDB_ERR_INVALID
+
+
+def test_plan_order_matches_the_oracle_for_every_shape():
+    """The engine's DAG order (operations/preprocessing.cpp:14-102, lineorder
+    scans deferred) equals the oracle restatement's for every plan builder."""
+    from oracle import oracle as O
+
+    L = capi.lib()
+    shapes = [plans.plan_filter_sum(1994), plans.plan_date_join(1995), plans.plan_star(2, 11),
+              plans.plan_star(1, 3, 1993, 1996, 12), plans.plan_customer_supplier_date(2),
+              plans.plan_customer_supplier_date(0, 1992, 1998, city_points=(21, 27)),
+              plans.plan_profit(1), plans.plan_profit(3, (2, 4))]
+    for p in shapes:
+        n = ctypes.c_int()
+        order = (ctypes.c_int * 64)()
+        capi.check(L.sdb_plan_check(json.dumps(p).encode(), ctypes.byref(n), order, 64))
+        assert list(order[:n.value]) == O.dag_topological_sort(p["rels"]), json.dumps(p)
+
+
+def test_plan_check_rejects_malformed_graphs():
+    """A FILTER with no node before it, a JOIN without two inputs or with an
+    input out of range: the plan is refused on the host, with a message."""
+    L = capi.lib()
+    scan = {"id": 0, "relOp": "TABLE_SCAN", "tables": ["ssb", "part"]}
+    bad = [
+        {"rels": [{"id": 0, "relOp": "FILTER", "condition": {"exprType": "LITERAL"}}]},
+        {"rels": [scan, {"id": 1, "relOp": "JOIN", "inputs": [0], "joinType": "inner",
+                         "condition": {"exprType": "EXPR", "op": "=", "operands": []}}]},
+        {"rels": [scan, {"id": 1, "relOp": "JOIN", "inputs": [0, 7], "joinType": "inner",
+                         "condition": {"exprType": "EXPR", "op": "=", "operands": []}}]},
+    ]
+    for p in bad:
+        assert L.sdb_plan_check(json.dumps(p).encode(), None, None, 0) == capi.SDB_ERR_INVALID, json.dumps(p)
+        assert capi.last_error()
