@@ -101,6 +101,12 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--sf", type=float, default=SF)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-configs", action="store_true",
+                    help="skip the SF1 configurations (filter-project-sum, date join + group-by)")
+    ap.add_argument("--only", default="", choices=["", "configs"],
+                    help="run one section alone (for profiling): configs")
+    ap.add_argument("--config-copies", type=int, default=8,
+                    help="copies of the SF1 fact columns the configs section rotates through (L2 defeat)")
     ap.add_argument("--no-widened", action="store_true",
                     help="skip the widened rows (flight-3 / flight-4 shapes, device ORDER BY, columnar loader)")
     ap.add_argument("--unfused", action="store_true",
@@ -235,28 +241,81 @@ def dims_host(sf):
 
 
 # ---------------------------------------------------------------------- CPU
-def cpu_oracle_run(sample_rows: int, sf: float, steps: int, warmup: int, salt: int = 0):
-    """The oracle on the first `sample_rows` fact rows; returns rows/s, threads."""
+# The CPU leg: the oracle (operator-at-a-time C/OpenMP restatement of the
+# reference executor) over the same seeded inputs, generated by the oracle's
+# own generator, so that this leg loads nothing of the native library.  It
+# runs the whole workload (no sampling) with the step/warm-up counts of the
+# GPU arm: W untimed repetitions, then K timed ones (the reference's own
+# method is 10 repetitions with the first dropped, common.hpp:5,
+# app/application.cpp:37-48).
+
+CPU_CONFIGS = {
+    # name -> (plan builder, fact column key, SF, dimensions read)
+    "filter_project_sum_sf1": (_plan_filter_sum, "q1", 1.0, ()),
+    "date_join_groupby_sf1": (_plan_date_join, "q2", 1.0, ("ddate",)),
+}
+
+
+def cpu_oracle_time(plan: dict, fact: dict, dims: dict, steps: int, warmup: int):
+    """Times the oracle executor on one plan; returns (per-step seconds of the
+    timed steps, canonical result rows, threads)."""
+    from oracle import oracle as O
+
+    tables = {"lineorder": O.make_table("lineorder", fact)}
+    for t, cols in dims.items():
+        tables[t] = O.make_table(t, cols)
+    ex = O.OracleExecutor(tables)
+    res = None
+    for _ in range(warmup):
+        res = ex.execute(plan)
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        res = ex.execute(plan)
+        times.append(time.perf_counter() - t0)
+    return times, O.canonical_rows(res), O.lib().o_num_threads()
+
+
+def cpu_workload(sf: float, cols, dim_names):
+    """Seeded fact and dimension columns from the oracle's generator."""
     from oracle import build_oracle
 
     build_oracle.build_oracle()
     from oracle import oracle as O
-    from sycldb_gb300 import plans, ssb
+    from sycldb_gb300 import ssb
 
-    fact = ssb.gen_lineorder_host(sample_rows, ssb.QUERY_COLUMNS["star"], sf, salt=salt)
-    dims = dims_host(sf)
-    tables = {"lineorder": O.make_table("lineorder", fact)}
-    for t, cols in dims.items():
-        tables[t] = O.make_table(t, cols)
-    plan = plans.plan_star(REGION, CATEGORY)
-    ex = O.OracleExecutor(tables)
-    for _ in range(warmup):
-        ex.execute(plan)
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        ex.execute(plan)
-    dt = time.perf_counter() - t0
-    return sample_rows * steps / dt, O.lib().o_num_threads(), dt / steps * 1e3
+    gen = O.OracleGen()
+    fact = ssb.gen_lineorder_host(ssb.fact_rows(sf), cols, sf, gen=gen)
+    dims = ssb.gen_dims(sf, gen=gen)
+    return fact, {t: dims[t] for t in dim_names}
+
+
+def _cpu_line(n: int, times, cores: int):
+    mean = sum(times) / len(times)
+    return {"value": n / mean, "unit": UNIT, "ms_per_step": mean * 1e3,
+            "ms_median": statistics.median(times) * 1e3, "cores": cores, "kind": "port"}
+
+
+def cpu_reference_all(sf: float, steps: int, warmup: int, configs: bool = True):
+    """The headline star join at full size, then (configs) the SF1
+    configurations; every result's canonical rows are returned with it."""
+    from sycldb_gb300 import ssb
+
+    n = ssb.fact_rows(sf)
+    fact, dims = cpu_workload(sf, ssb.QUERY_COLUMNS["star"], ("supplier", "part", "ddate"))
+    times, rows, cores = cpu_oracle_time(_plan_star(), fact, dims, steps, warmup)
+    main = _cpu_line(n, times, cores)
+    main["rows"] = rows
+    del fact
+    out = {}
+    if configs:
+        for name, (builder, key, csf, dnames) in CPU_CONFIGS.items():
+            cn = ssb.fact_rows(csf)
+            cfact, cdims = cpu_workload(csf, ssb.QUERY_COLUMNS[key], dnames)
+            ct, crows, _ = cpu_oracle_time(builder(), cfact, cdims, steps, warmup)
+            out[name] = _cpu_line(cn, ct, cores)
+            out[name]["rows"] = crows
+    return main, out
 
 
 def run_reference(args, rank, world, pg):
@@ -264,22 +323,65 @@ def run_reference(args, rank, world, pg):
         return 0
     from sycldb_gb300 import ssb
 
-    n_full = ssb.fact_rows(args.sf)
-    sample = max(1, n_full // 16)
-    value, cores, ms = cpu_oracle_run(sample, args.sf, args.steps, args.warmup)
+    n = ssb.fact_rows(args.sf)
+    main, cfgs = cpu_reference_all(args.sf, args.steps, args.warmup, configs=not args.no_configs)
+    sample = ("the whole workload per step (%d fact rows, full dimensions): %d untimed repetitions, then %d "
+              "timed; inputs from the oracle's own seeded generator" % (n, args.warmup, args.steps))
     line = {
-        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "int32/uint64", "data": "synthetic",
-        "config": {"workload": workload_name(args.sf), "sample_fact_rows": sample},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": "first %d of %d fact rows per step (1/16), full dimensions" % (sample, n_full)},
-        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "impl": "reference", "metric": METRIC, "value": main["value"], "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": main["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "int32/uint64", "data": DATA,
+        "config": workload_config(args.sf, len(main["rows"])),
+        "cpu_baseline": {"value": main["value"], "unit": UNIT, "cores": main["cores"], "kind": "port",
+                         "sample": sample, "ms_median": main["ms_median"]},
+        "e2e": {"value": main["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "configs": {k: {kk: vv for kk, vv in v.items() if kk != "rows"} for k, v in cfgs.items()},
+        "result_digests": {"star": rows_digest(main["rows"]), **{k: rows_digest(v["rows"]) for k, v in cfgs.items()}},
         "note": "CPU restatement of the reference executor (oracle port: C/OpenMP kernels, operator at a "
-                "time); the reference's SYCL CPU path needs AdaptiveCpp, oneDPL and Thrift, absent here",
+                "time, all host threads); the reference's SYCL CPU path needs AdaptiveCpp, oneDPL and Thrift, "
+                "absent here",
     }
     print(json.dumps(line), flush=True)
     return 0
+
+
+def cpu_baseline_child(args):
+    """Runs the CPU leg in a child process (its own address space, before
+    the GPU work) and returns its JSON line, or None."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--impl", "reference", "--steps", str(args.steps),
+           "--warmup", str(max(1, args.warmup)), "--sf", str(args.sf)]
+    if args.no_configs:
+        cmd.append("--no-configs")
+    env = dict(os.environ)
+    for k in ("RANK", "WORLD_SIZE", "LOCAL_RANK", "MASTER_ADDR", "MASTER_PORT"):
+        env.pop(k, None)
+    r = subprocess.run(cmd, capture_output=True, text=True, env=env, timeout=1800)
+    for line in r.stdout.splitlines():
+        if line.startswith("{"):
+            return json.loads(line)
+    print("cpu baseline leg failed (rc %d): %s" % (r.returncode, r.stderr[-2000:]), file=sys.stderr)
+    return None
+
+
+DATA = "synthetic (seeded SplitMix64 columns, SSB SF20 shapes)"
+
+
+def rows_digest(rows) -> str:
+    """SHA-256 of canonical result rows (sorted tuples of ints): what the two
+    arms compare."""
+    import hashlib
+
+    return hashlib.sha256(json.dumps([list(map(int, r)) for r in rows]).encode()).hexdigest()
+
+
+def workload_config(sf, groups):
+    """The workload part of the bench line's config, the same in both arms."""
+    from sycldb_gb300 import ssb
+
+    n = ssb.fact_rows(sf)
+    return {"workload": workload_name(sf), "fact_rows_per_gpu": n, "groups": groups,
+            "l2": "inputs larger than L2 (%.2f GB of fact columns per step)" % (16 * n / 1e9),
+            "parallelism": "1 GPU"}
 
 
 def workload_name(sf):
@@ -297,6 +399,16 @@ def run_ours(args, rank, world, local, pg):
     build.build()
     torch.cuda.set_device(local)
     from sycldb_gb300.engine import Engine
+
+    # the CPU leg first, in a child process, before any device work
+    ref = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and args.plan == "star":
+        ref = cpu_baseline_child(args)
+    if args.only == "configs":
+        out = run_configs(args, rank, torch.cuda.Stream(), measured_peaks()[0], ref)
+        if rank == 0:
+            print(json.dumps({"configs": out}), flush=True)
+        return 0
 
     L = capi.lib()
     sf = args.sf
@@ -354,6 +466,7 @@ def run_ours(args, rank, world, local, pg):
     for _ in range(max(3, args.warmup)):
         res = eng.execute(plan)
     assert res.nrows == n_groups
+    star_rows = res.canonical()
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -400,21 +513,29 @@ def run_ours(args, rank, world, local, pg):
     eng.close()
     del fact
     torch.cuda.empty_cache()
+    configs = run_configs(args, rank, stream, peak, ref) if not args.no_configs else None
     batched = run_batched(args, rank, world, local, pg, stream, peak) if args.batched_runs > 0 else None
     served = run_served(args, rank, world, local, pg, stream) if args.served_rates.strip() else None
     widened = run_widened(args, rank, stream, peak) if not args.no_widened else None
 
+    if args.plan == "star":
+        config = workload_config(sf, n_groups)
+        if world > 1:
+            config["parallelism"] = "replicas"
+    else:
+        config = {"workload": "%s plan, SF%g (%d fact rows)" % (args.plan, sf, n), "fact_rows_per_gpu": n,
+                  "groups": n_groups, "l2": "inputs larger than L2 (%.2f GB of fact columns per step)" %
+                  (alg_bytes / 1e9), "parallelism": "replicas" if world > 1 else "1 GPU"}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "int32/uint64", "data": "synthetic (seeded SplitMix64 columns, SSB SF20 shapes)",
-        "config": {"workload": workload_name(sf) if args.plan == "star" else "%s plan, SF%g (%d fact rows)" % (
-                       args.plan, sf, n), "fact_rows_per_gpu": n, "groups": n_groups,
-                   "l2": "inputs larger than L2 (%.2f GB of fact columns per step)" % (alg_bytes / 1e9),
-                   "segment_rows": 1 << 28, "fused": fuse, "parallelism": "replicas" if world > 1 else "1 GPU",
+        "vs_baseline": None, "dtype": "int32/uint64", "data": DATA,
+        "config": config,
+        "engine": {"segment_rows": 1 << 28, "fused": fuse,
                    "plan_cache": "on: steps 2.. replay the prepared plan as one CUDA graph (all kernels run)",
                    "plain_path_ms_per_step": plain_ms_per_step},
         "roofline": roof,
+        "configs": configs,
         "e2e": e2e,
         "batched": batched,
         "served": served,
@@ -426,14 +547,115 @@ def run_ours(args, rank, world, local, pg):
         "kernel_ms_last_step": {k: v[1] for k, v in stats_last.items()},
         "clocks": clk,
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        sample = max(1, n // 16)
-        v, cores, _ = cpu_oracle_run(sample, sf, steps=3, warmup=1)
-        line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
-                                "sample": "3 runs on the first %d of %d fact rows (1/16), full dimensions" % (sample, n)}
+    if ref is not None:
+        cb = dict(ref["cpu_baseline"])
+        cb["bit_exact_vs_gpu"] = rows_digest(star_rows) == ref["result_digests"]["star"]
+        line["cpu_baseline"] = cb
     if rank == 0:
         print(json.dumps(line), flush=True)
     return 0
+
+
+def run_configs(args, rank, stream, peak, ref):
+    """The SF1 configurations (6 M fact rows): filter-project-sum and filter +
+    date join + group-by by year.  The fact columns (72-96 MB) would stay in
+    the 126 MB L2 from one step to the next, so the section keeps
+    ``--config-copies`` copies of them in separate buffers (768 MB for the
+    filter-project-sum) and step i runs on copy i mod copies: every step
+    reads its columns from HBM.  Per configuration: rows/s through the
+    prepared plans (CUDA events over K steps), the fused kernel's time per
+    launch from the plain path (CUDA events around each launch) and its
+    roofline over the referenced fact columns, and the CPU leg's time and
+    result on the same inputs."""
+    import torch
+
+    from sycldb_gb300 import ssb
+    from sycldb_gb300.engine import Engine
+
+    out = {}
+    copies = max(1, args.config_copies)
+    for name, (builder, key, csf, dnames) in CPU_CONFIGS.items():
+        n = ssb.fact_rows(csf)
+        cols = ssb.QUERY_COLUMNS[key]
+        base = ssb.gen_lineorder_device(n, cols, csf, salt=rank)
+        tabs = [{c: base[c].clone() for c in cols} for _ in range(copies)]
+        del base
+        dims = ssb.gen_dims(csf)
+        pls = [_with_fact_tag(builder, i) for i in range(copies)]
+        torch.cuda.synchronize()
+
+        def loaded(**kw):
+            e = Engine(fuse=True, stream=stream.cuda_stream, **kw)
+            for i, t in enumerate(tabs):
+                e.load_table("lineorder@%d" % i, t)
+            for d in dnames:
+                e.load_table(d, dims[d])
+            return e
+
+        # the fused kernel's time per launch (plain path, every launch timed)
+        peng = loaded(profile=True)
+        for i in range(copies * 2):
+            peng.execute(pls[i % copies])
+        kms, kn, prof = 0.0, 0, max(copies * 3, min(args.steps, 64))
+        for i in range(prof):
+            peng.execute(pls[i % copies])
+            st = peng.kernel_stats()
+            if "fused_chain" in st:
+                kn += st["fused_chain"][0]
+                kms += st["fused_chain"][1]
+        peng.close()
+        # rows/s through the prepared plans
+        eng = loaded(plan_cache=copies + 2)
+        rows = None
+        for _ in range(max(3, args.warmup)):
+            for p in pls:
+                rows = eng.execute(p).canonical()
+        exact_copies = all(eng.execute(p).canonical() == rows for p in pls)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(args.steps):
+            eng.execute(pls[i % copies])
+        e1.record(stream)
+        e1.synchronize()
+        eng.close()
+        ms = e0.elapsed_time(e1) / args.steps
+        alg = 4 * len(cols) * n
+        per = kms / max(1, kn)
+        ach = alg / (per / 1e3) / 1e9 if kn else None
+        entry = {
+            "workload": "%s: %d fact rows x %d int32 columns (%s)" % (name, n, len(cols), ", ".join(
+                "lo_col%d" % c for c in cols)),
+            "rows_per_s": n / (ms / 1e3), "ms_per_step": ms, "steps": args.steps, "groups": len(rows),
+            "l2": "%d copies of the fact columns (%.0f MB), step i reads copy i mod %d: inputs not L2-resident "
+                  "between steps" % (copies, copies * alg / 1e6, copies),
+            "roofline": {"kernel": "k_dense (fused chain)", "bound": "hbm", "achieved": ach, "peak": peak,
+                         "unit": "GB/s", "frac": (ach / peak) if ach else None, "launch_ms": per,
+                         "launches": kn, "algorithmic_bytes_per_launch": alg,
+                         "timing": "CUDA events around each fused-pass launch, %d plain-path steps" % prof},
+            "same_rows_every_copy": exact_copies,
+        }
+        if ref is not None and name in (ref.get("configs") or {}):
+            cb = dict(ref["configs"][name])
+            cb["sample"] = "the whole workload, %d untimed + %d timed repetitions" % (max(1, args.warmup),
+                                                                                       args.steps)
+            cb["bit_exact_vs_gpu"] = rows_digest(rows) == ref["result_digests"][name]
+            entry["cpu_baseline"] = cb
+        out[name] = entry
+        del tabs
+        torch.cuda.empty_cache()
+    return out
+
+
+def _with_fact_tag(builder, tag):
+    """The configuration's plan over fact table lineorder@tag."""
+    from sycldb_gb300 import plans
+
+    p = builder()
+    for r in p["rels"]:
+        if r.get("relOp") == "TABLE_SCAN" and r["tables"][-1] == "lineorder":
+            r["tables"] = list(r["tables"][:-1]) + ["lineorder@%d" % tag]
+    return p
 
 
 def run_e2e(args, eng, plan, n, cols, sf, rank, stream, pg):

@@ -177,9 +177,11 @@ int sdb_compact_row_ids(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t
  * segment); larger n is refused with SDB_ERR_INVALID.  The first call on a
  * device looks up that array's device address (a one-time set-up per device,
  * done with the device current); make that first call before any stream
- * capture.  All calls on a device share the array, so calls that overlap on
- * the GPU (different streams, no ordering between them) race and must not be
- * issued.  It calls no allocator. */
+ * capture.  The address is kept for the rest of the process: a device reset
+ * (cudaDeviceReset) after the first call is not supported, since it rebuilds
+ * the context and the array may move.  All calls on a device share the
+ * array, so calls that overlap on the GPU (different streams, no ordering
+ * between them) race and must not be issued.  It calls no allocator. */
 #define SDB_COMPACT_NOALLOC_MAX_ROWS 268435456ull
 int sdb_compact_row_ids_noalloc(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t *count,
                                 sdb_stream_t stream);

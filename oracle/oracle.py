@@ -147,6 +147,9 @@ def lib():
             "o_count_flags": (ctypes.c_uint64, [_P_U8, u64]),
             "o_min_max": (None, [_P_I32, u64, _P_I32, _P_I32]),
             "o_num_threads": (ctypes.c_int, []),
+            "o_gen_uniform": (None, [_P_I32, u64, u64, u64, u64, i32, i32]),
+            "o_gen_dates": (None, [_P_I32, u64, u64, u64, u64, i32]),
+            "o_gen_datekeys": (None, [_P_I32, u64, ctypes.c_int64]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -154,6 +157,30 @@ def lib():
             fn.argtypes = args
         _LIB = L
     return _LIB
+
+
+class OracleGen:
+    """The seeded column generator restated in sdb_oracle.c, with the
+    interface of ``sycldb_gb300.ssb.LibGen``: the CPU legs of the benchmark
+    generate their inputs with it and load nothing of the native library."""
+
+    @staticmethod
+    def _dst(a: np.ndarray, n: int):
+        assert a.dtype == np.int32 and a.size >= n and a.flags["C_CONTIGUOUS"]
+        return _p(a, ctypes.c_int32)
+
+    def uniform(self, a, n, row0, seed, sid, lo, hi):
+        if hi < lo:
+            raise ValueError("uniform: hi < lo")
+        lib().o_gen_uniform(self._dst(a, n), n, row0, seed, sid, lo, hi)
+
+    def dates(self, a, n, row0, seed, sid, ndays):
+        if ndays < 1:
+            raise ValueError("dates: ndays < 1")
+        lib().o_gen_dates(self._dst(a, n), n, row0, seed, sid, ndays)
+
+    def datekeys(self, a, n, day0):
+        lib().o_gen_datekeys(self._dst(a, n), n, day0)
 
 
 def _p(a: np.ndarray, ctype):

@@ -394,3 +394,77 @@ int o_num_threads(void)
     return 1;
 #endif
 }
+
+/* ------------------------------------------------------------------------
+ * Seeded synthetic columns, restated for the CPU legs of the benchmark so
+ * that they need nothing of the product library.  Each value depends only on
+ * (seed, stream, row): a SplitMix64 finaliser (Steele, Lea, Flood, "Fast
+ * splittable pseudorandom number generators", OOPSLA 2014) of the row added
+ * to a per-stream key, scaled to [lo, hi] by a 32x32 multiply-shift of its
+ * high half.  Dates are days counted from 1992-01-01, encoded YYYYMMDD with
+ * the days-to-civil conversion of H. Hinnant ("chrono-Compatible Low-Level
+ * Date Algorithms").  The tests check these columns bit for bit against the
+ * library's own generator.
+ * ------------------------------------------------------------------------ */
+static inline uint64_t o_mix64(uint64_t z)
+{
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+static inline uint64_t o_stream_key(uint64_t seed, uint64_t stream)
+{
+    return o_mix64(seed ^ (stream * 0xD1B54A32D192ED03ull));
+}
+
+static inline int32_t o_uniform(uint64_t key, uint64_t row, int32_t lo, int32_t hi)
+{
+    const uint64_t r = o_mix64(key + row) >> 32;
+    const uint64_t span = (uint64_t)((int64_t)hi - (int64_t)lo) + 1u;
+    return (int32_t)((int64_t)lo + (int64_t)((r * span) >> 32));
+}
+
+/* days since 1970-01-01 -> YYYYMMDD (proleptic Gregorian) */
+static inline int32_t o_yyyymmdd(int64_t z)
+{
+    int64_t era, doe, yoe, doy, mp, y, m, d;
+    z += 719468;
+    era = (z >= 0 ? z : z - 146096) / 146097;
+    doe = z - era * 146097;
+    yoe = (doe - doe / 1460 + doe / 36524 - doe / 146096) / 365;
+    doy = doe - (365 * yoe + yoe / 4 - yoe / 100);
+    mp = (5 * doy + 2) / 153;
+    d = doy - (153 * mp + 2) / 5 + 1;
+    m = mp < 10 ? mp + 3 : mp - 9;
+    y = yoe + era * 400 + (m <= 2 ? 1 : 0);
+    return (int32_t)(y * 10000 + m * 100 + d);
+}
+
+#define O_DAY_1992 8035 /* 1992-01-01 in days since 1970-01-01 */
+
+void o_gen_uniform(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, uint64_t stream, int32_t lo, int32_t hi)
+{
+    const uint64_t key = o_stream_key(seed, stream);
+    int64_t i;
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < (int64_t)n; i++)
+        dst[i] = o_uniform(key, row0 + (uint64_t)i, lo, hi);
+}
+
+void o_gen_dates(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, uint64_t stream, int32_t ndays)
+{
+    const uint64_t key = o_stream_key(seed, stream);
+    int64_t i;
+#pragma omp parallel for schedule(static)
+    for (i = 0; i < (int64_t)n; i++)
+        dst[i] = o_yyyymmdd(O_DAY_1992 + o_uniform(key, row0 + (uint64_t)i, 0, ndays - 1));
+}
+
+void o_gen_datekeys(int32_t *dst, uint64_t n, int64_t day0)
+{
+    uint64_t i;
+    for (i = 0; i < n; i++)
+        dst[i] = o_yyyymmdd(O_DAY_1992 + day0 + (int64_t)i);
+}

@@ -15,8 +15,9 @@
 
 namespace sdb {
 
-constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs (grids are sized from the
-                           // device's own count at run time; this is a default)
+// SM count of the calling thread's current device, queried once per device
+// (errors.cpp); every grid of the library is sized from it.
+int device_sms();
 
 __host__ __device__ __forceinline__ bool compare(int cmp, int32_t a, int32_t b)
 {
@@ -104,7 +105,7 @@ __host__ __device__ inline bool aligned(const void *p, uintptr_t a)
 inline unsigned grid_for(uint64_t work, int threads, int blocks_per_sm = 8)
 {
     uint64_t b = (work + threads - 1) / threads;
-    uint64_t cap = (uint64_t)kSMs * blocks_per_sm;
+    uint64_t cap = (uint64_t)device_sms() * blocks_per_sm;
     if (b > cap) b = cap;
     if (b == 0) b = 1;
     return (unsigned)b;

@@ -43,6 +43,25 @@ int sdb_check_launch(const char *what)
     return SDB_OK;
 }
 
+namespace sdb {
+int device_sms()
+{
+    constexpr int kMaxDevices = 64;
+    static std::atomic<int> cache[kMaxDevices];  // 0: not queried yet
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0) dev = 0;
+    if (dev >= kMaxDevices) dev = kMaxDevices - 1;
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n > 0) return n;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) {
+        cudaGetLastError();
+        n = 152;  // GB300's count, as a default when the query fails
+    }
+    cache[dev].store(n, std::memory_order_relaxed);
+    return n;
+}
+}  // namespace sdb
+
 void sdb_errors_add_reader(unsigned long long (*reader)(cudaStream_t))
 {
     std::lock_guard<std::mutex> lk(g_readers_mu);

@@ -561,16 +561,7 @@ __global__ void __launch_bounds__(kThreads, min_blocks_of(ITEMS)) k_chain(const 
     }
 }
 
-int num_sms()
-{
-    static const int sms = [] {  // initialised once, thread-safe
-        int dev = 0, n = 0;
-        cudaGetDevice(&dev);
-        if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0) n = sdb::kSMs;
-        return n;
-    }();
-    return sms;
-}
+int num_sms() { return sdb::device_sms(); }
 
 template <int TERM, int NREGS, int ITEMS>
 int launch_term(const ChainLaunch &L, cudaStream_t s)
@@ -1016,22 +1007,27 @@ __device__ __forceinline__ void run_steps1(const Launch &L, RowT &R, const uint3
     (step1<kinds[BEGIN + IS]>(L.ops[BEGIN + IS], R, bits), ...);
 }
 
-// Adds one row to the group-by (block table first, global on overflow) and
-// runs the first-writer exchange; key(kk) gives the row's key values.
+// Adds the lane's row (when `row`) to the group-by (block table first, global
+// on overflow) and runs the first-writer exchange; key(kk) gives the row's
+// key values.  All 32 lanes of the warp call it (with row false where the
+// lane holds none): the lanes that take part in the warp aggregation are
+// named by a ballot over the full warp, never by the lanes that happen to
+// be converged.
 template <class KeyFn>
 __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsigned long long *s_sum, bool direct,
-                                          uint32_t h, int32_t value, KeyFn key)
+                                          bool row, uint32_t h, int32_t value, KeyFn key)
 {
-    const int64_t sl = sdb::group_slot(h, L.P);
-    if (sl < 0 || (uint64_t)sl >= L.P) {
-        atomicAdd(&g_errors, 1ull);
-        return;
-    }
+    const int64_t sl = row ? sdb::group_slot(h, L.P) : 0;
+    const bool bad = row && (sl < 0 || (uint64_t)sl >= L.P);
+    if (bad) atomicAdd(&g_errors, 1ull);
+    const bool go = row && !bad;
+    const unsigned mask = __ballot_sync(0xffffffffu, go);
+    if (!go) return;
     unsigned long long val = (unsigned long long)sdb::widen(value);
     // warp aggregation: lanes here with the same slot sum their values (exactly:
     // 16-bit halves reduced in 32 bits, then recombined in 64) and only the
     // lowest of them updates the table
-    const unsigned peers = __match_any_sync(__activemask(), (unsigned)sl);
+    const unsigned peers = __match_any_sync(mask, (unsigned)sl);
     if (__popc(peers) > 1) {
         const uint32_t lo = __reduce_add_sync(peers, (uint32_t)value & 0xffffu);
         const int32_t hi = (int32_t)__reduce_add_sync(peers, (uint32_t)(value >> 16));
@@ -1120,16 +1116,18 @@ template <int TERM, class RowT>
 __device__ __forceinline__ void finish_row(const Launch &L, RowT &R, uint32_t *s_key, unsigned long long *s_sum,
                                            bool direct, uint64_t &acc)
 {
-    if (R.live) {
-        if (TERM == T_SUM) {
-            acc += sdb::widen(fetch1(L.value, R));
-        } else if (TERM == T_GROUP) {
-            uint32_t h = 0;
+    if (TERM == T_SUM) {
+        if (R.live) acc += sdb::widen(fetch1(L.value, R));
+    } else if (TERM == T_GROUP) {
+        // every lane of the warp reaches group_row (its warp aggregation
+        // needs the whole warp); values of a lane without a live row are
+        // read from its registers or staged rows and not used
+        uint32_t h = 0;
 #pragma unroll
-            for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-                if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
-            group_row(L, s_key, s_sum, direct, h, fetch1(L.value, R), [&R, &L](int kk) { return fetch1(L.keys[kk], R); });
-        }
+        for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+            if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
+        group_row(L, s_key, s_sum, direct, R.live, h, fetch1(L.value, R),
+                  [&R, &L](int kk) { return fetch1(L.keys[kk], R); });
     }
 }
 
@@ -1374,33 +1372,34 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             for (int k = 0; k < kItems; k++)
                 if ((S.valid >> k) & 1u) L.flags_out[S.base + k] = (uint8_t)((S.live >> k) & 1u);
         }
-        if (S.live) {
+        if (TERM == T_SUM && S.live) {
             int32_t v[kItems];
-            if (TERM == T_SUM) {
-                fetch4(L.value, S, v);
+            fetch4(L.value, S, v);
 #pragma unroll
-                for (int k = 0; k < kItems; k++)
-                    if ((S.live >> k) & 1u) acc += sdb::widen(v[k]);
-            } else if (TERM == T_GROUP) {
-                fetch4(L.value, S, v);
-                uint32_t h[kItems] = {0, 0, 0, 0};
+            for (int k = 0; k < kItems; k++)
+                if ((S.live >> k) & 1u) acc += sdb::widen(v[k]);
+        } else if (TERM == T_GROUP && __any_sync(0xffffffffu, S.live != 0)) {
+            // the whole warp runs the group-by of its items (group_row's
+            // warp aggregation needs every lane); staged values of dead or
+            // missing rows are read and not used
+            int32_t v[kItems];
+            fetch4(L.value, S, v);
+            uint32_t h[kItems] = {0, 0, 0, 0};
 #pragma unroll
-                for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-                    if (kk < L.n_keys) {
-                        int32_t kv[kItems];
-                        fetch4(L.keys[kk], S, kv);
+            for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
+                if (kk < L.n_keys) {
+                    int32_t kv[kItems];
+                    fetch4(L.keys[kk], S, kv);
 #pragma unroll
-                        for (int k = 0; k < kItems; k++) h[k] += ((uint32_t)kv[k] - (uint32_t)L.key_min[kk]) * L.mults[kk];
-                    }
+                    for (int k = 0; k < kItems; k++) h[k] += ((uint32_t)kv[k] - (uint32_t)L.key_min[kk]) * L.mults[kk];
+                }
 #pragma unroll
-                for (int k = 0; k < kItems; k++)
-                    if ((S.live >> k) & 1u)
-                        group_row(L, s_key, s_sum, direct, h[k], v[k], [&](int kk) {
-                            int32_t kv[kItems];
-                            fetch4(L.keys[kk], S, kv);
-                            return kv[k];
-                        });
-            }
+            for (int k = 0; k < kItems; k++)
+                group_row(L, s_key, s_sum, direct, ((S.live >> k) & 1u) != 0, h[k], v[k], [&](int kk) {
+                    int32_t kv[kItems];
+                    fetch4(L.keys[kk], S, kv);
+                    return kv[k];
+                });
         }
     }
 }

@@ -889,13 +889,13 @@ int sdb_groupby_sum(const int32_t *const *keys, const int32_t *mins, const int32
     // a block per 32 x 8 groups, capped at the resident blocks
     const uint64_t want = (groups + 32 * (kThreads / 32) - 1) / (32 * (kThreads / 32));
     if (P <= 8192) {
-        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)sdb::kSMs * 2));
+        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)sdb::device_sms() * 2));
         if (vec)
             k_groupby<true, true><<<blocks, kThreads, smem, s>>>(a);
         else
             k_groupby<true, false><<<blocks, kThreads, smem, s>>>(a);
     } else {
-        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)sdb::kSMs * 8));
+        const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)sdb::device_sms() * 8));
         if (vec)
             k_groupby<false, true><<<blocks, kThreads, smem, s>>>(a);
         else
@@ -977,7 +977,7 @@ int sdb_compact_row_ids(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t
     if (!scratch || scratch_bytes < sdb_compact_scratch_bytes(n))
         return sdb_set_error(SDB_ERR_INVALID, "sdb_compact_row_ids: scratch needs %zu bytes", sdb_compact_scratch_bytes(n));
     uint32_t *bc = static_cast<uint32_t *>(scratch);
-    const unsigned grid = (unsigned)std::min<uint64_t>(nchunks, (uint64_t)sdb::kSMs * 8);
+    const unsigned grid = (unsigned)std::min<uint64_t>(nchunks, (uint64_t)sdb::device_sms() * 8);
     k_compact_count<<<grid, kThreads, 0, s>>>(flags, n, bc, nchunks);
     k_compact_scan<<<1, kThreads, 0, s>>>(bc, nchunks, count);
     k_compact_write<<<grid, kThreads, 0, s>>>(flags, n, bc, nchunks, ids);
@@ -992,7 +992,13 @@ int sdb_compact_row_ids(const uint8_t *flags, uint64_t n, int32_t *ids, uint32_t
 // segment of up to SDB_COMPACT_NOALLOC_MAX_ROWS rows (256 KB).  It lives in
 // the library's own device image, so every device that loads the library
 // holds it until the process exits, and every call on that device shares it.
+static_assert(SDB_COMPACT_NOALLOC_MAX_ROWS % kCompactChunk == 0,
+              "the no-allocation scratch holds one count per whole chunk of the largest segment");
 static __device__ __align__(256) uint32_t g_noalloc_compact_scratch[SDB_COMPACT_NOALLOC_MAX_ROWS / kCompactChunk];
+// what sdb_compact_scratch_bytes(SDB_COMPACT_NOALLOC_MAX_ROWS) asks for must fit the array
+static_assert(((SDB_COMPACT_NOALLOC_MAX_ROWS / kCompactChunk) * sizeof(uint32_t) + 255) / 256 * 256 <=
+                  sizeof(g_noalloc_compact_scratch),
+              "no-allocation scratch smaller than the compaction needs at the row limit");
 
 namespace {
 constexpr int kNoAllocMaxDevices = 64;
@@ -1019,6 +1025,9 @@ int sdb_compact_row_ids_noalloc(const uint8_t *flags, uint64_t n, int32_t *ids, 
     {
         // Set-up, once per device, with that device current: the host-side
         // name of the array is not a device address, so ask the runtime for it.
+        // The address is kept for the life of the process; a cudaDeviceReset
+        // destroys the module that holds the array, so the entry must not be
+        // called on a device after it was reset.
         std::lock_guard<std::mutex> lk(g_noalloc_mu);
         if (!g_noalloc_scratch_ptr[dev]) {
             void *p = nullptr;

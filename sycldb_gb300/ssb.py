@@ -3,7 +3,10 @@
 Every column comes from the counter-based generator of the native library
 (``sdb_gen_uniform`` / ``sdb_gen_uniform_cpu``, SplitMix64 of
 (seed, stream, row)), so host and device produce identical columns for any
-row range.  The public SSB dataset is not available offline; these columns
+row range.  The host generators take an optional ``gen`` object with the same
+three functions (``uniform``, ``dates``, ``datekeys``) over numpy buffers:
+the CPU checker supplies its own restatement through it, so that its legs
+load nothing of the native library.  The public SSB dataset is not available offline; these columns
 stand in for it with the distributions of the benchmark's configurations:
 
 * lineorder (6,000,000 x SF rows): orderdate uniform over a 2,556-day
@@ -79,11 +82,28 @@ def _spec(col: int, sf: float):
     return kind, lo, hi
 
 
+class LibGen:
+    """The native library's host generator (the default ``gen``)."""
+
+    def uniform(self, a: np.ndarray, n: int, row0: int, seed: int, sid: int, lo: int, hi: int):
+        capi.check(capi.lib().sdb_gen_uniform_cpu(a.ctypes.data, n, row0, seed, sid, lo, hi))
+
+    def dates(self, a: np.ndarray, n: int, row0: int, seed: int, sid: int, ndays: int):
+        capi.check(capi.lib().sdb_gen_dates_cpu(a.ctypes.data, n, row0, seed, sid, ndays))
+
+    def datekeys(self, a: np.ndarray, n: int, day0: int):
+        capi.check(capi.lib().sdb_gen_datekeys_cpu(a.ctypes.data, n, day0))
+
+
+def _gen(gen):
+    return gen if gen is not None else LibGen()
+
+
 def gen_lineorder_host(n: int, cols: Iterable[int], sf: float, seed: int = SEED, row0: int = 0,
-                       out: Optional[Dict[int, np.ndarray]] = None, salt: int = 0) -> Dict[int, np.ndarray]:
+                       out: Optional[Dict[int, np.ndarray]] = None, salt: int = 0, gen=None) -> Dict[int, np.ndarray]:
     """Host columns (numpy int32; ``out`` may supply destination arrays,
     e.g. views of pinned tensors)."""
-    L = capi.lib()
+    g = _gen(gen)
     res = {}
     for c in cols:
         a = out[c] if out and c in out else np.empty(n, dtype=np.int32)
@@ -91,9 +111,9 @@ def gen_lineorder_host(n: int, cols: Iterable[int], sf: float, seed: int = SEED,
         kind, lo, hi = _spec(c, sf)
         sid = stream_id("lineorder", c, salt)
         if kind == "date":
-            capi.check(L.sdb_gen_dates_cpu(a.ctypes.data, n, row0, seed, sid, NDAYS))
+            g.dates(a, n, row0, seed, sid, NDAYS)
         else:
-            capi.check(L.sdb_gen_uniform_cpu(a.ctypes.data, n, row0, seed, sid, lo, hi))
+            g.uniform(a, n, row0, seed, sid, lo, hi)
         res[c] = a
     return res
 
@@ -117,33 +137,33 @@ def gen_lineorder_device(n: int, cols: Iterable[int], sf: float, seed: int = SEE
     return res
 
 
-def _uniform(table: str, col: int, n: int, lo: int, hi: int, seed: int, salt: int = 0) -> np.ndarray:
+def _uniform(table: str, col: int, n: int, lo: int, hi: int, seed: int, salt: int = 0, gen=None) -> np.ndarray:
     a = np.empty(n, dtype=np.int32)
-    capi.check(capi.lib().sdb_gen_uniform_cpu(a.ctypes.data, n, 0, seed, stream_id(table, col, salt), lo, hi))
+    _gen(gen).uniform(a, n, 0, seed, stream_id(table, col, salt), lo, hi)
     return a
 
 
-def gen_geo_dim(table: str, n: int, seed: int = SEED) -> Dict[int, np.ndarray]:
+def gen_geo_dim(table: str, n: int, seed: int = SEED, gen=None) -> Dict[int, np.ndarray]:
     """supplier / customer: key, city(3), nation(4), region(5)."""
     key = np.arange(1, n + 1, dtype=np.int32)
-    region = _uniform(table, 5, n, 0, 4, seed)
-    nation = (region * 5 + _uniform(table, 4, n, 0, 4, seed)).astype(np.int32)
-    city = (nation * 10 + _uniform(table, 3, n, 0, 9, seed)).astype(np.int32)
+    region = _uniform(table, 5, n, 0, 4, seed, gen=gen)
+    nation = (region * 5 + _uniform(table, 4, n, 0, 4, seed, gen=gen)).astype(np.int32)
+    city = (nation * 10 + _uniform(table, 3, n, 0, 9, seed, gen=gen)).astype(np.int32)
     return {0: key, 3: city, 4: nation, 5: region}
 
 
-def gen_part(n: int, seed: int = SEED) -> Dict[int, np.ndarray]:
+def gen_part(n: int, seed: int = SEED, gen=None) -> Dict[int, np.ndarray]:
     key = np.arange(1, n + 1, dtype=np.int32)
-    category = _uniform("part", 3, n, 0, 24, seed)
-    brand = (category * 40 + _uniform("part", 4, n, 0, 39, seed)).astype(np.int32)
+    category = _uniform("part", 3, n, 0, 24, seed, gen=gen)
+    brand = (category * 40 + _uniform("part", 4, n, 0, 39, seed, gen=gen)).astype(np.int32)
     mfgr = (category // 5).astype(np.int32)
-    size = _uniform("part", 7, n, 1, 50, seed)
+    size = _uniform("part", 7, n, 1, 50, seed, gen=gen)
     return {0: key, 2: mfgr, 3: category, 4: brand, 7: size}
 
 
-def gen_ddate(n: int = NDAYS) -> Dict[int, np.ndarray]:
+def gen_ddate(n: int = NDAYS, gen=None) -> Dict[int, np.ndarray]:
     key = np.empty(n, dtype=np.int32)
-    capi.check(capi.lib().sdb_gen_datekeys_cpu(key.ctypes.data, n, 0))
+    _gen(gen).datekeys(key, n, 0)
     days = np.datetime64("1992-01-01") + np.arange(n)
     year = (key // 10000).astype(np.int32)
     month = (key // 100 % 100).astype(np.int32)
@@ -155,12 +175,12 @@ def gen_ddate(n: int = NDAYS) -> Dict[int, np.ndarray]:
             11: ((doy - 1) // 7 + 1).astype(np.int32)}
 
 
-def gen_dims(sf: float, seed: int = SEED) -> Dict[str, Dict[int, np.ndarray]]:
+def gen_dims(sf: float, seed: int = SEED, gen=None) -> Dict[str, Dict[int, np.ndarray]]:
     return {
-        "supplier": gen_geo_dim("supplier", dim_rows("supplier", sf), seed),
-        "customer": gen_geo_dim("customer", dim_rows("customer", sf), seed),
-        "part": gen_part(dim_rows("part", sf), seed),
-        "ddate": gen_ddate(),
+        "supplier": gen_geo_dim("supplier", dim_rows("supplier", sf), seed, gen=gen),
+        "customer": gen_geo_dim("customer", dim_rows("customer", sf), seed, gen=gen),
+        "part": gen_part(dim_rows("part", sf), seed, gen=gen),
+        "ddate": gen_ddate(gen=gen),
     }
 
 

@@ -7,7 +7,7 @@ import pytest
 
 from sycldb_gb300 import capi, plans, ssb, workloads
 from sycldb_gb300.engine import Engine
-from tests import datasets
+from tests import datasets, naive
 
 pytestmark = pytest.mark.gpu
 
@@ -134,16 +134,24 @@ def test_batch_run_without_unpacking_and_errors(tables, oracle_rows):
 
 def test_batched_form_full_size_equals_plain():
     """64 star-join plans over fact partitions of 1M..50M rows (lognormal),
-    SF20 dimensions: the batch gives each plan's own result."""
+    SF20 dimensions: the batch gives each plan's own result, and every plan's
+    rows are those of the independent naive evaluator over its partition
+    (with the plan's region, category, year and brand windows)."""
     wl = workloads.batch_workload()
+    dims = ssb.gen_dims(wl.dim_sf, wl.seed)
     with Engine() as eng:
-        workloads.load_batch_tables(eng, wl, device=True)
+        workloads.load_batch_tables(eng, wl, device=True, dims=dims)
         pls = wl.plans()
         alone = [eng.execute(pl).canonical() for pl in pls]
         with eng.batch(pls) as b:
             got = [r.canonical() for r in b.run()]
             st = b.stats()
     assert got == alone
+    for p, (n, prm) in enumerate(zip(wl.rows, wl.params)):
+        fact = ssb.gen_lineorder_host(n, workloads.STAR_COLS, wl.dim_sf, wl.seed, salt=p + 1)
+        want = naive.star_vec(fact, dims["supplier"], dims["part"], dims["ddate"], prm.region, prm.category,
+                              prm.year_lo, prm.year_hi, prm.brand_count)
+        assert alone[p] == want, p
     # the fact chains of partitions under 2^23 rows in one launch (larger ones
     # run the single-chain kernel on their own), the 192 dimension builds in one
     small = sum(1 for r in wl.rows if r < (1 << 23))

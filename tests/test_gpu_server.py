@@ -5,9 +5,9 @@ plain one-at-a-time replay of the same trace must give the same results."""
 import numpy as np
 import pytest
 
-from sycldb_gb300 import capi, plans, workloads
+from sycldb_gb300 import capi, plans, ssb, workloads
 from sycldb_gb300.engine import Engine, Server, replay_plain
-from tests import datasets
+from tests import datasets, naive
 
 pytestmark = pytest.mark.gpu
 
@@ -125,3 +125,68 @@ def test_large_chains_run_on_their_own_in_the_mix():
         with eng.batch(pls[:12]) as b:
             assert [r.canonical() for r in b.run()] == alone[:12]
             assert b.stats()["batched_chains"] == 0  # every fact chain is large
+
+
+def _naive_of(kind, plan, fact, dims):
+    """The naive evaluator's rows for a served request, from its plan's
+    constants (the plan builders of sycldb_gb300.plans)."""
+    rels = plan["rels"]
+    if kind == "filter_sum":
+        cond = rels[1]["condition"]["operands"]
+        lo = int(cond[0]["operands"][1]["literal"]["rangeSet"][0][1])
+        d_lo = int(cond[1]["operands"][1]["literal"]["rangeSet"][0][1])
+        d_hi = int(cond[1]["operands"][1]["literal"]["rangeSet"][0][2])
+        q = int(cond[2]["operands"][1]["literal"]["value"])
+        return naive.filter_sum_vec(fact, lo // 10000, d_lo, d_hi, q)
+    if kind == "date_join":
+        rs = rels[1]["condition"]["operands"][1]["literal"]["rangeSet"][0]
+        y0 = int(rels[3]["condition"]["operands"][1]["literal"]["rangeSet"][0][1])
+        return naive.date_join_vec(fact, dims["ddate"], y0, int(rs[1]), int(rs[2]))
+    region = int(rels[2]["condition"]["operands"][1]["literal"]["value"])
+    pf = rels[5]["condition"]
+    if kind == "star":
+        return naive.star_vec(fact, dims["supplier"], dims["part"], dims["ddate"], region,
+                              int(pf["operands"][1]["literal"]["value"]))
+    cat = int(pf["operands"][0]["operands"][1]["literal"]["value"])
+    b = pf["operands"][1]["operands"][1]["literal"]["rangeSet"][0]
+    y = rels[8]["condition"]["operands"][1]["literal"]["rangeSet"][0]
+    return naive.star_vec(fact, dims["supplier"], dims["part"], dims["ddate"], region, cat, int(y[1]), int(y[2]),
+                          int(b[2]) - int(b[1]) + 1)
+
+
+def test_served_sf50_every_plan_kind_matches_naive():
+    """The served configuration's table at full size: SF50, 300 M fact rows
+    in two 2^28-row segments, SF50 dimensions.  A Poisson stream with every
+    plan kind goes through the server and the plain path; two requests of
+    each kind are checked against the independent naive evaluator."""
+    import torch
+
+    sf = 50.0
+    n = ssb.fact_rows(sf)
+    cols = (3, 4, 5, 8, 9, 11, 12)
+    dims = ssb.gen_dims(sf)
+    reqs = workloads.poisson_stream(1000.0, 32, seed=ssb.SEED + 5)
+    kinds = {}
+    for i, r in enumerate(reqs):
+        kinds.setdefault(r.kind, []).append(i)
+    assert set(kinds) == {"filter_sum", "date_join", "star", "batch_star"}
+    pls, at = [r.plan for r in reqs], [r.t for r in reqs]
+    fact = ssb.gen_lineorder_device(n, cols, sf)
+    with Engine() as eng:
+        eng.load_table("lineorder", fact)
+        for t in ("supplier", "part", "ddate"):
+            eng.load_table(t, dims[t])
+        pst, _, pres, _ = replay_plain(eng, pls, at)
+        with Server(eng, budget_bytes=60 << 30) as srv:
+            sst, _, sres, _ = srv.replay(pls, at)
+    del fact
+    torch.cuda.empty_cache()
+    assert pst == [capi.SDB_OK] * len(pls) and sst == [capi.SDB_OK] * len(pls)
+    plain = [r.canonical() for r in pres]
+    assert [r.canonical() for r in sres] == plain
+    host = ssb.gen_lineorder_host(n, cols, sf)
+    for kind, idx in kinds.items():
+        for i in idx[:2]:
+            want = _naive_of(kind, pls[i], host, dims)
+            assert plain[i] == want, (kind, i)
+            assert len(want) > 0
