@@ -435,11 +435,28 @@ typedef struct sdb_engine_config {
                                    reference gives them (its SORT is a pass-through) */
 } sdb_engine_config;
 
+/* Plan text.  Every entry that takes plan_json reads two dialects: the
+ * reference's Thrift IDL shape (PlanResult/RelNode/ExprType of
+ * server/thrift/calciteserver.thrift:22-80, enums by name or number) and
+ * Calcite's RelJson as the reference's planner emits it, which
+ * SycldbJsonConverter turns into those structs
+ * (server/src/main/java/com/eurecom/calcite/SycldbJsonConverter.java:31-163:
+ * planner class names as relOp, "table", string ids and inputs,
+ * {"name": ...} operators and aggregates, bare-number literals, Sarg
+ * rangeSets). */
+
 /* Parses a plan and derives its execution order and group-by columns
  * (operations/preprocessing.cpp:104-275) without touching a device.
  * *n_rels = number of plan nodes; order (optional, n_rels entries) = the DAG
  * execution order. */
 int sdb_plan_check(const char *plan_json, int *n_rels, int *order, int order_cap);
+
+/* The plan as parsed, written back in the IDL shape (what
+ * SycldbJsonConverter hands the executor through Thrift): *len = its length
+ * without the terminating NUL; the text is copied to out when cap > *len.
+ * Replaces SycldbJsonConverter.getRels + the Thrift transfer
+ * (SycldbJsonConverter.java:13-29). */
+int sdb_plan_to_idl_json(const char *plan_json, char *out, size_t cap, size_t *len);
 
 int sdb_engine_create(const sdb_engine_config *cfg, sdb_engine **out);
 int sdb_engine_destroy(sdb_engine *eng);

@@ -144,6 +144,7 @@ _SIGS = {
     "sdb_gen_dates": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32, _P]),
     "sdb_gen_dates_cpu": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32]),
     "sdb_plan_check": (c_int, [c_char_p, POINTER(c_int), POINTER(c_int), c_int]),
+    "sdb_plan_to_idl_json": (c_int, [c_char_p, c_char_p, c_size_t, POINTER(c_size_t)]),
     "sdb_engine_create": (c_int, [POINTER(EngineConfig), POINTER(c_void_p)]),
     "sdb_engine_destroy": (c_int, [c_void_p]),
     "sdb_engine_load_table": (c_int, [c_void_p, c_char_p, c_int, POINTER(c_void_p), c_uint64, c_int]),
@@ -222,3 +223,17 @@ def force_chain_variant(variant: int):
         for nregs in (1, 4, 8):
             for b in range(40):
                 check(L.sdb_chain_tune_set(term, nregs, 1 << b, variant))
+
+
+def plan_to_idl(plan) -> dict:
+    """A plan in either dialect the executor reads (IDL shape or Calcite
+    RelJson), as the executor parsed it, in the IDL shape."""
+    import json
+
+    text = (plan if isinstance(plan, str) else json.dumps(plan)).encode()
+    L = lib()
+    n = c_size_t(0)
+    check(L.sdb_plan_to_idl_json(text, None, 0, ctypes.byref(n)))
+    buf = ctypes.create_string_buffer(n.value + 1)
+    check(L.sdb_plan_to_idl_json(text, buf, n.value + 1, ctypes.byref(n)))
+    return json.loads(buf.value.decode())

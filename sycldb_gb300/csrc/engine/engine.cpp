@@ -2661,6 +2661,16 @@ int sdb_plan_check(const char *plan_json, int *n_rels, int *order, int order_cap
     });
 }
 
+int sdb_plan_to_idl_json(const char *plan_json, char *out, size_t cap, size_t *len)
+{
+    if (!plan_json || !len) return sdb_set_error(SDB_ERR_INVALID, "sdb_plan_to_idl_json: NULL argument");
+    return sdb::guarded([&] {
+        const std::string text = sdb::plan_to_json(sdb::plan_from_json(plan_json));
+        *len = text.size();
+        if (out && cap > text.size()) std::memcpy(out, text.c_str(), text.size() + 1);
+    });
+}
+
 int sdb_engine_create(const sdb_engine_config *cfg, sdb_engine **out)
 {
     if (!out) return sdb_set_error(SDB_ERR_INVALID, "sdb_engine_create: out is NULL");

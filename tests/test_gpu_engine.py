@@ -293,3 +293,21 @@ def test_wide_chains_split_only_when_order_does_not_matter():
     finally:
         capi.force_chain_variant(-1)
     assert all(len(w) > 0 for w in want)
+
+
+@pytest.mark.parametrize("fuse", [False, True])
+def test_reljson_plans_give_the_idl_plans_rows(fuse):
+    """SSB q1.1, q2.1 and q3.1 written in Calcite's RelJson dialect run on the
+    device and give the rows of the same plans in the IDL shape, which are
+    the oracle's."""
+    from tests import test_reljson_cpu as R
+
+    ds = datasets.dataset(0.05)
+    idl = R.idl_plans()
+    with Engine(arena_bytes=1 << 30, fuse=fuse, segment_rows=1 << 16) as eng:
+        load(eng, ds)
+        for name in ("q11", "q21", "q31"):
+            want = datasets.oracle_run(ds, idl[name], 1 << 16)
+            assert eng.execute(idl[name]).canonical() == want, name
+            assert eng.execute(R.reljson(name)).canonical() == want, name
+            assert len(want) > 0
