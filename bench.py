@@ -105,6 +105,8 @@ def parse_args():
                     help="skip the SF1 configurations (filter-project-sum, date join + group-by)")
     ap.add_argument("--only", default="", choices=["", "configs"],
                     help="run one section alone (for profiling): configs")
+    ap.add_argument("--config-names", default="",
+                    help="comma-separated subset of the SF1 configurations to run (default: all)")
     ap.add_argument("--config-copies", type=int, default=8,
                     help="copies of the SF1 fact columns the configs section rotates through (L2 defeat)")
     ap.add_argument("--no-widened", action="store_true",
@@ -220,12 +222,16 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """DRAM bytes per launch of the fused chain from the committed ncu summary."""
-    if not os.path.exists(PROFILE_SUMMARY):
+CONFIG_PROFILES = {"filter_project_sum_sf1": os.path.join(ROOT, "profiles", "fused_chain_filter_sum_sf1.txt"),
+                   "date_join_groupby_sf1": os.path.join(ROOT, "profiles", "fused_chain_date_join_sf1.txt")}
+
+
+def profile_traffic(path=PROFILE_SUMMARY, key="traffic_bytes_per_launch_sf20:"):
+    """DRAM bytes per launch of a fused chain from its committed ncu summary."""
+    if not os.path.exists(path):
         return None
-    for line in open(PROFILE_SUMMARY):
-        if line.startswith("traffic_bytes_per_launch_sf20:"):
+    for line in open(path):
+        if line.startswith(key):
             try:
                 return int(float(line.split(":", 1)[1].strip()))
             except ValueError:
@@ -415,7 +421,8 @@ def run_ours(args, rank, world, local, pg):
     n = ssb.fact_rows(sf)
     build_plan, cols_key, kernel_name = PLANS[args.plan]
     cols = ssb.QUERY_COLUMNS[cols_key]
-    plan = build_plan()
+    # plan text, serialised once: what a caller of sdb_engine_execute holds
+    plan = json.dumps(build_plan())
     dims = dims_host(sf)
     fact = ssb.gen_lineorder_device(n, cols, sf, salt=rank)
     torch.cuda.synchronize()
@@ -574,14 +581,17 @@ def run_configs(args, rank, stream, peak, ref):
 
     out = {}
     copies = max(1, args.config_copies)
+    wanted = [x for x in args.config_names.split(",") if x]
     for name, (builder, key, csf, dnames) in CPU_CONFIGS.items():
+        if wanted and name not in wanted:
+            continue
         n = ssb.fact_rows(csf)
         cols = ssb.QUERY_COLUMNS[key]
         base = ssb.gen_lineorder_device(n, cols, csf, salt=rank)
         tabs = [{c: base[c].clone() for c in cols} for _ in range(copies)]
         del base
         dims = ssb.gen_dims(csf)
-        pls = [_with_fact_tag(builder, i) for i in range(copies)]
+        pls = [json.dumps(_with_fact_tag(builder, i)) for i in range(copies)]
         torch.cuda.synchronize()
 
         def loaded(**kw):
@@ -632,6 +642,7 @@ def run_configs(args, rank, stream, peak, ref):
             "roofline": {"kernel": "k_dense (fused chain)", "bound": "hbm", "achieved": ach, "peak": peak,
                          "unit": "GB/s", "frac": (ach / peak) if ach else None, "launch_ms": per,
                          "launches": kn, "algorithmic_bytes_per_launch": alg,
+                         "traffic": profile_traffic(CONFIG_PROFILES[name], "traffic_bytes_per_launch:"),
                          "timing": "CUDA events around each fused-pass launch, %d plain-path steps" % prof},
             "same_rows_every_copy": exact_copies,
         }
@@ -756,6 +767,7 @@ def run_widened(args, rank, stream, peak):
         return e
 
     for name, (plan, cs) in shapes.items():
+        plan = json.dumps(plan)
         peng = loaded(profile=True)
         for _ in range(3):
             res = peng.execute(plan)
