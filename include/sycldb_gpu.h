@@ -601,7 +601,9 @@ typedef struct sdb_server_config {
     int32_t slots;            /* batches in flight; 0 = 4 */
     int32_t max_batch;        /* plans per batch; 0 = 64 */
     int32_t streams_per_slot; /* 0 = 4 */
-    int32_t pad;
+    int32_t no_direct;        /* 0: a request that arrives at an idle server with nothing else waiting
+                                 runs at once through the plain path (no sizing pass, no batch set-up);
+                                 1: every request goes through a batch */
 } sdb_server_config;
 
 typedef struct sdb_server_stats {
@@ -612,6 +614,7 @@ typedef struct sdb_server_stats {
     uint64_t peak_device_bytes;        /* most budget bytes in use at once */
     uint64_t peak_pinned_bytes;
     uint64_t budget_bytes;
+    uint64_t direct_plans;             /* requests run at once through the plain path (idle server) */
 } sdb_server_stats;
 
 int sdb_server_create(sdb_engine *eng, const sdb_server_config *cfg, sdb_server **out);

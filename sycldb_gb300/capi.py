@@ -71,13 +71,13 @@ class BatchStats(ctypes.Structure):
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("budget_bytes", c_uint64), ("pinned_bytes", c_uint64), ("slots", c_int32), ("max_batch", c_int32),
-                ("streams_per_slot", c_int32), ("pad", c_int32)]
+                ("streams_per_slot", c_int32), ("no_direct", c_int32)]
 
 
 class ServerStats(ctypes.Structure):
     _fields_ = [(f, c_uint64) for f in ("submitted", "completed", "failed", "batches", "batched_plans",
                                         "max_batch_plans", "max_inflight_plans", "peak_device_bytes",
-                                        "peak_pinned_bytes", "budget_bytes")]
+                                        "peak_pinned_bytes", "budget_bytes", "direct_plans")]
 
 
 SDB_BATCH_EAGER = 1

@@ -68,4 +68,8 @@ void batch_destroy(sdb_batch *b);
 // Runs one plan with the engine's plain path (sdb_engine_execute).
 sdb_result *execute_plain(sdb_engine *eng, const std::string &plan);
 
+// Device bytes of the engine's own arena and zeroed region (what a plain
+// execution can use at most).
+uint64_t engine_memory_bytes(const sdb_engine *eng);
+
 }  // namespace sdb

@@ -157,6 +157,8 @@ public:
     ~MemoryManager() { release(); }
 
     void init(uint64_t budget, cudaStream_t s) { init_sized(budget, std::max<uint64_t>(budget >> 6, 1u << 20), s); }
+    // device bytes of the arena and its zeroed region
+    uint64_t capacity() const { return size_ + zsize_; }
 
     void init_sized(uint64_t size, uint64_t zsize, cudaStream_t s)
     {
@@ -2616,6 +2618,8 @@ sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string>
 sdb_result *batch_take_result(const sdb_batch *B, size_t p) { return unpack_result(*B, p); }
 
 sdb_result *execute_plain(sdb_engine *eng, const std::string &plan) { return execute_plan(eng->E, plan).release(); }
+
+uint64_t engine_memory_bytes(const sdb_engine *eng) { return eng->E.mm.capacity(); }
 
 void batch_destroy(sdb_batch *B)
 {

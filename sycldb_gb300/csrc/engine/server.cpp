@@ -297,6 +297,7 @@ struct sdb_server {
     void run()
     {
         cudaSetDevice(device);
+        const bool direct = !cfg.no_direct && cfg.budget_bytes >= sdb::engine_memory_bytes(eng);
         for (;;) {
             bool progress = false;
             int busy = 0;
@@ -320,6 +321,28 @@ struct sdb_server {
                     waiting.push_back(std::move(incoming.front()));
                     incoming.pop_front();
                 }
+            }
+            // An idle server with one request and nothing else waiting runs it
+            // at once through the plain path: no sizing pass and no batch
+            // set-up, so a lone request waits no longer than on the plain
+            // path.  Requests that arrive meanwhile wait for it, then go into
+            // batches as usual.
+            // (Only when the budget covers the engine's own memory, which a
+            // plain execution uses: no plan then goes past the budget.)
+            if (direct && busy == 0 && waiting.size() == 1 && !waiting.front().sized) {
+                Request r = std::move(waiting.front());
+                waiting.pop_front();
+                try {
+                    sdb_result *res = sdb::execute_plain(eng, r.plan);
+                    finish(r, SDB_OK, "", res);
+                } catch (const sdb::Error &x) {
+                    finish(r, x.status, x.what(), nullptr);
+                } catch (const std::exception &x) {
+                    finish(r, SDB_ERR_INVALID, x.what(), nullptr);
+                }
+                std::lock_guard<std::mutex> g(mu);
+                st.direct_plans++;
+                continue;
             }
             for (size_t i = 0; i < waiting.size();) {
                 if (waiting[i].sized || size_request(waiting[i])) {

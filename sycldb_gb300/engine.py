@@ -307,9 +307,9 @@ class Server:
     used otherwise."""
 
     def __init__(self, engine: Engine, budget_bytes: int = 0, pinned_bytes: int = 0, slots: int = 0,
-                 max_batch: int = 0, streams_per_slot: int = 0):
+                 max_batch: int = 0, streams_per_slot: int = 0, direct: bool = True):
         L = capi.lib()
-        cfg = capi.ServerConfig(budget_bytes, pinned_bytes, slots, max_batch, streams_per_slot, 0)
+        cfg = capi.ServerConfig(budget_bytes, pinned_bytes, slots, max_batch, streams_per_slot, 0 if direct else 1)
         h = ctypes.c_void_p()
         capi.check(L.sdb_server_create(engine._h, ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

@@ -190,3 +190,28 @@ def test_served_sf50_every_plan_kind_matches_naive():
             want = _naive_of(kind, pls[i], host, dims)
             assert plain[i] == want, (kind, i)
             assert len(want) > 0
+
+
+@pytest.mark.parametrize("direct", [True, False])
+def test_lone_requests_at_an_idle_server_run_directly(ds, direct):
+    """At a low arrival rate most requests find the server idle: they run at
+    once through the plain path (no sizing pass, no batch); with direct off,
+    every one goes through a batch.  Results are each plan's own either way."""
+    pls, at = trace(50, 40, seed=31)
+    with make_engine(ds) as eng:
+        alone = [eng.execute(p).canonical() for p in pls]
+        with Server(eng, budget_bytes=8 << 30, direct=direct) as srv:
+            st, lat, res, wall = srv.replay(pls, at)
+            stats = srv.stats()
+        assert st == [capi.SDB_OK] * len(pls)
+        assert [r.canonical() for r in res] == alone
+        if direct:
+            assert stats["direct_plans"] > len(pls) // 2
+            assert stats["direct_plans"] + stats["batched_plans"] == len(pls)
+        else:
+            assert stats["direct_plans"] == 0 and stats["batched_plans"] == len(pls)
+        # a budget below the engine's own memory turns the direct path off
+        with Server(eng, budget_bytes=256 << 20) as small:
+            st2, _, res2, _ = small.replay(pls[:8], at[:8])
+            assert small.stats()["direct_plans"] == 0
+        assert [r.canonical() for r in res2] == alone[:8]
