@@ -348,6 +348,20 @@ int sdb_chain_tune_get(int terminal, int nregs, uint64_t rows);
  * every kind (what sdb_chain_tune_set does). */
 int sdb_chain_tune_set_op(int terminal, int nregs, int first_op, uint64_t rows, int variant);
 int sdb_chain_tune_get_op(int terminal, int nregs, int first_op, uint64_t rows);
+/* Launch shapes of the operator-at-a-time kernels (K1-K16): threads per
+ * block (128, 256 or 512) and resident blocks per SM the grid-stride grid is
+ * sized for, per kernel and row count (bucketed by log2).  No counterpart in
+ * the reference (its parallel_for ranges leave the work-group size to the
+ * SYCL runtime).  block = blocks_per_sm = 0 restores the default (256
+ * threads; 8 blocks per SM, 4 for the reductions K7, K16 and min/max). */
+typedef enum sdb_op_kernel {
+    SDB_OPK_FILL_U8 = 0, SDB_OPK_SELECT_LIT, SDB_OPK_SELECT_COLS, SDB_OPK_LOGICAL, SDB_OPK_FILL_I32, SDB_OPK_BINOP,
+    SDB_OPK_SUM, SDB_OPK_COUNT_FLAGS, SDB_OPK_MIN_MAX, SDB_OPK_OCC_TO_FLAGS, SDB_OPK_BUILD_KEYS, SDB_OPK_PROBE_SEMI,
+    SDB_OPK_BUILD_KV, SDB_OPK_PROBE_FULL, SDB_OPK_GATHER, SDB_OPK_COUNT
+} sdb_op_kernel;
+int sdb_op_tune_set(int op_kernel, uint64_t rows, int block, int blocks_per_sm);
+int sdb_op_tune_get(int op_kernel, uint64_t rows, int *block, int *blocks_per_sm);
+
 /* Registers (1..8) a chain needs, or a negative status if it is invalid. */
 int sdb_chain_registers(const sdb_chain_desc *chain);
 /* 1 when the chain has a shape-specialised instantiation (variants 3-7), 0

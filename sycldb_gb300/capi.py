@@ -26,6 +26,9 @@ NONE, AND, OR = range(3)
 MUL, DIV, ADD, SUB = range(4)
 
 SRC_COL, SRC_REG, SRC_LIT = range(3)
+# sdb_op_kernel: the operator-at-a-time kernels whose launch shape is tuned
+OP_KERNELS = ("fill_u8", "select_lit", "select_cols", "logical", "fill_i32", "binop", "sum", "count_flags", "min_max",
+              "occ_to_flags", "build_keys", "probe_semi", "build_kv", "probe_full", "gather")
 OP_SELECT, OP_SEARCH_RANGE, OP_SEARCH_POINTS, OP_SEMI_PROBE, OP_FULL_PROBE, OP_BINOP, OP_FILL = range(7)
 TERM_FLAGS, TERM_SUM, TERM_GROUPBY, TERM_BUILD_KEYS, TERM_BUILD_KV = range(5)
 CHAIN_MAX_OPS, CHAIN_MAX_REGS, CHAIN_MAX_KEYS = 16, 8, 4
@@ -144,6 +147,8 @@ _SIGS = {
     "sdb_gen_dates": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32, _P]),
     "sdb_gen_dates_cpu": (c_int, [_P, c_uint64, c_uint64, c_uint64, c_uint64, c_int32]),
     "sdb_plan_check": (c_int, [c_char_p, POINTER(c_int), POINTER(c_int), c_int]),
+    "sdb_op_tune_set": (c_int, [c_int, c_uint64, c_int, c_int]),
+    "sdb_op_tune_get": (c_int, [c_int, c_uint64, POINTER(c_int), POINTER(c_int)]),
     "sdb_plan_to_idl_json": (c_int, [c_char_p, c_char_p, c_size_t, POINTER(c_size_t)]),
     "sdb_engine_create": (c_int, [POINTER(EngineConfig), POINTER(c_void_p)]),
     "sdb_engine_destroy": (c_int, [c_void_p]),

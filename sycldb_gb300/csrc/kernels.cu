@@ -6,6 +6,7 @@
 // are not 16-byte (columns) / 8-byte (flags) aligned take the scalar
 // instantiation, which computes the same values.
 #include <algorithm>
+#include <atomic>
 #include <cstdio>
 #include <initializer_list>
 #include <mutex>
@@ -30,6 +31,34 @@ unsigned long long read_errors(cudaStream_t s)
 const int g_reader_registered = (sdb_errors_add_reader(&read_errors), 0);
 
 constexpr int kThreads = 256;
+constexpr int kMaxBlock = 512;  // largest block an operator kernel is tuned to
+
+// Launch shape of an operator kernel: threads per block and the resident
+// blocks per SM its grid-stride grid is sized for.  Tuned per (operator,
+// log2 rows) by the autotuner (sdb_op_tune_set); unset entries take the
+// defaults (256 threads; 8 blocks per SM for the map kernels, 4 for the
+// reductions).
+struct LaunchShape {
+    int block, per_sm;
+};
+std::atomic<int32_t> g_op_tune[SDB_OPK_COUNT][40];  // block << 8 | per_sm; 0: default
+
+int op_bucket(uint64_t n)
+{
+    int b = 0;
+    while (b < 39 && (1ull << (b + 1)) <= n) b++;
+    return b;
+}
+
+LaunchShape op_shape(int opk, uint64_t rows, int default_per_sm)
+{
+    const int32_t e = g_op_tune[opk][op_bucket(rows)].load(std::memory_order_relaxed);
+    if (e <= 0) return {kThreads, default_per_sm};
+    return {e >> 8, e & 0xff};
+}
+
+// Grid of `work` items for a launch shape (grid-stride kernels).
+unsigned grid_of(uint64_t work, const LaunchShape &sh) { return sdb::grid_for(work, sh.block, sh.per_sm); }
 
 // ---------------------------------------------------------------- vector io
 __device__ __forceinline__ void ld8(const int32_t *p, uint64_t r0, int32_t (&v)[8])
@@ -75,7 +104,7 @@ __device__ __forceinline__ void stf8(uint8_t *p, uint64_t r0, uint32_t m)
 // Grid-stride driver: Op provides group(r0) for 8 rows (vector path) and
 // row(r) for one row.  VEC=false walks rows one at a time.
 template <bool VEC, class Op>
-__global__ void __launch_bounds__(kThreads) k_map(uint64_t n, Op op)
+__global__ void __launch_bounds__(kMaxBlock) k_map(uint64_t n, Op op)
 {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -89,13 +118,14 @@ __global__ void __launch_bounds__(kThreads) k_map(uint64_t n, Op op)
 }
 
 template <class Op>
-int launch_map(uint64_t n, bool vec, const Op &op, cudaStream_t s, const char *what)
+int launch_map(uint64_t n, bool vec, const Op &op, cudaStream_t s, const char *what, int opk)
 {
     if (n == 0) return SDB_OK;
+    const LaunchShape sh = op_shape(opk, n, 8);
     if (vec)
-        k_map<true, Op><<<sdb::grid_for((n + 7) / 8, kThreads), kThreads, 0, s>>>(n, op);
+        k_map<true, Op><<<grid_of((n + 7) / 8, sh), sh.block, 0, s>>>(n, op);
     else
-        k_map<false, Op><<<sdb::grid_for(n, kThreads), kThreads, 0, s>>>(n, op);
+        k_map<false, Op><<<grid_of(n, sh), sh.block, 0, s>>>(n, op);
     return sdb_check_launch(what);
 }
 
@@ -203,7 +233,7 @@ __device__ __forceinline__ uint64_t warp_sum_u64(uint64_t v)
 
 __device__ __forceinline__ uint64_t block_sum_u64(uint64_t v)
 {
-    __shared__ uint64_t part[kThreads / 32];
+    __shared__ uint64_t part[kMaxBlock / 32];
     v = warp_sum_u64(v);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     if (lane == 0) part[wid] = v;
@@ -219,7 +249,7 @@ __device__ __forceinline__ uint64_t block_sum_u64(uint64_t v)
 
 // K7: one 64-bit atomic per block.
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads) k_sum(const int32_t *col, const uint8_t *flags, uint64_t n, uint64_t *acc)
+__global__ void __launch_bounds__(kMaxBlock) k_sum(const int32_t *col, const uint8_t *flags, uint64_t n, uint64_t *acc)
 {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -246,7 +276,7 @@ __global__ void __launch_bounds__(kThreads) k_sum(const int32_t *col, const uint
 
 // K16
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads) k_count(const uint8_t *flags, uint64_t n, uint64_t *out)
+__global__ void __launch_bounds__(kMaxBlock) k_count(const uint8_t *flags, uint64_t n, uint64_t *out)
 {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -269,7 +299,7 @@ __global__ void k_minmax_init(int32_t *mm)
 }
 
 template <bool VEC>
-__global__ void __launch_bounds__(kThreads) k_minmax(const int32_t *col, uint64_t n, int32_t *mm)
+__global__ void __launch_bounds__(kMaxBlock) k_minmax(const int32_t *col, uint64_t n, int32_t *mm)
 {
     const uint64_t tid = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -426,7 +456,7 @@ struct OccToFlags {
 };
 
 // ---------------------------------------------------------------- K10 - K13
-__global__ void __launch_bounds__(kThreads) k_build_keys(const int32_t *key, const uint8_t *flags, uint64_t n,
+__global__ void __launch_bounds__(kMaxBlock) k_build_keys(const int32_t *key, const uint8_t *flags, uint64_t n,
                                                          uint8_t *ht, int32_t mn, int32_t len)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -437,7 +467,7 @@ __global__ void __launch_bounds__(kThreads) k_build_keys(const int32_t *key, con
     }
 }
 
-__global__ void __launch_bounds__(kThreads) k_build_kv(const int32_t *key, const int32_t *val, const uint8_t *flags,
+__global__ void __launch_bounds__(kMaxBlock) k_build_kv(const int32_t *key, const int32_t *val, const uint8_t *flags,
                                                        uint64_t n, int32_t *ht2, int32_t mn, int32_t len)
 {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -623,7 +653,7 @@ __global__ void __launch_bounds__(kThreads) k_compact_write(const uint8_t *flags
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_gather(const T *src, const int32_t *ids, const uint32_t *count, T *dst,
+__global__ void __launch_bounds__(kMaxBlock) k_gather(const T *src, const int32_t *ids, const uint32_t *count, T *dst,
                                                      uint64_t cap)
 {
     const uint64_t c = min((uint64_t)*count, cap);
@@ -745,7 +775,7 @@ extern "C" {
 int sdb_fill_u8(uint8_t *flags, uint64_t n, uint8_t v, sdb_stream_t stream)
 {
     if (n && !flags) return sdb_set_error(SDB_ERR_INVALID, "sdb_fill_u8: NULL buffer");
-    return launch_map(n, flags_ok(flags), FillU8{flags, v}, (cudaStream_t)stream, "sdb_fill_u8");
+    return launch_map(n, flags_ok(flags), FillU8{flags, v}, (cudaStream_t)stream, "sdb_fill_u8", SDB_OPK_FILL_U8);
 }
 
 int sdb_select_lit(const int32_t *col, int32_t v, int cmp_op, int logic_op, const uint8_t *in, uint8_t *out,
@@ -754,7 +784,7 @@ int sdb_select_lit(const int32_t *col, int32_t v, int cmp_op, int logic_op, cons
     SDB_REQUIRE_ALIGNED(nat4({col}), "sdb_select_lit");
     if (n && (!col || !in || !out)) return sdb_set_error(SDB_ERR_INVALID, "sdb_select_lit: NULL buffer");
     bool vec = col_ok(col) && flags_ok(in) && flags_ok(out);
-    return launch_map(n, vec, SelectLit{col, v, cmp_op, logic_op, in, out}, (cudaStream_t)stream, "sdb_select_lit");
+    return launch_map(n, vec, SelectLit{col, v, cmp_op, logic_op, in, out}, (cudaStream_t)stream, "sdb_select_lit", SDB_OPK_SELECT_LIT);
 }
 
 int sdb_select_cols(const int32_t *a, const int32_t *b, int cmp_op, int logic_op, const uint8_t *in, uint8_t *out,
@@ -763,21 +793,21 @@ int sdb_select_cols(const int32_t *a, const int32_t *b, int cmp_op, int logic_op
     SDB_REQUIRE_ALIGNED(nat4({a, b}), "sdb_select_cols");
     if (n && (!a || !b || !in || !out)) return sdb_set_error(SDB_ERR_INVALID, "sdb_select_cols: NULL buffer");
     bool vec = col_ok(a) && col_ok(b) && flags_ok(in) && flags_ok(out);
-    return launch_map(n, vec, SelectCols{a, b, cmp_op, logic_op, in, out}, (cudaStream_t)stream, "sdb_select_cols");
+    return launch_map(n, vec, SelectCols{a, b, cmp_op, logic_op, in, out}, (cudaStream_t)stream, "sdb_select_cols", SDB_OPK_SELECT_COLS);
 }
 
 int sdb_logical(int logic_op, const uint8_t *in, const uint8_t *local, uint8_t *out, uint64_t n, sdb_stream_t stream)
 {
     if (n && (!in || !local || !out)) return sdb_set_error(SDB_ERR_INVALID, "sdb_logical: NULL buffer");
     bool vec = flags_ok(in) && flags_ok(local) && flags_ok(out);
-    return launch_map(n, vec, Logical{logic_op, in, local, out}, (cudaStream_t)stream, "sdb_logical");
+    return launch_map(n, vec, Logical{logic_op, in, local, out}, (cudaStream_t)stream, "sdb_logical", SDB_OPK_LOGICAL);
 }
 
 int sdb_fill_i32(int32_t *dst, int32_t v, uint64_t n, sdb_stream_t stream)
 {
     SDB_REQUIRE_ALIGNED(nat4({dst}), "sdb_fill_i32");
     if (n && !dst) return sdb_set_error(SDB_ERR_INVALID, "sdb_fill_i32: NULL buffer");
-    return launch_map(n, col_ok(dst), FillI32{dst, v}, (cudaStream_t)stream, "sdb_fill_i32");
+    return launch_map(n, col_ok(dst), FillI32{dst, v}, (cudaStream_t)stream, "sdb_fill_i32", SDB_OPK_FILL_I32);
 }
 
 static int binop_common(int32_t *res, const int32_t *a, const int32_t *b, int32_t la, int32_t lb, int op, int mode,
@@ -788,7 +818,7 @@ static int binop_common(int32_t *res, const int32_t *a, const int32_t *b, int32_
     if (n && (!res || !flags || (mode != 1 && !a) || (mode != 2 && !b)))
         return sdb_set_error(SDB_ERR_INVALID, "%s: NULL buffer", what);
     bool vec = col_ok(res) && col_ok(a) && col_ok(b) && flags_ok(flags);
-    return launch_map(n, vec, Binop{res, a, b, la, lb, op, mode, flags}, (cudaStream_t)stream, what);
+    return launch_map(n, vec, Binop{res, a, b, la, lb, op, mode, flags}, (cudaStream_t)stream, what, SDB_OPK_BINOP);
 }
 
 int sdb_binop_cc(int32_t *res, const int32_t *a, const int32_t *b, int bin_op, const uint8_t *flags, uint64_t n,
@@ -815,10 +845,11 @@ int sdb_sum_i32_u64(const int32_t *col, const uint8_t *flags, uint64_t n, uint64
     if (!acc || (n && (!col || !flags))) return sdb_set_error(SDB_ERR_INVALID, "sdb_sum_i32_u64: NULL buffer");
     if (n == 0) return SDB_OK;
     cudaStream_t s = (cudaStream_t)stream;
+    const LaunchShape sh = op_shape(SDB_OPK_SUM, n, 4);
     if (col_ok(col) && flags_ok(flags))
-        k_sum<true><<<sdb::grid_for((n + 7) / 8, kThreads, 4), kThreads, 0, s>>>(col, flags, n, acc);
+        k_sum<true><<<grid_of((n + 7) / 8, sh), sh.block, 0, s>>>(col, flags, n, acc);
     else
-        k_sum<false><<<sdb::grid_for(n, kThreads, 4), kThreads, 0, s>>>(col, flags, n, acc);
+        k_sum<false><<<grid_of(n, sh), sh.block, 0, s>>>(col, flags, n, acc);
     return sdb_check_launch("sdb_sum_i32_u64");
 }
 
@@ -829,10 +860,11 @@ int sdb_count_flags(const uint8_t *flags, uint64_t n, uint64_t *out, sdb_stream_
     cudaStream_t s = (cudaStream_t)stream;
     if (cudaMemsetAsync(out, 0, sizeof(uint64_t), s) != cudaSuccess) return sdb_check_launch("sdb_count_flags");
     if (n == 0) return SDB_OK;
+    const LaunchShape sh = op_shape(SDB_OPK_COUNT_FLAGS, n, 4);
     if (flags_ok(flags))
-        k_count<true><<<sdb::grid_for((n + 7) / 8, kThreads, 4), kThreads, 0, s>>>(flags, n, out);
+        k_count<true><<<grid_of((n + 7) / 8, sh), sh.block, 0, s>>>(flags, n, out);
     else
-        k_count<false><<<sdb::grid_for(n, kThreads, 4), kThreads, 0, s>>>(flags, n, out);
+        k_count<false><<<grid_of(n, sh), sh.block, 0, s>>>(flags, n, out);
     return sdb_check_launch("sdb_count_flags");
 }
 
@@ -842,10 +874,11 @@ int sdb_min_max_i32(const int32_t *col, uint64_t n, int32_t *minmax, sdb_stream_
     if (n == 0 || !col || !minmax) return sdb_set_error(SDB_ERR_INVALID, "sdb_min_max_i32: empty column or NULL buffer");
     cudaStream_t s = (cudaStream_t)stream;
     k_minmax_init<<<1, 1, 0, s>>>(minmax);
+    const LaunchShape sh = op_shape(SDB_OPK_MIN_MAX, n, 4);
     if (col_ok(col))
-        k_minmax<true><<<sdb::grid_for((n + 7) / 8, kThreads, 4), kThreads, 0, s>>>(col, n, minmax);
+        k_minmax<true><<<grid_of((n + 7) / 8, sh), sh.block, 0, s>>>(col, n, minmax);
     else
-        k_minmax<false><<<sdb::grid_for(n, kThreads, 4), kThreads, 0, s>>>(col, n, minmax);
+        k_minmax<false><<<grid_of(n, sh), sh.block, 0, s>>>(col, n, minmax);
     sdb_count_launches(1);
     return sdb_check_launch("sdb_min_max_i32");
 }
@@ -909,7 +942,7 @@ int sdb_occ_to_flags(const uint32_t *occ, uint8_t *flags, uint64_t P, sdb_stream
     SDB_REQUIRE_ALIGNED(nat4({occ}), "sdb_occ_to_flags");
     if (P && (!occ || !flags)) return sdb_set_error(SDB_ERR_INVALID, "sdb_occ_to_flags: NULL buffer");
     return launch_map(P, col_ok(occ) && flags_ok(flags), OccToFlags{occ, flags}, (cudaStream_t)stream,
-                      "sdb_occ_to_flags");
+                      "sdb_occ_to_flags", SDB_OPK_OCC_TO_FLAGS);
 }
 
 int sdb_ht_build_keys(const int32_t *key, const uint8_t *flags, uint64_t n, uint8_t *ht, int32_t min, int32_t len,
@@ -918,7 +951,8 @@ int sdb_ht_build_keys(const int32_t *key, const uint8_t *flags, uint64_t n, uint
     SDB_REQUIRE_ALIGNED(nat4({key}), "sdb_ht_build_keys");
     if (n && (!key || !flags || !ht)) return sdb_set_error(SDB_ERR_INVALID, "sdb_ht_build_keys: NULL buffer");
     if (n == 0) return SDB_OK;
-    k_build_keys<<<sdb::grid_for(n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(key, flags, n, ht, min, len);
+    const LaunchShape sh = op_shape(SDB_OPK_BUILD_KEYS, n, 8);
+    k_build_keys<<<grid_of(n, sh), sh.block, 0, (cudaStream_t)stream>>>(key, flags, n, ht, min, len);
     return sdb_check_launch("sdb_ht_build_keys");
 }
 
@@ -928,7 +962,7 @@ int sdb_probe_semi(const int32_t *key, const uint8_t *in, uint8_t *out, uint64_t
     SDB_REQUIRE_ALIGNED(nat4({key}), "sdb_probe_semi");
     if (n && (!key || !in || !out || !ht)) return sdb_set_error(SDB_ERR_INVALID, "sdb_probe_semi: NULL buffer");
     bool vec = col_ok(key) && flags_ok(in) && flags_ok(out);
-    return launch_map(n, vec, ProbeSemi{key, in, out, ht, min, max}, (cudaStream_t)stream, "sdb_probe_semi");
+    return launch_map(n, vec, ProbeSemi{key, in, out, ht, min, max}, (cudaStream_t)stream, "sdb_probe_semi", SDB_OPK_PROBE_SEMI);
 }
 
 int sdb_ht_build_kv(const int32_t *key, const int32_t *val, const uint8_t *flags, uint64_t n, int32_t *ht2,
@@ -937,7 +971,8 @@ int sdb_ht_build_kv(const int32_t *key, const int32_t *val, const uint8_t *flags
     SDB_REQUIRE_ALIGNED(nat4({key, val, ht2}), "sdb_ht_build_kv");
     if (n && (!key || !val || !flags || !ht2)) return sdb_set_error(SDB_ERR_INVALID, "sdb_ht_build_kv: NULL buffer");
     if (n == 0) return SDB_OK;
-    k_build_kv<<<sdb::grid_for(n, kThreads), kThreads, 0, (cudaStream_t)stream>>>(key, val, flags, n, ht2, min, len);
+    const LaunchShape sh = op_shape(SDB_OPK_BUILD_KV, n, 8);
+    k_build_kv<<<grid_of(n, sh), sh.block, 0, (cudaStream_t)stream>>>(key, val, flags, n, ht2, min, len);
     return sdb_check_launch("sdb_ht_build_kv");
 }
 
@@ -950,8 +985,8 @@ int sdb_probe_full(const int32_t *key, int32_t *val_out, const uint8_t *in, uint
     bool vec = col_ok(key) && flags_ok(in) && flags_ok(out);
     cudaStream_t s = (cudaStream_t)stream;
     if (sdb::aligned(ht2, 8))
-        return launch_map(n, vec, ProbeFull<true>{key, val_out, in, out, ht2, min, max}, s, "sdb_probe_full");
-    return launch_map(n, vec, ProbeFull<false>{key, val_out, in, out, ht2, min, max}, s, "sdb_probe_full");
+        return launch_map(n, vec, ProbeFull<true>{key, val_out, in, out, ht2, min, max}, s, "sdb_probe_full", SDB_OPK_PROBE_FULL);
+    return launch_map(n, vec, ProbeFull<false>{key, val_out, in, out, ht2, min, max}, s, "sdb_probe_full", SDB_OPK_PROBE_FULL);
 }
 
 size_t sdb_compact_scratch_bytes(uint64_t n)
@@ -1092,7 +1127,8 @@ int sdb_gather_i32(const int32_t *src, const int32_t *ids, const uint32_t *count
     SDB_REQUIRE_ALIGNED(nat4({src, ids, count, dst}), "sdb_gather_i32");
     if (cap == 0) return SDB_OK;
     if (!src || !ids || !count || !dst) return sdb_set_error(SDB_ERR_INVALID, "sdb_gather_i32: NULL buffer");
-    k_gather<int32_t><<<sdb::grid_for(cap, kThreads), kThreads, 0, (cudaStream_t)stream>>>(src, ids, count, dst, cap);
+    const LaunchShape sh = op_shape(SDB_OPK_GATHER, cap, 8);
+    k_gather<int32_t><<<grid_of(cap, sh), sh.block, 0, (cudaStream_t)stream>>>(src, ids, count, dst, cap);
     return sdb_check_launch("sdb_gather_i32");
 }
 
@@ -1102,7 +1138,8 @@ int sdb_gather_u64(const uint64_t *src, const int32_t *ids, const uint32_t *coun
     SDB_REQUIRE_ALIGNED(nat4({ids, count}) && nat8(src) && nat8(dst), "sdb_gather_u64");
     if (cap == 0) return SDB_OK;
     if (!src || !ids || !count || !dst) return sdb_set_error(SDB_ERR_INVALID, "sdb_gather_u64: NULL buffer");
-    k_gather<uint64_t><<<sdb::grid_for(cap, kThreads), kThreads, 0, (cudaStream_t)stream>>>(src, ids, count, dst, cap);
+    const LaunchShape sh = op_shape(SDB_OPK_GATHER, cap, 8);
+    k_gather<uint64_t><<<grid_of(cap, sh), sh.block, 0, (cudaStream_t)stream>>>(src, ids, count, dst, cap);
     return sdb_check_launch("sdb_gather_u64");
 }
 
@@ -1158,6 +1195,36 @@ int sdb_gen_dates_cpu(int32_t *dst, uint64_t n, uint64_t row0, uint64_t seed, ui
     if (n && !dst) return sdb_set_error(SDB_ERR_INVALID, "sdb_gen_dates_cpu: NULL buffer");
     const uint64_t key = sdb::stream_key(seed, stream_id);
     parallel_rows(n, [=](uint64_t i) { dst[i] = sdb::datekey_of_day(sdb::uniform_from_key(key, row0 + i, 0, ndays - 1)); });
+    return SDB_OK;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+int sdb_op_tune_set(int op_kernel, uint64_t rows, int block, int blocks_per_sm)
+{
+    if (op_kernel < 0 || op_kernel >= SDB_OPK_COUNT) return sdb_set_error(SDB_ERR_INVALID, "sdb_op_tune_set: bad kernel");
+    int32_t e = 0;
+    if (block != 0 || blocks_per_sm != 0) {
+        if (block != 128 && block != 256 && block != 512)
+            return sdb_set_error(SDB_ERR_INVALID, "sdb_op_tune_set: block must be 128, 256 or 512");
+        if (blocks_per_sm < 1 || blocks_per_sm > 32 || blocks_per_sm * block > 2048)
+            return sdb_set_error(SDB_ERR_INVALID, "sdb_op_tune_set: blocks_per_sm must be 1..32 and fit 2048 threads");
+        e = (block << 8) | blocks_per_sm;
+    }
+    g_op_tune[op_kernel][op_bucket(rows)].store(e, std::memory_order_relaxed);
+    return SDB_OK;
+}
+
+int sdb_op_tune_get(int op_kernel, uint64_t rows, int *block, int *blocks_per_sm)
+{
+    if (op_kernel < 0 || op_kernel >= SDB_OPK_COUNT || !block || !blocks_per_sm)
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_op_tune_get: bad argument");
+    const int def = (op_kernel == SDB_OPK_SUM || op_kernel == SDB_OPK_COUNT_FLAGS || op_kernel == SDB_OPK_MIN_MAX) ? 4 : 8;
+    const LaunchShape sh = op_shape(op_kernel, rows, def);
+    *block = sh.block;
+    *blocks_per_sm = sh.per_sm;
     return SDB_OK;
 }
 

@@ -1,4 +1,5 @@
 """The autotuner's table format and its loading into the library (no GPU)."""
+import ctypes
 import json
 
 from sycldb_gb300 import autotune, capi
@@ -67,3 +68,28 @@ def test_measured_buckets_cover_the_sizes_above_them(tmp_path):
     finally:
         capi.force_chain_variant(-1)
         autotune.load_default()
+
+
+def test_operator_launch_shapes_set_get_and_load():
+    L = capi.lib()
+    b, p = ctypes.c_int(), ctypes.c_int()
+    k = capi.OP_KERNELS.index("probe_full")
+    capi.check(L.sdb_op_tune_get(k, 1 << 24, ctypes.byref(b), ctypes.byref(p)))
+    assert (b.value, p.value) == (256, 8)
+    assert L.sdb_op_tune_set(k, 1 << 24, 384, 2) == capi.SDB_ERR_INVALID
+    assert L.sdb_op_tune_set(k, 1 << 24, 512, 8) == capi.SDB_ERR_INVALID  # over 2048 threads per SM
+    assert L.sdb_op_tune_set(len(capi.OP_KERNELS), 1, 256, 4) == capi.SDB_ERR_INVALID
+    try:
+        table = {"entries": [], "op_entries": [
+            {"kernel": "probe_full", "rows_bucket": 20, "block": 512, "blocks_per_sm": 2},
+            {"kernel": "probe_full", "rows_bucket": 24, "block": 128, "blocks_per_sm": 16}]}
+        assert autotune.load_ops(table) == 2
+        for rows, want in ((1 << 19, (256, 8)), (1 << 21, (512, 2)), (1 << 24, (128, 16)), (1 << 30, (128, 16))):
+            capi.check(L.sdb_op_tune_get(k, rows, ctypes.byref(b), ctypes.byref(p)))
+            assert (b.value, p.value) == want, rows
+        s = capi.OP_KERNELS.index("sum")
+        capi.check(L.sdb_op_tune_get(s, 1 << 24, ctypes.byref(b), ctypes.byref(p)))
+        assert (b.value, p.value) == (256, 4)
+    finally:
+        for bk in range(40):
+            capi.check(L.sdb_op_tune_set(k, 1 << bk, 0, 0))

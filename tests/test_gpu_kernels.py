@@ -324,3 +324,27 @@ def test_compact_gather_occ_equals_occ_to_flags_then_compact_gather(n):
     assert c == sel.size
     for (buf, ptr), x in zip(outs, (a, u)):
         assert np.array_equal(host(buf, ptr, c, x.dtype), x[sel])
+
+
+def _force_op_shape(block, per_sm):
+    for k in range(len(capi.OP_KERNELS)):
+        for b in range(40):
+            capi.check(capi.lib().sdb_op_tune_set(k, 1 << b, block, per_sm))
+
+
+@pytest.mark.parametrize("shape", [(128, 2), (512, 4), (512, 1), (128, 16)])
+def test_every_launch_shape_gives_the_golden_vectors(shape):
+    """The operator kernels' tuned launch shapes (threads per block x blocks
+    per SM) change only how the rows are spread over the grid: every golden
+    case, and the oracle sweeps at sizes beyond one wave, give the same."""
+    try:
+        _force_op_shape(*shape)
+        for case in CASES:
+            got = run_gpu(case)
+            for k in case["outputs"]:
+                assert np.array_equal(got[k], ARR["%s/out/%s" % (case["name"], k)]), (case["name"], shape)
+        for n in (1000, (1 << 20) + 5, 3 << 20):
+            test_select_and_sum_vs_oracle(n)
+        test_compaction_and_gather(1 << 20, 0.3)
+    finally:
+        _force_op_shape(0, 0)
