@@ -70,10 +70,17 @@ def test_measured_buckets_cover_the_sizes_above_them(tmp_path):
         autotune.load_default()
 
 
+def _clear_op_shapes():
+    for kk in range(len(capi.OP_KERNELS)):
+        for bk in range(40):
+            capi.check(capi.lib().sdb_op_tune_set(kk, 1 << bk, 0, 0))
+
+
 def test_operator_launch_shapes_set_get_and_load():
     L = capi.lib()
     b, p = ctypes.c_int(), ctypes.c_int()
     k = capi.OP_KERNELS.index("probe_full")
+    _clear_op_shapes()  # the defaults (an engine may have loaded the committed table)
     capi.check(L.sdb_op_tune_get(k, 1 << 24, ctypes.byref(b), ctypes.byref(p)))
     assert (b.value, p.value) == (256, 8)
     assert L.sdb_op_tune_set(k, 1 << 24, 384, 2) == capi.SDB_ERR_INVALID
@@ -91,5 +98,5 @@ def test_operator_launch_shapes_set_get_and_load():
         capi.check(L.sdb_op_tune_get(s, 1 << 24, ctypes.byref(b), ctypes.byref(p)))
         assert (b.value, p.value) == (256, 4)
     finally:
-        for bk in range(40):
-            capi.check(L.sdb_op_tune_set(k, 1 << bk, 0, 0))
+        _clear_op_shapes()
+        autotune.load_default()
