@@ -14,10 +14,13 @@
 // the last key's low word to the first key's high word.  Each word is
 // gathered once through the current order into a word array, then sorted 8
 // bits per pass with (word, row id) pairs carried along, each pass a stable
-// counting sort of 256-row blocks: per block digit counts (digit-major, so
-// that one exclusive scan gives every block's first slot per digit), the
-// scan, then a scatter in which a row's place among equal digits of its
-// block comes from a warp match and per-warp counts.
+// counting sort of 4096-row tiles (256 threads x 16 rows, row j * 256 + t of
+// a tile in thread t): per tile digit counts (digit-major, so that one
+// exclusive scan gives every tile's first slot per digit), the scan, then a
+// scatter that walks the tile's 16 rows of 256 in order -- a row's place among
+// equal digits comes from the rows of earlier steps (a running count per
+// digit), of earlier warps in this step (per-warp counts) and of lower lanes
+// of its own warp (a warp match).
 #include <algorithm>
 #include <cstdint>
 #include <utility>
@@ -26,7 +29,10 @@
 
 namespace {
 
-constexpr int kSortThreads = 256;  // rows per block
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 16;                          // rows per thread
+constexpr int kSortTile = kSortThreads * kSortItems;    // rows per block
+constexpr int kSortWarps = kSortThreads / 32;
 constexpr int kScanThreads = 1024;
 
 struct SortPass {
@@ -59,45 +65,98 @@ __global__ void k_gather_word(const SortPass p, const uint32_t *__restrict__ per
 __global__ void __launch_bounds__(kSortThreads) k_radix_count(const uint32_t *__restrict__ word, int shift,
                                                                  uint32_t n, uint32_t *__restrict__ hist, uint32_t nb)
 {
-    __shared__ uint32_t cnt[256];
-    cnt[threadIdx.x] = 0;
+    __shared__ uint32_t cnt[kSortWarps][256];
+    const uint32_t warp = threadIdx.x >> 5;
+    for (uint32_t k = threadIdx.x; k < kSortWarps * 256; k += kSortThreads) (&cnt[0][0])[k] = 0;
     __syncthreads();
-    const uint32_t i = blockIdx.x * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(word[i] >> shift) & 255u], 1u);
+    const uint32_t tile = blockIdx.x * (uint32_t)kSortTile;
+#pragma unroll 4
+    for (int j = 0; j < kSortItems; j++) {
+        const uint32_t i = tile + (uint32_t)j * kSortThreads + threadIdx.x;
+        if (i < n) atomicAdd(&cnt[warp][(word[i] >> shift) & 255u], 1u);
+    }
     __syncthreads();
-    hist[threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+    uint32_t t = 0;
+#pragma unroll
+    for (int w = 0; w < kSortWarps; w++) t += cnt[w][threadIdx.x];
+    hist[threadIdx.x * nb + blockIdx.x] = t;
 }
 
-// Moves (word, row id) pair i to its slot of this digit pass.
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s_warp, uint32_t &total);
+
+// Moves the (word, row id) pairs of one tile to their slots of this digit
+// pass, stably.  Warp w owns the tile's rows [512 w, 512 w + 512) and ranks
+// them on its own in 16 steps of 32 (a warp match gives the lanes of one
+// digit; a per-warp count per digit carries the earlier steps), with no block
+// barrier.  Then per digit the counts of earlier warps and of smaller digits
+// give each row its place in the tile order; the tile is ordered in shared
+// memory and goes out in runs of equal digits, so consecutive threads write
+// consecutive slots.
 __global__ void __launch_bounds__(kSortThreads) k_radix_scatter(const uint32_t *__restrict__ word,
                                                                    const uint32_t *__restrict__ perm, int shift,
                                                                    uint32_t n, const uint32_t *__restrict__ offs,
                                                                    uint32_t nb, uint32_t *__restrict__ word_out,
                                                                    uint32_t *__restrict__ perm_out)
 {
-    __shared__ uint32_t wcnt[kSortThreads / 32][256];
+    constexpr uint32_t kWarpRows = 32 * kSortItems;
+    __shared__ uint32_t s_w[kSortTile], s_r[kSortTile];
+    __shared__ uint32_t wc[kSortWarps][256];  // per warp and digit: count, then the earlier warps' count
+    __shared__ uint32_t first[256], tpre[256], s_warp[32];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    for (uint32_t k = threadIdx.x; k < (kSortThreads / 32) * 256; k += kSortThreads) (&wcnt[0][0])[k] = 0;
+    const uint32_t tile = blockIdx.x * (uint32_t)kSortTile;
+    const uint32_t rows = min((uint32_t)kSortTile, n - tile);
+    for (uint32_t k = threadIdx.x; k < kSortWarps * 256; k += kSortThreads) (&wc[0][0])[k] = 0;
+    first[threadIdx.x] = offs[threadIdx.x * nb + blockIdx.x];
     __syncthreads();
-    const uint32_t i = blockIdx.x * kSortThreads + threadIdx.x;
-    const bool valid = i < n;
-    const unsigned vmask = __ballot_sync(0xffffffffu, valid);
-    uint32_t w = 0, row = 0, d = 0, below = 0;
-    if (valid) {
-        w = word[i];
-        row = perm[i];
-        d = (w >> shift) & 255u;
-        const unsigned peers = __match_any_sync(vmask, d);
-        below = __popc(peers & ((1u << lane) - 1u));
-        if (below == 0) wcnt[warp][d] = __popc(peers);  // the lowest lane of each digit group
+    uint32_t w[kSortItems], r[kSortItems], rank[kSortItems];
+    const uint32_t base = warp * kWarpRows;
+#pragma unroll
+    for (int j = 0; j < kSortItems; j++) {
+        const uint32_t k = base + (uint32_t)j * 32 + lane;
+        const bool valid = k < rows;
+        const unsigned vmask = __ballot_sync(0xffffffffu, valid);
+        rank[j] = 0xFFFFFFFFu;
+        if (vmask == 0) continue;  // warp-uniform
+        if (valid) {
+            w[j] = word[tile + k];
+            r[j] = perm[tile + k];
+            const uint32_t d = (w[j] >> shift) & 255u;
+            const unsigned peers = __match_any_sync(vmask, d);
+            const uint32_t below = __popc(peers & ((1u << lane) - 1u));
+            rank[j] = wc[warp][d] + below;
+            __syncwarp(vmask);
+            if (below == 0) wc[warp][d] += __popc(peers);  // the group's lowest lane
+        }
+        __syncwarp();
     }
     __syncthreads();
-    if (valid) {
-        uint32_t before = below;
-        for (uint32_t q = 0; q < warp; q++) before += wcnt[q][d];
-        const uint32_t at = offs[d * nb + blockIdx.x] + before;
-        word_out[at] = w;
-        perm_out[at] = row;
+    // per digit: earlier warps' counts (in place) and the tile's count
+    uint32_t cnt = 0;
+#pragma unroll
+    for (int q = 0; q < kSortWarps; q++) {
+        const uint32_t c = wc[q][threadIdx.x];
+        wc[q][threadIdx.x] = cnt;
+        cnt += c;
+    }
+    uint32_t total;
+    tpre[threadIdx.x] = block_exclusive_scan(cnt, s_warp, total);
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < kSortItems; j++) {
+        if (rank[j] == 0xFFFFFFFFu) continue;
+        const uint32_t d = (w[j] >> shift) & 255u;
+        const uint32_t at = tpre[d] + wc[warp][d] + rank[j];
+        s_w[at] = w[j];
+        s_r[at] = r[j];
+    }
+    __syncthreads();
+    // out in tile order: slot p of digit d goes to first[d] + (p - tpre[d])
+    for (uint32_t p = threadIdx.x; p < rows; p += kSortThreads) {
+        const uint32_t x = s_w[p];
+        const uint32_t d = (x >> shift) & 255u;
+        const uint32_t at = first[d] + (p - tpre[d]);
+        word_out[at] = x;
+        perm_out[at] = s_r[p];
     }
 }
 
@@ -174,7 +233,7 @@ struct Scratch {
 
 size_t scratch_layout(uint64_t n, char *base, Scratch *s)
 {
-    const uint64_t nb = (n + kSortThreads - 1) / kSortThreads;
+    const uint64_t nb = (n + kSortTile - 1) / kSortTile;
     const uint64_t m = nb * 256;
     const uint64_t nsum = (m + kScanThreads - 1) / kScanThreads;
     size_t off = 0;
@@ -220,7 +279,7 @@ int sdb_sort_rows(const void *const *keys, const int *key_types, const int *desc
     Scratch sc;
     scratch_layout(n, static_cast<char *>(scratch), &sc);
     const uint32_t n32 = (uint32_t)n;
-    const uint32_t nb = (n32 + kSortThreads - 1) / kSortThreads;
+    const uint32_t nb = (n32 + kSortTile - 1) / kSortTile;
     const uint32_t m = nb * 256;
     const uint32_t nsum = (m + kScanThreads - 1) / kScanThreads;
     k_iota<<<std::min<uint32_t>((n32 + 255) / 256, 4096), 256, 0, s>>>(perm, n32);

@@ -34,7 +34,7 @@ def gpu_sort(keys, desc):
     return host(pb, perm, n, np.uint32)
 
 
-@pytest.mark.parametrize("n", [1, 2, 255, 256, 257, 1000, 65_537, 1_000_003])
+@pytest.mark.parametrize("n", [1, 2, 255, 256, 257, 1000, 4095, 4096, 4097, 3 * 4096 + 1, 65_537, 1_000_003])
 def test_sort_matches_a_stable_lexicographic_sort(n):
     rng = np.random.default_rng(n)
     k0 = rng.integers(-3, 4, n).astype(np.int32)                                  # few values: many ties
