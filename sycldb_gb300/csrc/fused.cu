@@ -1158,14 +1158,16 @@ template <int NREGS>
 struct Level2 {
     VRow<NREGS> r;   // lane j: pending row j
     uint32_t n = 0;  // pending rows (warp-uniform)
+    uint8_t *src = nullptr;  // the warp's 32-entry list: entry k = lane of the k-th live row of a group
 };
 
-// Row k (0-based, k < cnt) among the warp's live rows; every lane calls it
-// with its own k (k >= cnt: no row).
+// Row k (0-based, k < cnt) among the warp's live rows, whose lanes the
+// caller listed in src (entry k = lane of the k-th live row); every lane
+// calls it with its own k (k >= cnt: no row).
 template <int NREGS>
-__device__ __forceinline__ VRow<NREGS> take_row(const VRow<NREGS> &R, unsigned live, uint32_t k, uint32_t cnt)
+__device__ __forceinline__ VRow<NREGS> take_row(const VRow<NREGS> &R, const uint8_t *src_list, uint32_t k, uint32_t cnt)
 {
-    const int src = k < cnt ? (int)__fns(live, 0, (int)k + 1) : 0;
+    const int src = k < cnt ? (int)src_list[k] : 0;
     VRow<NREGS> o;
     o.v0 = __shfl_sync(0xffffffffu, R.v0, src);
     o.v1 = __shfl_sync(0xffffffffu, R.v1, src);
@@ -1197,10 +1199,14 @@ __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &
     const unsigned live = __ballot_sync(0xffffffffu, R.live);
     const uint32_t cnt = __popc(live);
     if (cnt == 0) return;
+    // list the live lanes in order (each writes its own entry), so that every
+    // lane finds the source of its row with one load
+    if (R.live) Q.src[__popc(live & ((1u << lane) - 1u))] = (uint8_t)lane;
+    __syncwarp();
     const uint32_t n2 = Q.n;
     {
         const uint32_t k = lane >= n2 ? lane - n2 : 32u;
-        const VRow<NREGS> got = take_row(R, live, k, cnt);
+        const VRow<NREGS> got = take_row(R, Q.src, k, cnt);
         if (lane >= n2 && k < cnt) Q.r = got;
     }
     if (n2 + cnt >= 32) {
@@ -1208,12 +1214,13 @@ __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &
         F.live = true;
         level2_run<TERM, NREGS, SPLIT, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
         const uint32_t used = 32 - n2;
-        const VRow<NREGS> got = take_row(R, live, lane + used, cnt);
+        const VRow<NREGS> got = take_row(R, Q.src, lane + used, cnt);
         if (lane < cnt - used) Q.r = got;
         Q.n = cnt - used;
     } else {
         Q.n = n2 + cnt;
     }
+    __syncwarp();  // every lane has read the list before it is written again
 }
 
 // Whether CARRY 2 uses the second level: there are ops after the first
@@ -1441,9 +1448,11 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
     __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
     __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
     __shared__ uint64_t s_part[kThreads / 32];
+    __shared__ uint8_t s_l2src[CARRY == 2 ? kThreads : 1];
     uint32_t carry = 0;  // rows the warp carries (warp-uniform)
     int4 ce = make_int4(0, 0, 0, 0);
     Level2<NREGS> Q;
+    Q.src = s_l2src + (CARRY == 2 ? (threadIdx.x & ~31u) : 0u);
     const bool direct = L.P <= kDenseCap;
     uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
     group_table_reset<TERM>(s_key, s_sum);
@@ -1496,9 +1505,11 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
     k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
             uint32_t *__restrict__ head)
 {
+    __shared__ uint8_t s_l2src[CARRY == 2 ? kThreads : 1];
     uint32_t carry = 0;
     int4 ce = make_int4(0, 0, 0, 0);
     Level2<NREGS> Q;
+    Q.src = s_l2src + (CARRY == 2 ? (threadIdx.x & ~31u) : 0u);
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
