@@ -334,7 +334,11 @@ int sdb_fused_chain(const sdb_chain_desc *chain, sdb_stream_t stream);
  * the next tile, so the one-row-per-lane ops run on full warps (chains whose
  * later ops write no column).  7: as 6, and the rows that survive the first
  * op after the compaction are compacted again, across lanes in registers,
- * so the later ops and the terminal run on full warps.  Shapes without a
+ * so the later ops and the terminal run on full warps.  8: as 7, and the
+ * columns that only the ops after that second compaction read are not
+ * staged: a surviving row carries its row number and loads them there
+ * (only the sectors holding such rows are read; chains under 2^31 rows,
+ * else as 7).  Shapes without a
  * specialised pass fall back to the general pass.  Default (and an unset
  * tuning entry): 5. */
 int sdb_fused_chain_variant(const sdb_chain_desc *chain, int variant, sdb_stream_t stream);
@@ -364,7 +368,7 @@ int sdb_op_tune_get(int op_kernel, uint64_t rows, int *block, int *blocks_per_sm
 
 /* Registers (1..8) a chain needs, or a negative status if it is invalid. */
 int sdb_chain_registers(const sdb_chain_desc *chain);
-/* 1 when the chain has a shape-specialised instantiation (variants 3-7), 0
+/* 1 when the chain has a shape-specialised instantiation (variants 3-8), 0
  * when only the general pass runs it, or a negative status if it is invalid.
  * Host-only. */
 int sdb_chain_specialised(const sdb_chain_desc *chain);

@@ -1,6 +1,6 @@
 """Autotuner for the fused fact-side pass.
 
-The fused chain has eight kernel variants (``sdb_fused_chain_variant``):
+The fused chain has nine kernel variants (``sdb_fused_chain_variant``):
 
   0/1/2  general interpreter, 4 / 8 / 16 rows per thread (items per thread)
   3      shape-specialised pass, every row through every op
@@ -10,6 +10,8 @@ The fused chain has eight kernel variants (``sdb_fused_chain_variant``):
   6      as 5, surviving rows that do not fill a warp carried into the next tile
   7      as 6, and the rows that survive the first row-per-lane op compacted
          again (across lanes, in registers) so the later ops run on full warps
+  8      as 7, and the columns that only the ops after that second compaction
+         read are not staged: each surviving row loads them by row number
 
 The fused passes keep 256 threads per block: their copy ring, per-warp row
 lists and tile shape (256 x 4 rows) are laid out for it, and the variants
@@ -44,7 +46,7 @@ from . import capi, plans, ssb
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 DEFAULT_TABLE = os.path.join(HERE, "tuning", "gb300.json")
-VARIANTS = (0, 1, 2, 3, 4, 5, 6, 7)
+VARIANTS = (0, 1, 2, 3, 4, 5, 6, 7, 8)
 TERMINALS = {"flags": 0, "sum": 1, "groupby": 2}
 
 OP_SEARCH_RANGE, OP_SEMI_PROBE = 1, 3  # SDB_OP_* kinds of a chain's first op

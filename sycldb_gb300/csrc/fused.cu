@@ -712,6 +712,10 @@ __device__ __forceinline__ bool in_range(int32_t a, int32_t lo, int32_t hi) { re
 
 constexpr int kItems = 4;
 constexpr int kSlots = 4;
+// Slots per ring stage: CARRY 3 stages only its first two slots (the late
+// ones, renumbered last, are not staged) and spends the space on more stages.
+template <int CARRY>
+__host__ __device__ constexpr int stage_slots() { return CARRY == 3 ? 2 : kSlots; }
 constexpr int kMaxOps = 8;
 
 struct Src {
@@ -741,6 +745,9 @@ struct Launch {
     uint64_t *sum_out;
     int32_t n_keys;
     uint32_t tail_slots;  // slots read after the first op (bit s = slot s): what a carried row keeps
+    uint32_t late_slots;  // CARRY 3: tail slots read only after the second compaction level -- not
+                          // staged; a row carries its row number there and the second level loads them
+    int32_t nstaged;      // slots staged by the copy ring: 0 .. nstaged-1 (all nslot but for CARRY 3)
     Src keys[SDB_CHAIN_MAX_KEYS];
     int32_t key_min[SDB_CHAIN_MAX_KEYS];
     uint32_t mults[SDB_CHAIN_MAX_KEYS];
@@ -1051,8 +1058,8 @@ __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsi
 // SPLIT = number of ops run on 4-row groups; the rest run on the compacted
 // rows.  SPLIT == sizeof...(KS) + 1 means no compaction (all ops dense, which
 // also serves SDB_TERM_FLAGS).
-template <int STAGES>
-__host__ __device__ constexpr int dense_min_blocks() { return STAGES >= 3 ? 3 : 5; }
+template <int STAGES, int CARRY>
+__host__ __device__ constexpr int dense_min_blocks() { return CARRY == 3 ? 5 : (STAGES >= 3 ? 3 : 5); }
 
 // ---- pieces shared by the single-chain pass and the batched pass ----------
 
@@ -1089,12 +1096,12 @@ __device__ __forceinline__ void stage_bitmap(const Launch &L, uint32_t *s_bits)
     }
 }
 
-// Copies this thread's 4 rows of every slot column of `tile` (rows
-// tile + 4t .. +3) into ring stage `st`; rows past the end are zero-filled
-// or skipped.  Always commits one group (possibly empty) so every thread
+// Copies this thread's 4 rows of slot columns 0 .. nstaged-1 of `tile` (rows
+// tile + 4t .. +3) into ring stage `st` (SS slots per stage); rows past the
+// end are zero-filled or skipped.  Always commits one group (possibly empty) so every thread
 // counts groups the same way.
-template <int STAGES>
-__device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nslot, uint64_t n, int4 *s_buf, int st,
+template <int STAGES, int SS>
+__device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nstaged, uint64_t n, int4 *s_buf, int st,
                                            uint64_t tile)
 {
     const uint64_t r0 = tile + (uint64_t)kItems * threadIdx.x;
@@ -1102,8 +1109,8 @@ __device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nslot
         const uint64_t left = n - r0;
         const uint32_t bytes = left >= kItems ? 16u : (uint32_t)(left * 4);
 #pragma unroll
-        for (int sl = 0; sl < kSlots; sl++)
-            if (sl < nslot) cp_async16(&s_buf[(st * kSlots + sl) * kThreads + threadIdx.x], slot[sl] + r0, bytes);
+        for (int sl = 0; sl < SS; sl++)
+            if (sl < nstaged) cp_async16(&s_buf[(st * SS + sl) * kThreads + threadIdx.x], slot[sl] + r0, bytes);
     }
     cp_async_commit();
 }
@@ -1179,18 +1186,30 @@ __device__ __forceinline__ VRow<NREGS> take_row(const VRow<NREGS> &R, const uint
     return o;
 }
 
-template <int TERM, int NREGS, int SPLIT, int... KS>
+// The ops after the first row-per-lane op and the terminal, for the rows of
+// a level-2 group (lane j: row j while F.live).  CARRY 3 first loads the late
+// slots of each live row from its row number.
+template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void level2_run(const Launch &L, VRow<NREGS> &F, const uint32_t *s_bits, uint32_t *s_key,
                                            unsigned long long *s_sum, bool direct, uint64_t &acc)
 {
     constexpr int N = sizeof...(KS);
+    if constexpr (CARRY == 3) {
+        const uint32_t late = L.late_slots;
+        if (F.live) {
+            if (late & 1u) F.v0 = __ldg(L.slot[0] + (uint32_t)F.v0);
+            if (late & 2u) F.v1 = __ldg(L.slot[1] + (uint32_t)F.v1);
+            if (late & 4u) F.v2 = __ldg(L.slot[2] + (uint32_t)F.v2);
+            if (late & 8u) F.v3 = __ldg(L.slot[3] + (uint32_t)F.v3);
+        }
+    }
     run_steps1<NREGS, SPLIT + 1, KS...>(L, F, s_bits, std::make_integer_sequence<int, N - SPLIT - 1>{});
     finish_row<TERM>(L, F, s_key, s_sum, direct, acc);
 }
 
 // After the first row-per-lane op of a group: appends its live rows to the
 // level-2 rows and runs the remaining ops whenever 32 are pending.
-template <int TERM, int NREGS, int SPLIT, int... KS>
+template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &R, Level2<NREGS> &Q,
                                             const uint32_t *s_bits, uint32_t *s_key, unsigned long long *s_sum,
                                             bool direct, uint64_t &acc)
@@ -1212,7 +1231,7 @@ __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &
     if (n2 + cnt >= 32) {
         VRow<NREGS> F = Q.r;
         F.live = true;
-        level2_run<TERM, NREGS, SPLIT, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
+        level2_run<TERM, NREGS, SPLIT, CARRY, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
         const uint32_t used = 32 - n2;
         const VRow<NREGS> got = take_row(R, Q.src, lane + used, cnt);
         if (lane < cnt - used) Q.r = got;
@@ -1223,16 +1242,16 @@ __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &
     __syncwarp();  // every lane has read the list before it is written again
 }
 
-// Whether CARRY 2 uses the second level: there are ops after the first
+// Whether CARRY 2 or 3 uses the second level: there are ops after the first
 // row-per-lane op.
 template <int SPLIT, int... KS>
 __host__ __device__ constexpr bool use_level2(int carry)
 {
-    return carry == 2 && SPLIT + 1 < (int)sizeof...(KS);
+    return carry >= 2 && SPLIT + 1 < (int)sizeof...(KS);
 }
 
 // The first row-per-lane op and then the second level, for one group.
-template <int TERM, int NREGS, int SPLIT, int... KS>
+template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void level2_group(const Launch &L, VRow<NREGS> &R, Level2<NREGS> &Q, const uint32_t *s_bits,
                                              uint32_t *s_key, unsigned long long *s_sum, bool direct, uint64_t &acc)
 {
@@ -1240,7 +1259,7 @@ __device__ __forceinline__ void level2_group(const Launch &L, VRow<NREGS> &R, Le
 #pragma unroll
     for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
     step1<kinds[SPLIT]>(L.ops[SPLIT], R, s_bits);
-    level2_push<TERM, NREGS, SPLIT, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+    level2_push<TERM, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
 }
 
 // Runs whatever the warp still holds (at the end of a block's rows of a chain).
@@ -1259,7 +1278,7 @@ __device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, co
         R.v3 = e.w;
         R.live = lane < carry;
         if constexpr (use_level2<SPLIT, KS...>(CARRY))
-            level2_group<TERM, NREGS, SPLIT, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+            level2_group<TERM, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
         else
             sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
     }
@@ -1268,11 +1287,21 @@ __device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, co
         if (Q.n) {
             VRow<NREGS> F = Q.r;
             F.live = lane < Q.n;
-            level2_run<TERM, NREGS, SPLIT, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
+            level2_run<TERM, NREGS, SPLIT, CARRY, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
         }
         Q.n = 0;
     }
     __syncwarp();
+}
+
+// What a compacted row keeps of slot s: its staged value when a later op
+// reads the slot, or (CARRY 3, late slot) its row number, row0 + r.
+template <int CARRY>
+__device__ __forceinline__ int32_t tail_value(const Launch &L, const int32_t *ws, uint32_t s, uint32_t r, uint64_t row0)
+{
+    if (!((L.tail_slots >> s) & 1u)) return 0;
+    if (CARRY == 3 && ((L.late_slots >> s) & 1u)) return (int32_t)(uint32_t)(row0 + r);
+    return ws[s * 4 * kThreads + r];
 }
 
 template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
@@ -1285,7 +1314,8 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
     constexpr bool kCompact = SPLIT <= N;
     constexpr int kDenseOps = kCompact ? SPLIT : N;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    S.stage = &s_buf[st * kSlots * kThreads + threadIdx.x];
+    constexpr int SS = stage_slots<CARRY>();
+    S.stage = &s_buf[st * SS * kThreads + threadIdx.x];
     S.base = tile + (uint64_t)kItems * threadIdx.x;
     if (S.base + kItems <= L.n) {
         S.valid = (1u << kItems) - 1u;
@@ -1321,11 +1351,12 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
         for (int k = 0; k < kItems; k++)
             if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
         __syncwarp();
-        const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[st * kSlots * kThreads + warp * 32]);
+        const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[st * SS * kThreads + warp * 32]);
         if constexpr (CARRY > 0) {
             // entries 0 .. carry-1 are the carried rows (entry j in lane j),
             // then this tile's survivors
             const uint32_t avail = carry + total;
+            const uint64_t row0 = tile + (uint64_t)warp * 32 * kItems;  // row of the warp's staged row 0
             auto entry = [&](uint32_t idx) {
                 VRow<NREGS> R;
                 if (idx < carry) {  // only in the first group: idx == lane
@@ -1335,10 +1366,10 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
                     R.v3 = ce.w;
                 } else {
                     const uint32_t r = list[idx - carry];
-                    R.v0 = (L.tail_slots & 1u) ? ws[r] : 0;
-                    R.v1 = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
-                    R.v2 = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
-                    R.v3 = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
+                    R.v0 = tail_value<CARRY>(L, ws, 0, r, row0);
+                    R.v1 = tail_value<CARRY>(L, ws, 1, r, row0);
+                    R.v2 = tail_value<CARRY>(L, ws, 2, r, row0);
+                    R.v3 = tail_value<CARRY>(L, ws, 3, r, row0);
                 }
                 R.live = true;
                 return R;
@@ -1347,17 +1378,17 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             for (; b + 32 <= avail; b += 32) {
                 VRow<NREGS> R = entry(b + lane);
                 if constexpr (use_level2<SPLIT, KS...>(CARRY))
-                    level2_group<TERM, NREGS, SPLIT, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+                    level2_group<TERM, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
                 else
                     sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
             const uint32_t rem = avail - b;
             if (lane < rem && b + lane >= carry) {  // carry a survivor of this tile
                 const uint32_t r = list[b + lane - carry];
-                ce.x = (L.tail_slots & 1u) ? ws[r] : 0;
-                ce.y = (L.tail_slots & 2u) ? ws[4 * kThreads + r] : 0;
-                ce.z = (L.tail_slots & 4u) ? ws[8 * kThreads + r] : 0;
-                ce.w = (L.tail_slots & 8u) ? ws[12 * kThreads + r] : 0;
+                ce.x = tail_value<CARRY>(L, ws, 0, r, row0);
+                ce.y = tail_value<CARRY>(L, ws, 1, r, row0);
+                ce.z = tail_value<CARRY>(L, ws, 2, r, row0);
+                ce.w = tail_value<CARRY>(L, ws, 3, r, row0);
             }
             carry = rem;
             __syncwarp();
@@ -1439,22 +1470,23 @@ __device__ __forceinline__ void block_flush(const Launch &L, uint32_t *s_key, un
 }
 
 template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
-__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(const __grid_constant__ Launch L)
+__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k_dense(const __grid_constant__ Launch L)
 {
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
-    extern __shared__ int4 s_buf[];  // [kStages][kSlots][kThreads], then the semi-join bitmap
+    constexpr int SS = stage_slots<CARRY>();
+    extern __shared__ int4 s_buf[];  // [kStages][SS][kThreads], then the semi-join bitmap
     __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
     __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
     __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
     __shared__ uint64_t s_part[kThreads / 32];
-    __shared__ uint8_t s_l2src[CARRY == 2 ? kThreads : 1];
+    __shared__ uint8_t s_l2src[CARRY >= 2 ? kThreads : 1];
     uint32_t carry = 0;  // rows the warp carries (warp-uniform)
     int4 ce = make_int4(0, 0, 0, 0);
     Level2<NREGS> Q;
-    Q.src = s_l2src + (CARRY == 2 ? (threadIdx.x & ~31u) : 0u);
+    Q.src = s_l2src + (CARRY >= 2 ? (threadIdx.x & ~31u) : 0u);
     const bool direct = L.P <= kDenseCap;
-    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads);
     group_table_reset<TERM>(s_key, s_sum);
     stage_bitmap(L, s_bits);
     if (TERM == T_GROUP || L.bitmap_ht) __syncthreads();
@@ -1471,10 +1503,11 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>()) k_dense(
 
     uint64_t tile = (uint64_t)blockIdx.x * kTile;
 #pragma unroll
-    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, p, tile + p * stride);
+    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages, SS>(L.slot, L.nstaged, L.n, s_buf, p, tile + p * stride);
     int st = 0;
     for (; tile < L.n; tile += stride) {
-        issue_tile<kStages>(L.slot, L.nslot, L.n, s_buf, (st + kStages - 1) % kStages, tile + (kStages - 1) * stride);
+        issue_tile<kStages, SS>(L.slot, L.nstaged, L.n, s_buf, (st + kStages - 1) % kStages,
+                                tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
         tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
                                                    carry, ce, Q);
@@ -1501,15 +1534,15 @@ struct Span {
 // Within a span the tiles go through the same cp.async ring as the
 // single-chain pass.
 template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
-__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
+__global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
     k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
             uint32_t *__restrict__ head)
 {
-    __shared__ uint8_t s_l2src[CARRY == 2 ? kThreads : 1];
+    __shared__ uint8_t s_l2src[CARRY >= 2 ? kThreads : 1];
     uint32_t carry = 0;
     int4 ce = make_int4(0, 0, 0, 0);
     Level2<NREGS> Q;
-    Q.src = s_l2src + (CARRY == 2 ? (threadIdx.x & ~31u) : 0u);
+    Q.src = s_l2src + (CARRY >= 2 ? (threadIdx.x & ~31u) : 0u);
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
@@ -1520,7 +1553,8 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
     __shared__ uint64_t s_part[kThreads / 32];
     __shared__ Launch s_L;
     __shared__ uint32_t s_next;
-    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * kSlots * kThreads);
+    constexpr int SS = stage_slots<CARRY>();
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads);
 
     State<NREGS> S;
     S.bits = s_bits;
@@ -1555,13 +1589,15 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES>())
 #pragma unroll
         for (int p = 0; p < kStages - 1; p++) {
             const uint32_t t = span.t0 + p;
-            if (t < span.t1) issue_tile<kStages>(s_L.slot, s_L.nslot, n, s_buf, p, (uint64_t)t * kTile);
+            if (t < span.t1) issue_tile<kStages, SS>(s_L.slot, s_L.nstaged, n, s_buf, p, (uint64_t)t * kTile);
             else cp_async_commit();
         }
         int st = 0;
         for (uint32_t t = span.t0; t < span.t1; t++) {
             const uint32_t tn = t + kStages - 1;
-            if (tn < span.t1) issue_tile<kStages>(s_L.slot, s_L.nslot, n, s_buf, (st + kStages - 1) % kStages, (uint64_t)tn * kTile);
+            if (tn < span.t1)
+                issue_tile<kStages, SS>(s_L.slot, s_L.nstaged, n, s_buf, (st + kStages - 1) % kStages,
+                                        (uint64_t)tn * kTile);
             else cp_async_commit();
             cp_async_wait<kStages - 1>();
             tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum,
@@ -1580,7 +1616,7 @@ template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 int launch_stages(const Launch &L, cudaStream_t s)
 {
     auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
-    const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
     static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
@@ -1600,15 +1636,28 @@ int launch_stages(const Launch &L, cudaStream_t s)
 }
 
 // Ring stages 3 or 2; rows carried between tiles (carry 1; 2: and the second
-// compaction level) only with compaction and a 2-stage ring.
+// compaction level) only with compaction and a 2-stage ring; carry 3 (as 2,
+// and late slots) with a 4-stage ring of two slots, for a launch that
+// prepare_late accepted.
 template <int TERM, int NREGS, int SPLIT, int... KS>
 int launch(const Launch &L, int stages, int carry, cudaStream_t s)
 {
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
+    if (kLate && carry == 3) return launch_stages<TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(L, s);
     if (stages >= 3) return launch_stages<TERM, NREGS, 3, SPLIT, 0, KS...>(L, s);
-    if (kCompact && carry == 2) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(L, s);
+    if (kCompact && carry >= 2) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(L, s);
     if (kCompact && carry == 1) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(L, s);
     return launch_stages<TERM, NREGS, 2, SPLIT, 0, KS...>(L, s);
+}
+
+// Slot bit of an operand (bit s: column slot s), and the slots an op reads.
+inline uint32_t slot_bit(const Src &x) { return x.src == 0 ? (1u << x.idx) : 0u; }
+inline uint32_t op_slots(const Op &o)
+{
+    if (o.kind == SDB_OP_FILL) return 0;
+    const bool uses_b = o.kind == SDB_OP_SELECT || o.kind == SDB_OP_BINOP;
+    return slot_bit(o.a) | (uses_b ? slot_bit(o.b) : 0u);
 }
 
 // Converts a checked chain into a dense launch.  Returns false when the chain
@@ -1678,12 +1727,26 @@ bool convert(const ChainLaunch &C, int nregs, Launch &D)
     D.out_sum = c.out_sum;
     D.occ = c.occ;
     // slots a row still needs after the first op
-    auto slot_bit = [](const Src &x) { return x.src == 0 ? (1u << x.idx) : 0u; };
     D.tail_slots = 0;
-    for (int k = 1; k < c.n_ops; k++) D.tail_slots |= slot_bit(D.ops[k].a) | slot_bit(D.ops[k].b);
+    for (int k = 1; k < c.n_ops; k++) D.tail_slots |= op_slots(D.ops[k]);
     if (c.terminal != SDB_TERM_FLAGS) D.tail_slots |= slot_bit(D.value);
     for (int j = 0; j < D.n_keys; j++) D.tail_slots |= slot_bit(D.keys[j]);
+    D.late_slots = 0;
+    D.nstaged = D.nslot;
     return true;
+}
+
+// Late slots of a chain whose ops from SPLIT on run on compacted rows with
+// the second level: the tail slots that neither the ops on 4-row groups nor
+// the first row-per-lane op read.  None when a row number does not fit 31
+// bits.
+template <int SPLIT>
+uint32_t late_slots_of(const Launch &D)
+{
+    if (D.n >= (1ull << 31)) return 0;
+    uint32_t early = 0;
+    for (int k = 0; k <= SPLIT && k < D.n_ops; k++) early |= op_slots(D.ops[k]);
+    return D.tail_slots & ~early;
 }
 
 // Whether the ops from index `split` on can run on compacted rows: no flags
@@ -1766,6 +1829,76 @@ int with_shape(const Launch &D, int term, int compact, F &f)
     return SDB_ERR_UNSUPPORTED;
 }
 
+struct LateProbe {
+    Launch &D;
+    template <int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        constexpr bool kLate = SPLIT <= (int)sizeof...(KS) && use_level2<SPLIT, KS...>(3);
+        D.late_slots = kLate ? late_slots_of<SPLIT>(D) : 0u;
+        return SDB_OK;
+    }
+};
+
+// Fills D.late_slots for the instantiation with_shape picks with compaction.
+void set_late_slots(Launch &D, int term)
+{
+    LateProbe p{D};
+    if (with_shape(D, term, 1, p) != SDB_OK) D.late_slots = 0;
+}
+
+// Readies D for carry 3: finds its late slots and renumbers the slots so the
+// staged ones come first (every operand, mask and pointer renamed alike).
+// False when the chain has no late slot or more than two staged ones; D then
+// stages every slot again (run_all_staged) and runs as it did under carry 2.
+void run_all_staged(Launch &D)
+{
+    D.late_slots = 0;
+    D.nstaged = D.nslot;
+}
+
+bool prepare_late(Launch &D, int term)
+{
+    set_late_slots(D, term);
+    if (!D.late_slots) {
+        run_all_staged(D);
+        return false;
+    }
+    int perm[kSlots];
+    int k = 0;
+    for (int s = 0; s < D.nslot; s++)
+        if (!((D.late_slots >> s) & 1u)) perm[s] = k++;
+    const int staged = k;
+    for (int s = 0; s < D.nslot; s++)
+        if ((D.late_slots >> s) & 1u) perm[s] = k++;
+    auto rename = [&](Src &x) {
+        if (x.src == 0) x.idx = perm[x.idx];
+    };
+    for (int i = 0; i < D.n_ops; i++) {
+        rename(D.ops[i].a);
+        rename(D.ops[i].b);
+    }
+    rename(D.value);
+    for (int j = 0; j < D.n_keys; j++) rename(D.keys[j]);
+    auto remask = [&](uint32_t m) {
+        uint32_t r = 0;
+        for (int s = 0; s < D.nslot; s++)
+            if ((m >> s) & 1u) r |= 1u << perm[s];
+        return r;
+    };
+    D.tail_slots = remask(D.tail_slots);
+    D.late_slots = remask(D.late_slots);
+    const int32_t *old[kSlots];
+    for (int s = 0; s < kSlots; s++) old[s] = D.slot[s];
+    for (int s = 0; s < D.nslot; s++) D.slot[perm[s]] = old[s];
+    D.nstaged = staged;
+    if (staged > stage_slots<3>()) {
+        run_all_staged(D);
+        return false;
+    }
+    return true;
+}
+
 // Shape identity of a launch: which kernel instantiation with_shape picks.
 struct ShapeProbe {
     int id = -1;
@@ -1799,7 +1932,12 @@ int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages,
 {
     Launch D;
     if (!convert(C, nregs, D)) return SDB_ERR_UNSUPPORTED;
-    SingleLauncher f{D, stages, can_carry(D, term) ? carry : 0, s};
+    if (carry == 3 && !(compact && can_carry(D, term) && prepare_late(D, term))) {
+        carry = 2;  // as variant 7
+        stages = 2;
+    }
+    if (!can_carry(D, term)) carry = 0;
+    SingleLauncher f{D, stages, carry, s};
     return with_shape(D, term, compact, f);
 }
 
@@ -1809,7 +1947,7 @@ int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, ui
                  cudaStream_t s)
 {
     auto kern = k_batch<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
-    const int ring = STAGES * kSlots * kThreads * (int)sizeof(int4);
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (int)sizeof(int4);
     const int smem = ring + (int)(bitmap_words * 4);
     static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
@@ -1839,9 +1977,13 @@ struct BatchLauncher {
     int run()
     {
         constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+        constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
+        if (kLate && carry == 3)
+            return batch_stages<TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(launches, spans, n_spans, head,
+                                                                           bitmap_words, s);
         if (stages >= 3)
             return batch_stages<TERM, NREGS, 3, SPLIT, 0, KS...>(launches, spans, n_spans, head, bitmap_words, s);
-        if (kCompact && carry == 2)
+        if (kCompact && carry >= 2)
             return batch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(launches, spans, n_spans, head,
                                                                               bitmap_words, s);
         if (kCompact && carry == 1)
@@ -1896,10 +2038,14 @@ constexpr int kDenseVariant = 3;
 constexpr int kCompact2Variant = 5;  // as 4 with a 2-stage copy ring
 constexpr int kCarryVariant = 6;     // as 5, compacted rows carried across tiles
 constexpr int kLevel2Variant = 7;    // as 6, plus a second compaction after the first row-per-lane op
-constexpr int kMaxVariant = 7;
+constexpr int kLateVariant = 8;      // as 7, the columns read only after the second compaction loaded per row
+constexpr int kMaxVariant = 8;
 
-int variant_stages(int v) { return (v == kCompact2Variant || v >= kCarryVariant) ? 2 : 3; }
-int variant_carry(int v) { return v == kLevel2Variant ? 2 : (v == kCarryVariant ? 1 : 0); }
+int variant_stages(int v) { return v == kLateVariant ? 4 : ((v == kCompact2Variant || v >= kCarryVariant) ? 2 : 3); }
+int variant_carry(int v)
+{
+    return v == kLateVariant ? 3 : (v == kLevel2Variant ? 2 : (v == kCarryVariant ? 1 : 0));
+}
 
 bool operand_ok(const sdb_operand &o, int &nregs, bool &vec, const char **why)
 {
@@ -2238,13 +2384,19 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
     for (size_t g = 0; g < groups.size(); g++) {
         BatchPlan::G &G = groups[g];
         for (const Item &it : of[g]->items) {
-            if (G.carry && !dense::can_carry(it.D, G.term)) G.carry = false;  // every chain of the launch must allow it
+            if (G.carry && !dense::can_carry(it.D, G.term)) G.carry = 0;  // every chain of the launch must allow it
             const uint32_t c = (uint32_t)G.launches.size();
             G.launches.push_back(it.D);
+            if (G.carry == 3 && !dense::prepare_late(G.launches.back(), G.term)) {
+                G.carry = 2;  // as variant 7
+                G.stages = 2;
+            }
             if (it.D.bitmap_ht) G.bitmap_words = std::max<uint32_t>(G.bitmap_words, (it.D.bitmap_len + 31) / 32);
             for (uint64_t t = 0; t < it.tiles; t += S)
                 G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + S, it.tiles), 0});
         }
+        if (G.carry != 3)  // chains readied for carry 3 before the group fell back
+            for (dense::Launch &x : G.launches) dense::run_all_staged(x);
     }
     // all builds run in one launch before the other chains: none may probe a
     // table another build writes

@@ -42,7 +42,7 @@ def test_first_op_keys_are_separate():
         assert L.sdb_chain_tune_get_op(2, 2, 1, 1 << 26) == 6
         assert L.sdb_chain_tune_get_op(2, 2, 0, 1 << 26) == 5  # unset entries use the default
         assert L.sdb_chain_tune_set_op(2, 2, 9, 1, 5) == capi.SDB_ERR_INVALID
-        assert L.sdb_chain_tune_set_op(2, 2, 1, 1, 8) == capi.SDB_ERR_INVALID
+        assert L.sdb_chain_tune_set_op(2, 2, 1, 1, 9) == capi.SDB_ERR_INVALID
     finally:
         capi.force_chain_variant(-1)
         autotune.load_default()

@@ -161,7 +161,7 @@ def test_batched_form_full_size_equals_plain():
     assert max(groups) <= 280 and all(g <= p.max_groups for g, p in zip(groups, wl.params))
 
 
-@pytest.mark.parametrize("variant", [3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [3, 4, 5, 6, 7, 8])
 def test_batch_under_each_specialised_variant(tables, oracle_rows, variant):
     """The chain batch with every shape-specialised variant (dense, compacted
     with a 3- or 2-stage ring, rows carried across tiles)."""

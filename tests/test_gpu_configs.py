@@ -65,7 +65,7 @@ def test_sf1_configuration_matches_oracle_and_naive(ds, kind, year):
             assert eng.execute(plan).canonical() == want
 
 
-@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6, 7, 8])
 def test_sf1_configurations_on_every_fused_variant(ds, variant):
     from sycldb_gb300 import capi
 

@@ -148,7 +148,7 @@ def test_every_kernel_variant_matches_golden(variant):
         capi.force_chain_variant(-1)
 
 
-@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6, 7])
+@pytest.mark.parametrize("variant", [0, 3, 4, 5, 6, 7, 8])
 def test_reversed_search_range_is_empty(variant):
     """A SEARCH range whose low bound is above its high bound selects no row
     (the reference's `c >= lo` then `c <= hi`), in every fused variant."""
