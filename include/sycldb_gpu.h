@@ -366,11 +366,19 @@ typedef enum sdb_op_kernel {
 int sdb_op_tune_set(int op_kernel, uint64_t rows, int block, int blocks_per_sm);
 int sdb_op_tune_get(int op_kernel, uint64_t rows, int *block, int *blocks_per_sm);
 
+/* Launches of the shape-specialised passes since the library loaded
+ * (single-chain and batched), and how many of them ran a bound pass: a hot
+ * shape (star join, date join, filter-project-sum) under variant 8 whose
+ * operands sit where the shape's canonical binding puts them, so the pass
+ * reads every operand at a place fixed at compile time.  Host counters;
+ * either pointer may be NULL. */
+int sdb_fused_launch_counts(uint64_t *specialised, uint64_t *bound);
 /* Registers (1..8) a chain needs, or a negative status if it is invalid. */
 int sdb_chain_registers(const sdb_chain_desc *chain);
-/* 1 when the chain has a shape-specialised instantiation (variants 3-8), 0
- * when only the general pass runs it, or a negative status if it is invalid.
- * Host-only. */
+/* 2 when the chain has a shape-specialised instantiation (variants 3-8) and
+ * variant 8 runs it in a bound pass (see sdb_fused_launch_counts), 1 when it
+ * has one but no bound pass, 0 when only the general pass runs it, or a
+ * negative status if it is invalid.  Host-only. */
 int sdb_chain_specialised(const sdb_chain_desc *chain);
 
 /* ------------------------------------------------------------ chain batches

@@ -132,6 +132,7 @@ _SIGS = {
     "sdb_chain_tune_get_op": (c_int, [c_int, c_int, c_int, c_uint64]),
     "sdb_chain_registers": (c_int, [POINTER(ChainDesc)]),
     "sdb_chain_specialised": (c_int, [POINTER(ChainDesc)]),
+    "sdb_fused_launch_counts": (c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     "sdb_chain_batch_scratch_bytes": (c_size_t, [POINTER(ChainDesc), c_int]),
     "sdb_chain_batch_create": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
     "sdb_chain_batch_create_async": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, c_void_p, c_size_t, _P,
@@ -219,6 +220,14 @@ def check(status: int):
     if status != SDB_OK:
         raise SdbError(status, last_error())
     return status
+
+
+def fused_launch_counts() -> tuple:
+    """(launches of the shape-specialised passes, of those the bound passes)
+    since the library loaded."""
+    a, b = c_uint64(0), c_uint64(0)
+    check(lib().sdb_fused_launch_counts(ctypes.byref(a), ctypes.byref(b)))
+    return a.value, b.value
 
 
 def force_chain_variant(variant: int):

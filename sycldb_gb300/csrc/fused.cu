@@ -766,6 +766,94 @@ constexpr uint32_t kBitmapMax = 1u << 18;
 // for five resident blocks per SM; a group-by has few live slots per block.
 constexpr uint32_t kDenseCap = 512;
 
+// ---- operand bindings -------------------------------------------------------
+// A binding fixes at compile time where each operand of a chain shape comes
+// from: column slot i (code i), register r (code 8 + r) or a literal (code 16,
+// its value still read at run time); kAny reads the operand's Src at run time.
+// Dyn binds nothing.  The bound passes of the hot shapes (the shapes'
+// canonical bindings, checked on the host before a launch) read every operand
+// straight from its register or staged row, and values that no later op
+// reads are never moved.
+constexpr int kAny = -1;
+constexpr int kLitCode = 16;
+__host__ __device__ constexpr int bslot(int i) { return i; }
+__host__ __device__ constexpr int breg(int r) { return 8 + r; }
+__host__ __device__ constexpr uint32_t code_bit(int c) { return c >= 0 && c < 8 ? 1u << c : 0u; }
+
+struct Dyn {
+    static constexpr bool bound = false;
+    __host__ __device__ static constexpr int a(int) { return kAny; }
+    __host__ __device__ static constexpr int b(int) { return kAny; }
+    __host__ __device__ static constexpr int out(int) { return kAny; }
+    __host__ __device__ static constexpr int value() { return kAny; }
+    __host__ __device__ static constexpr int n_keys() { return kAny; }
+    __host__ __device__ static constexpr int key(int) { return kAny; }
+};
+
+// Star join (semi, full, full -> group-by): semi(slot 0); full(slot 1) -> r0;
+// full(slot 2) -> r1; group by (r1, r0), sum slot 3.
+struct StarBind : Dyn {
+    static constexpr bool bound = true;
+    __host__ __device__ static constexpr int a(int i) { return bslot(i); }
+    __host__ __device__ static constexpr int out(int i) { return i == 1 ? 0 : (i == 2 ? 1 : kAny); }
+    __host__ __device__ static constexpr int value() { return bslot(3); }
+    __host__ __device__ static constexpr int n_keys() { return 2; }
+    __host__ __device__ static constexpr int key(int q) { return q == 0 ? breg(1) : (q == 1 ? breg(0) : kAny); }
+};
+
+// Range filter + join + projection -> group-by (date join): search(slot 0);
+// full(slot 1) -> r0; r1 = slot 2 op slot 0; group by r0, sum r1.
+struct DateJoinBind : Dyn {
+    static constexpr bool bound = true;
+    __host__ __device__ static constexpr int a(int i) { return bslot(i); }
+    __host__ __device__ static constexpr int b(int i) { return i == 2 ? bslot(0) : kAny; }
+    __host__ __device__ static constexpr int out(int i) { return i == 1 ? 0 : (i == 2 ? 1 : kAny); }
+    __host__ __device__ static constexpr int value() { return breg(1); }
+    __host__ __device__ static constexpr int n_keys() { return 1; }
+    __host__ __device__ static constexpr int key(int q) { return q == 0 ? breg(0) : kAny; }
+};
+
+// Filter-project-sum: search(slot 0), search(slot 1), select(slot 2 cmp
+// literal); r0 = slot 3 op slot 1; sum r0.
+struct FilterSumBind : Dyn {
+    static constexpr bool bound = true;
+    __host__ __device__ static constexpr int a(int i) { return bslot(i); }
+    __host__ __device__ static constexpr int b(int i) { return i == 2 ? kLitCode : (i == 3 ? bslot(1) : kAny); }
+    __host__ __device__ static constexpr int out(int i) { return i == 3 ? 0 : kAny; }
+    __host__ __device__ static constexpr int value() { return breg(0); }
+    __host__ __device__ static constexpr int n_keys() { return 0; }
+};
+
+// Slots op i of a bound shape reads.
+template <class B, int... KS>
+__host__ __device__ constexpr uint32_t bound_op_bits(int i)
+{
+    constexpr int kinds[] = {KS...};
+    const int k = kinds[i];
+    if (k == SDB_OP_FILL) return 0u;
+    const bool uses_b = k == SDB_OP_SELECT || k == SDB_OP_BINOP;
+    return code_bit(B::a(i)) | (uses_b ? code_bit(B::b(i)) : 0u);
+}
+
+// The tail and late slot masks of a bound shape (what convert and
+// late_slots_of compute from the launch).
+template <class B, int TERM, int... KS>
+__host__ __device__ constexpr uint32_t bound_tail()
+{
+    uint32_t m = 0;
+    for (int i = 1; i < (int)sizeof...(KS); i++) m |= bound_op_bits<B, KS...>(i);
+    if (TERM != T_FLAGS) m |= code_bit(B::value());
+    for (int q = 0; q < B::n_keys(); q++) m |= code_bit(B::key(q));
+    return m;
+}
+template <class B, int TERM, int SPLIT, int... KS>
+__host__ __device__ constexpr uint32_t bound_late()
+{
+    uint32_t e = 0;
+    for (int i = 0; i <= SPLIT && i < (int)sizeof...(KS); i++) e |= bound_op_bits<B, KS...>(i);
+    return bound_tail<B, TERM, KS...>() & ~e;
+}
+
 // Tile rows are staged in shared memory by cp.async: thread t's four rows
 // (tile + 4t .. 4t + 3) of every chain column arrive as one 16-byte copy per
 // column into a ring of STAGES (2 or 3) stages, issued STAGES - 1 tiles
@@ -823,6 +911,38 @@ __device__ __forceinline__ void set_regs(State<NREGS> &S, int r, const int32_t (
         }
 }
 
+// fetch4 / set_regs with the operand's binding code C (kAny: at run time).
+template <int C, int NREGS>
+__device__ __forceinline__ void fetch4c(const Src &s, const State<NREGS> &S, int32_t (&v)[kItems])
+{
+    if constexpr (C == kAny) {
+        fetch4(s, S, v);
+    } else if constexpr (C < 8) {
+        const int4 q = S.stage[C * kThreads];
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else if constexpr (C < kLitCode) {
+        static_assert(C - 8 < NREGS, "bound register outside the instantiation");
+#pragma unroll
+        for (int k = 0; k < kItems; k++) v[k] = S.reg[C - 8][k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < kItems; k++) v[k] = s.lit;
+    }
+}
+
+template <int OUT, int NREGS>
+__device__ __forceinline__ void set_regs_c(State<NREGS> &S, int r, const int32_t (&v)[kItems], uint32_t mask)
+{
+    if constexpr (OUT == kAny) {
+        set_regs(S, r, v, mask);
+    } else {
+        static_assert(OUT < NREGS, "bound register outside the instantiation");
+#pragma unroll
+        for (int k = 0; k < kItems; k++)
+            if ((mask >> k) & 1u) S.reg[OUT][k] = v[k];
+    }
+}
+
 __device__ __forceinline__ void store4(int32_t *col, uint64_t base, const int32_t (&v)[kItems], uint32_t mask)
 {
 #pragma unroll
@@ -830,7 +950,7 @@ __device__ __forceinline__ void store4(int32_t *col, uint64_t base, const int32_
         if ((mask >> k) & 1u) col[base + k] = v[k];
 }
 
-template <int K, int NREGS>
+template <int K, int NREGS, int A, int BB, int OUT>
 __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
 {
     int32_t a[kItems], b[kItems];
@@ -838,8 +958,8 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         const bool and_op = op.logic == SDB_AND;
         if (and_op && S.live == 0) return;
         const uint32_t need = and_op ? S.live : S.valid;
-        fetch4(op.a, S, a);
-        if (K == SDB_OP_SELECT) fetch4(op.b, S, b);
+        fetch4c<A>(op.a, S, a);
+        if (K == SDB_OP_SELECT) fetch4c<BB>(op.b, S, b);
         uint32_t m = 0;
 #pragma unroll
         for (int k = 0; k < kItems; k++) {
@@ -852,7 +972,7 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         S.live = sdb::logical4(op.logic, S.live, m & need) & S.valid;
     } else if (K == SDB_OP_SEMI_PROBE) {
         if (S.live == 0) return;
-        fetch4(op.a, S, a);
+        fetch4c<A>(op.a, S, a);
         const uint8_t *ht = static_cast<const uint8_t *>(op.ht);
         uint32_t m = 0;
         if (op.smem_bits) {
@@ -877,7 +997,7 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         S.live &= m;
     } else if (K == SDB_OP_FULL_PROBE) {
         if (S.live == 0) return;
-        fetch4(op.a, S, a);
+        fetch4c<A>(op.a, S, a);
         const int2 *ht = static_cast<const int2 *>(op.ht);
         int2 e[kItems];
 #pragma unroll
@@ -894,29 +1014,29 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
         }
         m &= S.live;
         S.live = m;
-        set_regs(S, op.out_reg, b, m);
+        set_regs_c<OUT>(S, op.out_reg, b, m);
         if (op.out_col && m) store4(op.out_col, S.base, b, m);
     } else if (K == SDB_OP_BINOP) {
         if (S.live == 0) return;
-        fetch4(op.a, S, a);
-        fetch4(op.b, S, b);
+        fetch4c<A>(op.a, S, a);
+        fetch4c<BB>(op.b, S, b);
 #pragma unroll
         for (int k = 0; k < kItems; k++) a[k] = sdb::binop(a[k], b[k], op.bin);
-        set_regs(S, op.out_reg, a, S.live);
+        set_regs_c<OUT>(S, op.out_reg, a, S.live);
         if (op.out_col) store4(op.out_col, S.base, a, S.live);
     } else if (K == SDB_OP_FILL) {
 #pragma unroll
         for (int k = 0; k < kItems; k++) a[k] = op.a.lit;
-        set_regs(S, op.out_reg, a, S.valid);
+        set_regs_c<OUT>(S, op.out_reg, a, S.valid);
         if (op.out_col) store4(op.out_col, S.base, a, S.valid);
     }
 }
 
-template <int NREGS, int BEGIN, int... KS, int... IS>
+template <class B, int NREGS, int BEGIN, int... KS, int... IS>
 __device__ __forceinline__ void run_steps(const Launch &L, State<NREGS> &S, std::integer_sequence<int, IS...>)
 {
     constexpr int kinds[] = {KS...};
-    (step<kinds[BEGIN + IS], NREGS>(L.ops[BEGIN + IS], S), ...);
+    (step<kinds[BEGIN + IS], NREGS, B::a(BEGIN + IS), B::b(BEGIN + IS), B::out(BEGIN + IS)>(L.ops[BEGIN + IS], S), ...);
 }
 
 // Sparse phase: after op SPLIT - 1 each warp compacts its surviving rows
@@ -970,59 +1090,109 @@ __device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
     return s.lit;
 }
 
+// fetch1 with the operand's binding code C (kAny: at run time).
+template <int C, int NREGS>
+__device__ __forceinline__ int32_t fetch1c(const Src &s, const VRow<NREGS> &R)
+{
+    if constexpr (C == kAny) {
+        return fetch1(s, R);
+    } else if constexpr (C < 8) {
+        static_assert(C < kSlots, "bound slot outside the launch");
+        return C == 0 ? R.v0 : (C == 1 ? R.v1 : (C == 2 ? R.v2 : R.v3));
+    } else if constexpr (C < kLitCode) {
+        static_assert(C - 8 < NREGS, "bound register outside the instantiation");
+        return R.reg[C - 8];
+    } else {
+        return s.lit;
+    }
+}
+
+template <int C, int NREGS>
+__device__ __forceinline__ int32_t fetch1c(const Src &s, const Row<NREGS> &R)
+{
+    if constexpr (C == kAny) {
+        return fetch1(s, R);
+    } else if constexpr (C < 8) {
+        return R.wstage[C * 4 * kThreads + R.r];
+    } else if constexpr (C < kLitCode) {
+        static_assert(C - 8 < NREGS, "bound register outside the instantiation");
+        return R.reg[C - 8];
+    } else {
+        return s.lit;
+    }
+}
+
 // One op on one row per lane.
-template <int K, class RowT>
+template <int K, int A, int BB, int OUT, class RowT>
 __device__ __forceinline__ void step1(const Op &op, RowT &R, const uint32_t *bits)
 {
     constexpr int NREGS = RowT::kRegs;
     if (!R.live) return;
     if (K == SDB_OP_SELECT) {
-        R.live = sdb::compare(op.cmp, fetch1(op.a, R), fetch1(op.b, R));
+        R.live = sdb::compare(op.cmp, fetch1c<A>(op.a, R), fetch1c<BB>(op.b, R));
     } else if (K == SDB_OP_SEARCH_RANGE) {
-        R.live = in_range(fetch1(op.a, R), op.lo, op.hi);
+        R.live = in_range(fetch1c<A>(op.a, R), op.lo, op.hi);
     } else if (K == SDB_OP_SEARCH_POINTS) {
-        const int32_t a = fetch1(op.a, R);
+        const int32_t a = fetch1c<A>(op.a, R);
         R.live = a == op.lo || a == op.hi;
     } else if (K == SDB_OP_SEMI_PROBE) {
-        const int32_t a = fetch1(op.a, R);
+        const int32_t a = fetch1c<A>(op.a, R);
         const bool ok = in_range(a, op.lo, op.hi);
         const uint32_t i = ok ? (uint32_t)a - (uint32_t)op.lo : 0u;
         const bool hit = op.smem_bits ? ((bits[i >> 5] >> (i & 31u)) & 1u) != 0
                                       : __ldg(static_cast<const uint8_t *>(op.ht) + i) != 0;
         R.live = ok && hit;
     } else if (K == SDB_OP_FULL_PROBE) {
-        const int32_t a = fetch1(op.a, R);
+        const int32_t a = fetch1c<A>(op.a, R);
         const bool ok = in_range(a, op.lo, op.hi);
         const int2 e = __ldg(static_cast<const int2 *>(op.ht) + (ok ? (uint32_t)a - (uint32_t)op.lo : 0u));
         R.live = ok && e.x == 1;
+        if constexpr (OUT == kAny) {
 #pragma unroll
-        for (int i = 0; i < NREGS; i++) R.reg[i] = (R.live && op.out_reg == i) ? e.y : R.reg[i];
+            for (int i = 0; i < NREGS; i++) R.reg[i] = (R.live && op.out_reg == i) ? e.y : R.reg[i];
+        } else {
+            R.reg[OUT] = R.live ? e.y : R.reg[OUT];
+        }
         if (R.live && op.out_col) op.out_col[R.grow] = e.y;
     } else if (K == SDB_OP_BINOP) {
-        const int32_t v = sdb::binop(fetch1(op.a, R), fetch1(op.b, R), op.bin);
+        const int32_t v = sdb::binop(fetch1c<A>(op.a, R), fetch1c<BB>(op.b, R), op.bin);
+        if constexpr (OUT == kAny) {
 #pragma unroll
-        for (int i = 0; i < NREGS; i++) R.reg[i] = op.out_reg == i ? v : R.reg[i];
+            for (int i = 0; i < NREGS; i++) R.reg[i] = op.out_reg == i ? v : R.reg[i];
+        } else {
+            R.reg[OUT] = v;
+        }
         if (op.out_col) op.out_col[R.grow] = v;
     }
 }
 
-template <int NREGS, int BEGIN, int... KS, class RowT, int... IS>
+template <class B, int NREGS, int BEGIN, int... KS, class RowT, int... IS>
 __device__ __forceinline__ void run_steps1(const Launch &L, RowT &R, const uint32_t *bits,
                                            std::integer_sequence<int, IS...>)
 {
     constexpr int kinds[] = {KS...};
-    (step1<kinds[BEGIN + IS]>(L.ops[BEGIN + IS], R, bits), ...);
+    (step1<kinds[BEGIN + IS], B::a(BEGIN + IS), B::b(BEGIN + IS), B::out(BEGIN + IS)>(L.ops[BEGIN + IS], R, bits),
+     ...);
 }
 
 // Adds the lane's row (when `row`) to the group-by (block table first, global
-// on overflow) and runs the first-writer exchange; key(kk) gives the row's
-// key values.  All 32 lanes of the warp call it (with row false where the
+// on overflow) and runs the first-writer exchange; key(std::integral_constant
+// <int, q>) gives the row's key q, nk the number of keys.  All 32 lanes of the warp call it (with row false where the
 // lane holds none): the lanes that take part in the warp aggregation are
 // named by a ballot over the full warp, never by the lanes that happen to
 // be converged.
+// Writes the first-writer's key values of slot sl: key(std::integral_constant
+// <int, q>) gives key q.
+template <class KeyFn, int... KK>
+__device__ __forceinline__ void write_keys(const Launch &L, int nk, int64_t sl, KeyFn &key,
+                                           std::integer_sequence<int, KK...>)
+{
+    ((KK < nk ? (void)(L.out_keys[KK][sl] = key(std::integral_constant<int, KK>{})) : (void)0), ...);
+}
+
 template <class KeyFn>
 __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsigned long long *s_sum, bool direct,
-                                          bool row, uint32_t h, int32_t value, KeyFn key)
+                                          bool row, uint32_t h, int32_t value, int nk, KeyFn key)
 {
     const int64_t sl = row ? sdb::group_slot(h, L.P) : 0;
     const bool bad = row && (sl < 0 || (uint64_t)sl >= L.P);
@@ -1048,11 +1218,7 @@ __device__ __forceinline__ void group_row(const Launch &L, uint32_t *s_key, unsi
         first = L.occ[sl] == 0u && atomicExch(&L.occ[sl], 1u) == 0u;
         atomicAdd(reinterpret_cast<unsigned long long *>(&L.out_sum[sl]), val);
     }
-    if (first) {
-#pragma unroll
-        for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-            if (kk < L.n_keys) L.out_keys[kk][sl] = key(kk);
-    }
+    if (first) write_keys(L, nk, sl, key, std::make_integer_sequence<int, SDB_CHAIN_MAX_KEYS>{});
 }
 
 // SPLIT = number of ops run on 4-row groups; the rest run on the compacted
@@ -1119,35 +1285,43 @@ __device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nstag
 // SPLIT <= N) warp compaction and the remaining ops one row per lane, then
 // the terminal into the block's partials.
 // The terminal for one row held by one lane.
-template <int TERM, class RowT>
+// The group slot hash of a row: sum over its keys of (key - min) * mult.
+template <class B, class RowT, int... KK>
+__device__ __forceinline__ uint32_t key_hash(const Launch &L, const RowT &R, int nk, std::integer_sequence<int, KK...>)
+{
+    uint32_t h = 0;
+    ((h += KK < nk ? ((uint32_t)fetch1c<B::key(KK)>(L.keys[KK], R) - (uint32_t)L.key_min[KK]) * L.mults[KK] : 0u),
+     ...);
+    return h;
+}
+
+template <int TERM, class B, class RowT>
 __device__ __forceinline__ void finish_row(const Launch &L, RowT &R, uint32_t *s_key, unsigned long long *s_sum,
                                            bool direct, uint64_t &acc)
 {
     if (TERM == T_SUM) {
-        if (R.live) acc += sdb::widen(fetch1(L.value, R));
+        if (R.live) acc += sdb::widen(fetch1c<B::value()>(L.value, R));
     } else if (TERM == T_GROUP) {
         // every lane of the warp reaches group_row (its warp aggregation
         // needs the whole warp); values of a lane without a live row are
         // read from its registers or staged rows and not used
-        uint32_t h = 0;
-#pragma unroll
-        for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
-            if (kk < L.n_keys) h += ((uint32_t)fetch1(L.keys[kk], R) - (uint32_t)L.key_min[kk]) * L.mults[kk];
-        group_row(L, s_key, s_sum, direct, R.live, h, fetch1(L.value, R),
-                  [&R, &L](int kk) { return fetch1(L.keys[kk], R); });
+        const int nk = B::n_keys() == kAny ? L.n_keys : B::n_keys();
+        const uint32_t h = key_hash<B>(L, R, nk, std::make_integer_sequence<int, SDB_CHAIN_MAX_KEYS>{});
+        auto key = [&R, &L](auto q) { return fetch1c<B::key(decltype(q)::value)>(L.keys[decltype(q)::value], R); };
+        group_row(L, s_key, s_sum, direct, R.live, h, fetch1c<B::value()>(L.value, R), nk, key);
     }
 }
 
 // The ops from SPLIT on and the terminal, for one row held by one lane.
-template <int TERM, int NREGS, int SPLIT, int... KS, class RowT>
+template <int TERM, class B, int NREGS, int SPLIT, int... KS, class RowT>
 __device__ __forceinline__ void sparse_row(const Launch &L, RowT &R, const uint32_t *s_bits, uint32_t *s_key,
                                            unsigned long long *s_sum, bool direct, uint64_t &acc)
 {
     constexpr int N = sizeof...(KS);
 #pragma unroll
     for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
-    run_steps1<NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
-    finish_row<TERM>(L, R, s_key, s_sum, direct, acc);
+    run_steps1<B, NREGS, SPLIT, KS...>(L, R, s_bits, std::make_integer_sequence<int, N - SPLIT>{});
+    finish_row<TERM, B>(L, R, s_key, s_sum, direct, acc);
 }
 
 
@@ -1189,13 +1363,13 @@ __device__ __forceinline__ VRow<NREGS> take_row(const VRow<NREGS> &R, const uint
 // The ops after the first row-per-lane op and the terminal, for the rows of
 // a level-2 group (lane j: row j while F.live).  CARRY 3 first loads the late
 // slots of each live row from its row number.
-template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
+template <int TERM, class B, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void level2_run(const Launch &L, VRow<NREGS> &F, const uint32_t *s_bits, uint32_t *s_key,
                                            unsigned long long *s_sum, bool direct, uint64_t &acc)
 {
     constexpr int N = sizeof...(KS);
     if constexpr (CARRY == 3) {
-        const uint32_t late = L.late_slots;
+        const uint32_t late = B::bound ? bound_late<B, TERM, SPLIT, KS...>() : L.late_slots;
         if (F.live) {
             if (late & 1u) F.v0 = __ldg(L.slot[0] + (uint32_t)F.v0);
             if (late & 2u) F.v1 = __ldg(L.slot[1] + (uint32_t)F.v1);
@@ -1203,13 +1377,13 @@ __device__ __forceinline__ void level2_run(const Launch &L, VRow<NREGS> &F, cons
             if (late & 8u) F.v3 = __ldg(L.slot[3] + (uint32_t)F.v3);
         }
     }
-    run_steps1<NREGS, SPLIT + 1, KS...>(L, F, s_bits, std::make_integer_sequence<int, N - SPLIT - 1>{});
-    finish_row<TERM>(L, F, s_key, s_sum, direct, acc);
+    run_steps1<B, NREGS, SPLIT + 1, KS...>(L, F, s_bits, std::make_integer_sequence<int, N - SPLIT - 1>{});
+    finish_row<TERM, B>(L, F, s_key, s_sum, direct, acc);
 }
 
 // After the first row-per-lane op of a group: appends its live rows to the
 // level-2 rows and runs the remaining ops whenever 32 are pending.
-template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
+template <int TERM, class B, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &R, Level2<NREGS> &Q,
                                             const uint32_t *s_bits, uint32_t *s_key, unsigned long long *s_sum,
                                             bool direct, uint64_t &acc)
@@ -1231,7 +1405,7 @@ __device__ __forceinline__ void level2_push(const Launch &L, const VRow<NREGS> &
     if (n2 + cnt >= 32) {
         VRow<NREGS> F = Q.r;
         F.live = true;
-        level2_run<TERM, NREGS, SPLIT, CARRY, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
+        level2_run<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
         const uint32_t used = 32 - n2;
         const VRow<NREGS> got = take_row(R, Q.src, lane + used, cnt);
         if (lane < cnt - used) Q.r = got;
@@ -1251,19 +1425,19 @@ __host__ __device__ constexpr bool use_level2(int carry)
 }
 
 // The first row-per-lane op and then the second level, for one group.
-template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
+template <int TERM, class B, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void level2_group(const Launch &L, VRow<NREGS> &R, Level2<NREGS> &Q, const uint32_t *s_bits,
                                              uint32_t *s_key, unsigned long long *s_sum, bool direct, uint64_t &acc)
 {
     constexpr int kinds[] = {KS...};
 #pragma unroll
     for (int i = 0; i < NREGS; i++) R.reg[i] = 0;
-    step1<kinds[SPLIT]>(L.ops[SPLIT], R, s_bits);
-    level2_push<TERM, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+    step1<kinds[SPLIT], B::a(SPLIT), B::b(SPLIT), B::out(SPLIT)>(L.ops[SPLIT], R, s_bits);
+    level2_push<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
 }
 
 // Runs whatever the warp still holds (at the end of a block's rows of a chain).
-template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
+template <int TERM, class B, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, const int4 &ce, Level2<NREGS> &Q,
                                             const uint32_t *s_bits, uint32_t *s_key, unsigned long long *s_sum,
                                             bool direct, uint64_t &acc)
@@ -1278,16 +1452,16 @@ __device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, co
         R.v3 = e.w;
         R.live = lane < carry;
         if constexpr (use_level2<SPLIT, KS...>(CARRY))
-            level2_group<TERM, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+            level2_group<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
         else
-            sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+            sparse_row<TERM, B, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
     }
     carry = 0;
     if constexpr (use_level2<SPLIT, KS...>(CARRY)) {
         if (Q.n) {
             VRow<NREGS> F = Q.r;
             F.live = lane < Q.n;
-            level2_run<TERM, NREGS, SPLIT, CARRY, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
+            level2_run<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, F, s_bits, s_key, s_sum, direct, acc);
         }
         Q.n = 0;
     }
@@ -1296,15 +1470,23 @@ __device__ __forceinline__ void drain_carry(const Launch &L, uint32_t &carry, co
 
 // What a compacted row keeps of slot s: its staged value when a later op
 // reads the slot, or (CARRY 3, late slot) its row number, row0 + r.
-template <int CARRY>
-__device__ __forceinline__ int32_t tail_value(const Launch &L, const int32_t *ws, uint32_t s, uint32_t r, uint64_t row0)
+template <int CARRY, class B, int TERM, int SPLIT, int SL, int... KS>
+__device__ __forceinline__ int32_t tail_value(const Launch &L, const int32_t *ws, uint32_t r, uint64_t row0)
 {
-    if (!((L.tail_slots >> s) & 1u)) return 0;
-    if (CARRY == 3 && ((L.late_slots >> s) & 1u)) return (int32_t)(uint32_t)(row0 + r);
-    return ws[s * 4 * kThreads + r];
+    if constexpr (B::bound) {
+        constexpr uint32_t tail = bound_tail<B, TERM, KS...>();
+        constexpr uint32_t late = CARRY == 3 ? bound_late<B, TERM, SPLIT, KS...>() : 0u;
+        if constexpr (!((tail >> SL) & 1u)) return 0;
+        else if constexpr ((late >> SL) & 1u) return (int32_t)(uint32_t)(row0 + r);
+        else return ws[SL * 4 * kThreads + r];
+    } else {
+        if (!((L.tail_slots >> SL) & 1u)) return 0;
+        if (CARRY == 3 && ((L.late_slots >> SL) & 1u)) return (int32_t)(uint32_t)(row0 + r);
+        return ws[SL * 4 * kThreads + r];
+    }
 }
 
-template <int TERM, int NREGS, int SPLIT, int CARRY, int... KS>
+template <int TERM, class B, int NREGS, int SPLIT, int CARRY, int... KS>
 __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, const int4 *s_buf, int st, uint64_t tile,
                                           uint8_t *s_list, uint32_t *s_key, unsigned long long *s_sum,
                                           const uint32_t *s_bits, bool direct, uint64_t &acc, uint32_t &carry,
@@ -1333,7 +1515,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
     } else {
         S.live = S.valid;
     }
-    run_steps<NREGS, 0, KS...>(L, S, std::make_integer_sequence<int, kDenseOps>{});
+    run_steps<B, NREGS, 0, KS...>(L, S, std::make_integer_sequence<int, kDenseOps>{});
 
     if constexpr (kCompact) {
         // warp prefix sum of the live-row counts
@@ -1366,10 +1548,10 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
                     R.v3 = ce.w;
                 } else {
                     const uint32_t r = list[idx - carry];
-                    R.v0 = tail_value<CARRY>(L, ws, 0, r, row0);
-                    R.v1 = tail_value<CARRY>(L, ws, 1, r, row0);
-                    R.v2 = tail_value<CARRY>(L, ws, 2, r, row0);
-                    R.v3 = tail_value<CARRY>(L, ws, 3, r, row0);
+                    R.v0 = tail_value<CARRY, B, TERM, SPLIT, 0, KS...>(L, ws, r, row0);
+                    R.v1 = tail_value<CARRY, B, TERM, SPLIT, 1, KS...>(L, ws, r, row0);
+                    R.v2 = tail_value<CARRY, B, TERM, SPLIT, 2, KS...>(L, ws, r, row0);
+                    R.v3 = tail_value<CARRY, B, TERM, SPLIT, 3, KS...>(L, ws, r, row0);
                 }
                 R.live = true;
                 return R;
@@ -1378,17 +1560,17 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             for (; b + 32 <= avail; b += 32) {
                 VRow<NREGS> R = entry(b + lane);
                 if constexpr (use_level2<SPLIT, KS...>(CARRY))
-                    level2_group<TERM, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
+                    level2_group<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, R, Q, s_bits, s_key, s_sum, direct, acc);
                 else
-                    sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+                    sparse_row<TERM, B, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
             const uint32_t rem = avail - b;
             if (lane < rem && b + lane >= carry) {  // carry a survivor of this tile
                 const uint32_t r = list[b + lane - carry];
-                ce.x = tail_value<CARRY>(L, ws, 0, r, row0);
-                ce.y = tail_value<CARRY>(L, ws, 1, r, row0);
-                ce.z = tail_value<CARRY>(L, ws, 2, r, row0);
-                ce.w = tail_value<CARRY>(L, ws, 3, r, row0);
+                ce.x = tail_value<CARRY, B, TERM, SPLIT, 0, KS...>(L, ws, r, row0);
+                ce.y = tail_value<CARRY, B, TERM, SPLIT, 1, KS...>(L, ws, r, row0);
+                ce.z = tail_value<CARRY, B, TERM, SPLIT, 2, KS...>(L, ws, r, row0);
+                ce.w = tail_value<CARRY, B, TERM, SPLIT, 3, KS...>(L, ws, r, row0);
             }
             carry = rem;
             __syncwarp();
@@ -1400,7 +1582,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
                 R.live = idx < total;
                 R.r = R.live ? list[idx] : 0;
                 R.grow = tile + (uint64_t)warp * 32 * kItems + R.r;
-                sparse_row<TERM, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
+                sparse_row<TERM, B, NREGS, SPLIT, KS...>(L, R, s_bits, s_key, s_sum, direct, acc);
             }
             __syncwarp();
         }
@@ -1433,9 +1615,9 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
                 }
 #pragma unroll
             for (int k = 0; k < kItems; k++)
-                group_row(L, s_key, s_sum, direct, ((S.live >> k) & 1u) != 0, h[k], v[k], [&](int kk) {
+                group_row(L, s_key, s_sum, direct, ((S.live >> k) & 1u) != 0, h[k], v[k], L.n_keys, [&](auto q) {
                     int32_t kv[kItems];
-                    fetch4(L.keys[kk], S, kv);
+                    fetch4(L.keys[decltype(q)::value], S, kv);
                     return kv[k];
                 });
         }
@@ -1469,7 +1651,7 @@ __device__ __forceinline__ void block_flush(const Launch &L, uint32_t *s_key, un
     }
 }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
+template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k_dense(const __grid_constant__ Launch L)
 {
     constexpr int kStages = STAGES;
@@ -1509,13 +1691,13 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
         issue_tile<kStages, SS>(L.slot, L.nstaged, L.n, s_buf, (st + kStages - 1) % kStages,
                                 tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
-        tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
+        tile_body<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
                                                    carry, ce, Q);
         st = (st + 1) % kStages;
     }
     cp_async_wait<0>();
     if constexpr (CARRY > 0)
-        drain_carry<TERM, NREGS, SPLIT, CARRY, KS...>(L, carry, ce, Q, s_bits, s_key, s_sum, direct, acc);
+        drain_carry<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, carry, ce, Q, s_bits, s_key, s_sum, direct, acc);
     block_flush<TERM>(L, s_key, s_sum, s_part, acc);
 }
 
@@ -1533,7 +1715,7 @@ struct Span {
 // new descriptor, resets its group table and re-stages the semi-join bitmap.
 // Within a span the tiles go through the same cp.async ring as the
 // single-chain pass.
-template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
+template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
     k_batch(const Launch *__restrict__ launches, const Span *__restrict__ spans, uint32_t n_spans,
             uint32_t *__restrict__ head)
@@ -1600,22 +1782,26 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
                                         (uint64_t)tn * kTile);
             else cp_async_commit();
             cp_async_wait<kStages - 1>();
-            tile_body<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum,
+            tile_body<TERM, B, NREGS, SPLIT, CARRY, KS...>(s_L, S, s_buf, st, (uint64_t)t * kTile, s_list, s_key, s_sum,
                                                        s_bits, direct, acc, carry, ce, Q);
             st = (st + 1) % kStages;
         }
         cp_async_wait<0>();
         // parked rows belong to this span's chain: run them before the next pull
         if constexpr (CARRY > 0)
-            drain_carry<TERM, NREGS, SPLIT, CARRY, KS...>(s_L, carry, ce, Q, s_bits, s_key, s_sum, direct, acc);
+            drain_carry<TERM, B, NREGS, SPLIT, CARRY, KS...>(s_L, carry, ce, Q, s_bits, s_key, s_sum, direct, acc);
     }
     if (cur != ~0u) block_flush<TERM>(s_L, s_key, s_sum, s_part, acc);
 }
 
-template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
+// Launches of the specialised passes, and of those the bound ones (host
+// counters, read by sdb_fused_launch_counts).
+std::atomic<uint64_t> g_dense_launches{0}, g_bound_launches{0};
+
+template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 int launch_stages(const Launch &L, cudaStream_t s)
 {
-    auto kern = k_dense<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
+    auto kern = k_dense<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
     const int ring = STAGES * stage_slots<CARRY>() * kThreads * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
     static const bool attr = [&] {  // once per instantiation, thread-safe
@@ -1632,6 +1818,8 @@ int launch_stages(const Launch &L, cudaStream_t s)
     if (blocks > cap) blocks = cap;
     if (blocks == 0) blocks = 1;
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(L);
+    g_dense_launches.fetch_add(1, std::memory_order_relaxed);
+    if (B::bound) g_bound_launches.fetch_add(1, std::memory_order_relaxed);
     return sdb_check_launch("sdb_fused_chain (dense)");
 }
 
@@ -1639,16 +1827,21 @@ int launch_stages(const Launch &L, cudaStream_t s)
 // compaction level) only with compaction and a 2-stage ring; carry 3 (as 2,
 // and late slots) with a 4-stage ring of two slots, for a launch that
 // prepare_late accepted.
-template <int TERM, int NREGS, int SPLIT, int... KS>
+template <class B, int TERM, int NREGS, int SPLIT, int... KS>
 int launch(const Launch &L, int stages, int carry, cudaStream_t s)
 {
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
-    if (kLate && carry == 3) return launch_stages<TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(L, s);
-    if (stages >= 3) return launch_stages<TERM, NREGS, 3, SPLIT, 0, KS...>(L, s);
-    if (kCompact && carry >= 2) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(L, s);
-    if (kCompact && carry == 1) return launch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(L, s);
-    return launch_stages<TERM, NREGS, 2, SPLIT, 0, KS...>(L, s);
+    if constexpr (B::bound) {  // bound passes are carry-3 passes (with_shape binds only those)
+        static_assert(kLate, "a bound shape needs the second level");
+        return launch_stages<B, TERM, NREGS, 4, SPLIT, 3, KS...>(L, s);
+    } else {
+        if (kLate && carry == 3) return launch_stages<Dyn, TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(L, s);
+        if (stages >= 3) return launch_stages<Dyn, TERM, NREGS, 3, SPLIT, 0, KS...>(L, s);
+        if (kCompact && carry >= 2) return launch_stages<Dyn, TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(L, s);
+        if (kCompact && carry == 1) return launch_stages<Dyn, TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(L, s);
+        return launch_stages<Dyn, TERM, NREGS, 2, SPLIT, 0, KS...>(L, s);
+    }
 }
 
 // Slot bit of an operand (bit s: column slot s), and the slots an op reads.
@@ -1780,11 +1973,42 @@ bool can_carry(const Launch &D, int term)
     return true;
 }
 
-// Calls f.run<TERM, NREGS, SPLIT, KS...>() for the instantiated shape that
+// Whether D's operands are exactly binding B's (and the slot masks the bound
+// pass derives from it match the launch's), so the bound pass reads what the
+// launch means.
+template <class B, int TERM, int SPLIT, int... KS>
+bool bound_ok(const Launch &D)
+{
+    constexpr int kinds[] = {KS...};
+    constexpr int N = sizeof...(KS);
+    auto code = [](const Src &x) { return x.src == 0 ? bslot(x.idx) : (x.src == 1 ? breg(x.idx) : kLitCode); };
+    if (D.n_ops != N) return false;
+    for (int i = 0; i < N; i++) {
+        const Op &o = D.ops[i];
+        const int k = kinds[i];
+        if (o.kind != k) return false;
+        if (k != SDB_OP_FILL && code(o.a) != B::a(i)) return false;
+        if ((k == SDB_OP_SELECT || k == SDB_OP_BINOP) && code(o.b) != B::b(i)) return false;
+        if ((k == SDB_OP_FULL_PROBE || k == SDB_OP_BINOP || k == SDB_OP_FILL) && o.out_reg != B::out(i)) return false;
+    }
+    if (TERM != T_FLAGS && code(D.value) != B::value()) return false;
+    if (TERM == T_GROUP) {
+        if (D.n_keys != B::n_keys()) return false;
+        for (int q = 0; q < D.n_keys; q++)
+            if (code(D.keys[q]) != B::key(q)) return false;
+    }
+    constexpr uint32_t late = bound_late<B, TERM, SPLIT, KS...>();
+    const uint32_t all = (1u << D.nslot) - 1u, staged = (1u << D.nstaged) - 1u;
+    return D.tail_slots == bound_tail<B, TERM, KS...>() && D.late_slots == late && late == (all & ~staged);
+}
+
+// Calls f.run<B, TERM, NREGS, SPLIT, KS...>() for the instantiation that
 // matches D, or returns SDB_ERR_UNSUPPORTED (without calling f).  `compact`:
-// 1 = compact after the first op when allowed.
+// 1 = compact after the first op when allowed; `bind`: a hot shape whose
+// operands match its canonical binding takes the bound pass (B), else B is
+// Dyn (only carry-3 launches, readied by prepare_late, bind).
 template <class F>
-int with_shape(const Launch &D, int term, int compact, F &f)
+int with_shape(const Launch &D, int term, int compact, F &f, bool bind = false)
 {
     int k[kMaxOps];
     for (int i = 0; i < D.n_ops; i++) k[i] = D.ops[i].kind;
@@ -1795,43 +2019,56 @@ int with_shape(const Launch &D, int term, int compact, F &f)
     const bool r2 = D.nregs <= 2;
     // star join: semi + full + full -> group-by (SSB flight 2)
     if (r2 && term == T_GROUP && n == 3 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE &&
-        k[2] == SDB_OP_FULL_PROBE)
-        return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>()
-                  : f.template run<T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+        k[2] == SDB_OP_FULL_PROBE) {
+        if (c1 && bind && bound_ok<StarBind, T_GROUP, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D))
+            return f.template run<StarBind, T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+        return c1 ? f.template run<Dyn, T_GROUP, 2, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>()
+                  : f.template run<Dyn, T_GROUP, 2, 4, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+    }
     // two semi probes -> flags (the flag-only front of a chain split in two)
     if (r2 && term == T_FLAGS && n == 2 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_SEMI_PROBE)
-        return f.template run<T_FLAGS, 2, 3, SDB_OP_SEMI_PROBE, SDB_OP_SEMI_PROBE>();
+        return f.template run<Dyn, T_FLAGS, 2, 3, SDB_OP_SEMI_PROBE, SDB_OP_SEMI_PROBE>();
     // full + full + projection -> group-by (SSB flight 4 after its semi joins)
     if (D.nregs <= 4 && term == T_GROUP && n == 3 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE &&
         k[2] == SDB_OP_BINOP)
-        return f.template run<T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+        return f.template run<Dyn, T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
     // full + full -> group-by
     if (r2 && term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
-        return f.template run<T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+        return f.template run<Dyn, T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
     // three full probes -> three-key group-by (SSB flight 3: customer, supplier, date)
     if (D.nregs <= 4 && term == T_GROUP && n == 3 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE &&
         k[2] == SDB_OP_FULL_PROBE)
-        return f.template run<T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
+        return f.template run<Dyn, T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
     // range filter + one join + projection -> group-by
     if (r2 && term == T_GROUP && n == 3 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_FULL_PROBE &&
-        k[2] == SDB_OP_BINOP)
-        return c1 ? f.template run<T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>()
-                  : f.template run<T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+        k[2] == SDB_OP_BINOP) {
+        if (c1 && bind && bound_ok<DateJoinBind, T_GROUP, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D))
+            return f.template run<DateJoinBind, T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+        return c1 ? f.template run<Dyn, T_GROUP, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>()
+                  : f.template run<Dyn, T_GROUP, 2, 4, SDB_OP_SEARCH_RANGE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+    }
     // filter-project-sum (SSB flight 1)
     if (r2 && term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
-        k[2] == SDB_OP_SELECT && k[3] == SDB_OP_BINOP)
-        return c1 ? f.template run<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>()
-                  : f.template run<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>();
+        k[2] == SDB_OP_SELECT && k[3] == SDB_OP_BINOP) {
+        if (c1 && bind &&
+            bound_ok<FilterSumBind, T_SUM, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>(D))
+            return f.template run<FilterSumBind, T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT,
+                                  SDB_OP_BINOP>();
+        return c1 ? f.template run<Dyn, T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>()
+                  : f.template run<Dyn, T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SELECT, SDB_OP_BINOP>();
+    }
     if (r2 && term == T_SUM && n == 4 && k[0] == SDB_OP_SEARCH_RANGE && k[1] == SDB_OP_SEARCH_RANGE &&
         k[2] == SDB_OP_SEARCH_RANGE && k[3] == SDB_OP_BINOP)
-        return c1 ? f.template run<T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>()
-                  : f.template run<T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_BINOP>();
+        return c1 ? f.template run<Dyn, T_SUM, 2, 1, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE,
+                                   SDB_OP_BINOP>()
+                  : f.template run<Dyn, T_SUM, 2, 5, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE, SDB_OP_SEARCH_RANGE,
+                                   SDB_OP_BINOP>();
     return SDB_ERR_UNSUPPORTED;
 }
 
 struct LateProbe {
     Launch &D;
-    template <int TERM, int NREGS, int SPLIT, int... KS>
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
         constexpr bool kLate = SPLIT <= (int)sizeof...(KS) && use_level2<SPLIT, KS...>(3);
@@ -1902,7 +2139,7 @@ bool prepare_late(Launch &D, int term)
 // Shape identity of a launch: which kernel instantiation with_shape picks.
 struct ShapeProbe {
     int id = -1;
-    template <int TERM, int NREGS, int SPLIT, int... KS>
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
         static const int kId = next_shape_id();
@@ -1921,10 +2158,10 @@ struct SingleLauncher {
     int stages;
     int carry;
     cudaStream_t s;
-    template <int TERM, int NREGS, int SPLIT, int... KS>
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
-        return launch<TERM, NREGS, SPLIT, KS...>(D, stages, carry, s);
+        return launch<B, TERM, NREGS, SPLIT, KS...>(D, stages, carry, s);
     }
 };
 
@@ -1938,15 +2175,15 @@ int dispatch(const ChainLaunch &C, int nregs, int term, int compact, int stages,
     }
     if (!can_carry(D, term)) carry = 0;
     SingleLauncher f{D, stages, carry, s};
-    return with_shape(D, term, compact, f);
+    return with_shape(D, term, compact, f, carry == 3);
 }
 
 // One launch of k_batch over the chains of one shape group.
-template <int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
+template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
 int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, uint32_t *head, uint32_t bitmap_words,
                  cudaStream_t s)
 {
-    auto kern = k_batch<TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
+    auto kern = k_batch<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
     const int ring = STAGES * stage_slots<CARRY>() * kThreads * (int)sizeof(int4);
     const int smem = ring + (int)(bitmap_words * 4);
     static const bool attr = [&] {  // once per instantiation, thread-safe
@@ -1961,6 +2198,8 @@ int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, ui
     if (blocks > n_spans) blocks = n_spans;
     if (blocks == 0) return SDB_OK;
     kern<<<(unsigned)blocks, kThreads, smem, s>>>(launches, spans, n_spans, head);
+    g_dense_launches.fetch_add(1, std::memory_order_relaxed);
+    if (B::bound) g_bound_launches.fetch_add(1, std::memory_order_relaxed);
     return sdb_check_launch("sdb_chain_batch_launch");
 }
 
@@ -1973,23 +2212,41 @@ struct BatchLauncher {
     int stages;
     int carry;
     cudaStream_t s;
-    template <int TERM, int NREGS, int SPLIT, int... KS>
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
     int run()
     {
         constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
         constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
-        if (kLate && carry == 3)
-            return batch_stages<TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(launches, spans, n_spans, head,
-                                                                           bitmap_words, s);
-        if (stages >= 3)
-            return batch_stages<TERM, NREGS, 3, SPLIT, 0, KS...>(launches, spans, n_spans, head, bitmap_words, s);
-        if (kCompact && carry >= 2)
-            return batch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(launches, spans, n_spans, head,
-                                                                              bitmap_words, s);
-        if (kCompact && carry == 1)
-            return batch_stages<TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(launches, spans, n_spans, head,
-                                                                              bitmap_words, s);
-        return batch_stages<TERM, NREGS, 2, SPLIT, 0, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+        if constexpr (B::bound) {  // bound passes are carry-3 passes
+            static_assert(kLate, "a bound shape needs the second level");
+            return batch_stages<B, TERM, NREGS, 4, SPLIT, 3, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+        } else {
+            if (kLate && carry == 3)
+                return batch_stages<Dyn, TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(launches, spans, n_spans, head,
+                                                                                    bitmap_words, s);
+            if (stages >= 3)
+                return batch_stages<Dyn, TERM, NREGS, 3, SPLIT, 0, KS...>(launches, spans, n_spans, head,
+                                                                        bitmap_words, s);
+            if (kCompact && carry >= 2)
+                return batch_stages<Dyn, TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(launches, spans, n_spans,
+                                                                                       head, bitmap_words, s);
+            if (kCompact && carry == 1)
+                return batch_stages<Dyn, TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(launches, spans, n_spans,
+                                                                                       head, bitmap_words, s);
+            return batch_stages<Dyn, TERM, NREGS, 2, SPLIT, 0, KS...>(launches, spans, n_spans, head, bitmap_words,
+                                                                    s);
+        }
+    }
+};
+
+// Whether with_shape binds D (its shape's bound pass runs it).
+struct BoundProbe {
+    bool bound = false;
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        bound = B::bound;
+        return SDB_OK;
     }
 };
 
@@ -2266,6 +2523,7 @@ struct sdb_chain_batch {
     struct Group {
         int term, compact, stages;
         int carry;
+        bool bound;                      // every chain takes its shape's bound pass
         dense::Launch first;             // host copy, picks the instantiation
         const dense::Launch *launches;   // device
         const dense::Span *spans;        // device
@@ -2293,6 +2551,7 @@ struct BatchPlan {
     struct G {
         int term, compact, stages, shape;
         int carry = 0;
+        bool bound = false;
         std::vector<dense::Launch> launches;
         std::vector<dense::Span> spans;
         uint32_t bitmap_words = 0;
@@ -2397,6 +2656,12 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         }
         if (G.carry != 3)  // chains readied for carry 3 before the group fell back
             for (dense::Launch &x : G.launches) dense::run_all_staged(x);
+        G.bound = G.carry == 3;
+        for (const dense::Launch &x : G.launches) {
+            dense::BoundProbe p;
+            if (G.bound && dense::with_shape(x, G.term, 1, p, true) == SDB_OK) G.bound = p.bound;
+            else G.bound = false;
+        }
     }
     // all builds run in one launch before the other chains: none may probe a
     // table another build writes
@@ -2464,6 +2729,7 @@ static int chain_batch_create(const sdb_chain_desc *chains, int n_chains, void *
         o.compact = G.compact;
         o.stages = G.stages;
         o.carry = G.carry;
+        o.bound = G.bound;
         o.first = G.launches[0];
         o.head = b->heads + g;
         o.bitmap_words = G.bitmap_words;
@@ -2528,7 +2794,7 @@ int sdb_chain_batch_launch_part(const sdb_chain_batch *b, int part, sdb_stream_t
     }
     for (const auto &G : b->groups) {
         dense::BatchLauncher f{G.launches, G.spans, G.n_spans, G.head, G.bitmap_words, G.stages, G.carry, s};
-        int st = dense::with_shape(G.first, G.term, G.compact, f);
+        int st = dense::with_shape(G.first, G.term, G.compact, f, G.bound);
         if (st != SDB_OK) return st;
     }
     for (const auto &c : b->singles) {
@@ -2575,6 +2841,13 @@ int sdb_chain_tune_set_op(int terminal, int nregs, int first_op, uint64_t rows, 
     return SDB_OK;
 }
 
+int sdb_fused_launch_counts(uint64_t *specialised, uint64_t *bound)
+{
+    if (specialised) *specialised = dense::g_dense_launches.load(std::memory_order_relaxed);
+    if (bound) *bound = dense::g_bound_launches.load(std::memory_order_relaxed);
+    return SDB_OK;
+}
+
 int sdb_chain_tune_set(int terminal, int nregs, uint64_t rows, int variant)
 {
     return sdb_chain_tune_set_op(terminal, nregs, -1, rows, variant);
@@ -2613,7 +2886,12 @@ int sdb_chain_specialised(const sdb_chain_desc *chain)
     dense::Launch D;
     if (!dense::convert(L, nregs, D)) return 0;
     dense::ShapeProbe probe;
-    return dense::with_shape(D, term, 1, probe) == SDB_OK ? 1 : 0;
+    if (dense::with_shape(D, term, 1, probe) != SDB_OK) return 0;
+    if (dense::can_carry(D, term) && dense::prepare_late(D, term)) {
+        dense::BoundProbe bp;
+        if (dense::with_shape(D, term, 1, bp, true) == SDB_OK && bp.bound) return 2;
+    }
+    return 1;
 }
 
 }  // extern "C"

@@ -210,6 +210,109 @@ def test_chain_specialised_is_a_host_query():
     assert L.sdb_chain_specialised(ctypes.byref(d)) == capi.SDB_ERR_INVALID
 
 
+def _col(o, addr):
+    o.kind = capi.SRC_COL
+    o.col = addr
+
+
+def _reg(o, r):
+    o.kind = capi.SRC_REG
+    o.reg = r
+
+
+def _star_desc(keys=(1, 0)):
+    """The star-join chain as the executor's fuser emits it: semi probe on
+    suppkey; full probes on partkey (-> r0) and orderdate (-> r1); group by
+    (r1, r0) summing revenue."""
+    d = capi.ChainDesc()
+    d.n = 1 << 20
+    d.n_ops = 3
+    o = d.ops[0]
+    o.kind, o.lo, o.hi, o.ht = capi.OP_SEMI_PROBE, 1, 40000, 0x200000
+    _col(o.a, 0x10000000)
+    for i, (col, ht, reg) in enumerate(((0x20000000, 0x300000, 0), (0x30000000, 0x400000, 1)), start=1):
+        o = d.ops[i]
+        o.kind, o.lo, o.hi, o.ht, o.out_reg = capi.OP_FULL_PROBE, 1, 1000, ht, reg
+        _col(o.a, col)
+    d.terminal = capi.TERM_GROUPBY
+    _col(d.value, 0x40000000)
+    d.n_keys = 2
+    for q, r in enumerate(keys):
+        _reg(d.keys[q], r)
+        d.key_min[q], d.key_max[q] = 0, 99
+        d.out_keys[q] = 0x500000 + 0x10000 * q
+    d.P, d.out_sum, d.occ = 10000, 0x600000, 0x700000
+    return d
+
+
+def _date_join_desc():
+    """Date join: discount range; full probe on orderdate (-> r0); r1 =
+    extendedprice * discount; group by r0 summing r1."""
+    d = capi.ChainDesc()
+    d.n = 1 << 20
+    d.n_ops = 3
+    o = d.ops[0]
+    o.kind, o.lo, o.hi, o.logic_op = capi.OP_SEARCH_RANGE, 4, 6, capi.AND
+    _col(o.a, 0x10000000)
+    o = d.ops[1]
+    o.kind, o.lo, o.hi, o.ht, o.out_reg = capi.OP_FULL_PROBE, 19920101, 19981230, 0x300000, 0
+    _col(o.a, 0x20000000)
+    o = d.ops[2]
+    o.kind, o.bin_op, o.out_reg = capi.OP_BINOP, capi.MUL, 1
+    _col(o.a, 0x30000000)
+    _col(o.b, 0x10000000)
+    d.terminal = capi.TERM_GROUPBY
+    _reg(d.value, 1)
+    d.n_keys = 1
+    _reg(d.keys[0], 0)
+    d.key_min[0], d.key_max[0] = 1992, 1998
+    d.out_keys[0] = 0x500000
+    d.P, d.out_sum, d.occ = 7, 0x600000, 0x700000
+    return d
+
+
+def _filter_sum_desc():
+    """Filter-project-sum: orderdate and discount ranges, quantity < 25;
+    r0 = extendedprice * discount; sum r0."""
+    d = capi.ChainDesc()
+    d.n = 1 << 20
+    d.n_ops = 4
+    for i, (col, lo, hi) in enumerate(((0x10000000, 19940101, 19941231), (0x20000000, 1, 3))):
+        o = d.ops[i]
+        o.kind, o.lo, o.hi, o.logic_op = capi.OP_SEARCH_RANGE, lo, hi, capi.AND
+        _col(o.a, col)
+    o = d.ops[2]
+    o.kind, o.cmp_op, o.logic_op = capi.OP_SELECT, capi.LT, capi.AND
+    _col(o.a, 0x30000000)
+    o.b.kind, o.b.lit = capi.SRC_LIT, 25
+    o = d.ops[3]
+    o.kind, o.bin_op, o.out_reg = capi.OP_BINOP, capi.MUL, 0
+    _col(o.a, 0x40000000)
+    _col(o.b, 0x20000000)
+    d.terminal = capi.TERM_SUM
+    _reg(d.value, 0)
+    d.sum_out = 0x600000
+    return d
+
+
+def test_hot_shapes_take_their_bound_pass():
+    """The star join, date join and filter-project-sum chains in the form
+    the fuser emits map to their bound pass (2); an operand elsewhere (the
+    star's group keys swapped, a column in place of the select's literal)
+    keeps the shape's run-time-bound pass (1)."""
+    L = capi.lib()
+    for d in (_star_desc(), _date_join_desc(), _filter_sum_desc()):
+        assert L.sdb_chain_specialised(ctypes.byref(d)) == 2
+    d = _star_desc(keys=(0, 1))
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
+    d = _filter_sum_desc()
+    _col(d.ops[2].b, 0x10000000)  # quantity < orderdate
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
+    d = _star_desc()
+    d.n = 1 << 31  # row numbers past 31 bits: no late columns, no bound pass
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
+
+
 def test_plan_order_matches_the_oracle_for_every_shape():
     """The engine's DAG order (operations/preprocessing.cpp:14-102, lineorder
     scans deferred) equals the oracle restatement's for every plan builder."""

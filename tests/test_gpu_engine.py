@@ -179,6 +179,28 @@ def test_reversed_search_range_is_empty(variant):
         capi.force_chain_variant(-1)
 
 
+def test_variant_8_runs_the_hot_shapes_bound():
+    """Under variant 8 the star join, date join and filter-project-sum plans
+    of the benchmark, as the executor fuses them, run their bound passes
+    (every operand at a place fixed at compile time), with the oracle's
+    results."""
+    ds = datasets.dataset(0.05)
+    pls = [plans.plan_star(2, 11), plans.plan_date_join(1995), plans.plan_filter_sum(1994),
+           plans.plan_star(1, 3, 1993, 1996, 12)]
+    try:
+        with Engine(arena_bytes=1 << 30, fuse=True) as eng:
+            capi.force_chain_variant(8)
+            load(eng, ds)
+            for p in pls:
+                before = capi.fused_launch_counts()
+                got = eng.execute(p).canonical()
+                after = capi.fused_launch_counts()
+                assert after[1] - before[1] >= 1, json.dumps(p)  # a bound pass ran
+                assert got == datasets.oracle_run(ds, p), json.dumps(p)
+    finally:
+        capi.force_chain_variant(-1)
+
+
 def test_plan_cache_replays_give_the_plain_results():
     """plan_cache: a plan seen twice becomes a prepared graph; replays, LRU
     eviction and table reloads all give the plain path's rows."""
