@@ -83,7 +83,8 @@ def _plan_date_join():
 
 # name -> (plan builder, fact columns key, dominant kernel)
 PLANS = {
-    "star": (_plan_star, "star", "k_dense (fused chain: semi + full + full probe, warp compaction, group-by)"),
+    "star": (_plan_star, "star", "k_dense (fused chain: semi + full + full probe, warp compaction, group-by; the "
+                                 "tuned variant, at SF20 the bound pass with late columns)"),
     "filter_sum": (_plan_filter_sum, "q1", "k_dense (fused chain: range + range + select + projection, sum)"),
     "date_join": (_plan_date_join, "q2", "k_dense (fused chain: range + full probe + projection, group-by)"),
 }
@@ -511,6 +512,10 @@ def run_ours(args, rank, world, local, pg):
             "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": (achieved / peak) if achieved else None, "peak_kind": peak_kind,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg_bytes,
+            "dram_gbs": (traffic / per_launch_ms / 1e6) if (traffic and per_launch_ms) else None,
+            "traffic_note": ("DRAM bytes per launch from the committed ncu summary; below the algorithmic bytes "
+                             "when the pass reads late columns only in the sectors of the rows that reach them"
+                             if traffic else None),
             "launch_ms": per_launch_ms, "launches": fused_launches,
             "timing": "CUDA events around each %s on the executor stream, %d plain-path steps" %
                       ("fused-pass launch" if fuse else "kernel launch, summed per step", prof_steps)}
