@@ -155,6 +155,31 @@ int sdb_ht_build_kv(const int32_t *key, const int32_t *val, const uint8_t *flags
 int sdb_probe_full(const int32_t *key, int32_t *val_out, const uint8_t *in, uint8_t *out,
                    uint64_t n, const int32_t *ht2, int32_t min, int32_t max, sdb_stream_t stream);
 
+/* K10-K13 on open-addressing tables, for join keys whose range [min, max] is
+ * much wider than the build side's rows (the engine's choice; the reference
+ * sizes its direct-address table by the range, models/models.hpp:1413-1452,
+ * 1509-1548, which a sparse key range makes as large as the range).  The
+ * table has 2^log2_slots slots (sdb_oa_log2_slots: at least twice the build
+ * rows) and must be all zero before its first build.  A slot is a 32-bit
+ * word tag << 1 | flag, tag = key - min + 1 (0 = empty), claimed with
+ * atomicCAS and probed linearly; the key/value table pairs it with the value
+ * (int32 pairs {word, value}, 8-byte aligned).  Builds write what K10/K12
+ * write -- a live row its key's hit (and value), a dead row a miss; `fresh`
+ * (the table is all zero and no other build writes it meanwhile) skips dead
+ * rows, as ht_zeroed does for the fused build.  Probes give exactly the hits
+ * and values of K11/K13 on the direct table.  The key range must hold fewer
+ * than 2^31 keys; keys outside it miss (probe) or are counted as errors and
+ * skipped (build). */
+int sdb_oa_log2_slots(uint64_t build_rows); /* smallest lg >= 4 with 2^lg >= 2 rows; rows <= 2^30 */
+int sdb_ht_build_keys_oa(const int32_t *key, const uint8_t *flags, uint64_t n, uint32_t *ht, int log2_slots,
+                         int32_t min, int32_t max, int fresh, sdb_stream_t stream);
+int sdb_probe_semi_oa(const int32_t *key, const uint8_t *in, uint8_t *out, uint64_t n, const uint32_t *ht,
+                      int log2_slots, int32_t min, int32_t max, sdb_stream_t stream);
+int sdb_ht_build_kv_oa(const int32_t *key, const int32_t *val, const uint8_t *flags, uint64_t n, int32_t *ht2,
+                       int log2_slots, int32_t min, int32_t max, int fresh, sdb_stream_t stream);
+int sdb_probe_full_oa(const int32_t *key, int32_t *val_out, const uint8_t *in, uint8_t *out, uint64_t n,
+                      const int32_t *ht2, int log2_slots, int32_t min, int32_t max, sdb_stream_t stream);
+
 /* K14: ids[0..count) = indices of set flags, in increasing order; *count
  * (device word) = how many.  Replaces build_row_ids
  * (models/transient_table.hpp:535-599), whose atomic append gives the same
@@ -267,7 +292,8 @@ typedef struct sdb_chain_op {
     sdb_operand b;
     int32_t lo, hi;      /* SEARCH bounds or probe min/max */
     int32_t out_reg;     /* FULL_PROBE / BINOP / FILL */
-    int32_t pad;
+    int32_t ht_log2;     /* SEMI / FULL: 0 = direct-address table (below); n > 0 = open-addressing
+                            table of 2^n slots (layout of sdb_probe_semi_oa / sdb_probe_full_oa) */
     const void *ht;      /* SEMI: uint8[hi-lo+1]; FULL: int32[2*(hi-lo+1)] */
     int32_t *out_col;    /* FULL_PROBE / BINOP / FILL: if non-NULL the register
                             is also stored where the composed kernel stores it */
@@ -313,7 +339,9 @@ typedef struct sdb_chain_desc {
                                    zero) is skipped, so dead rows cost no key load and no store.  With
                                    duplicate keys the table is the one the reference's unordered
                                    writes give when dead rows write first. */
-    int32_t pad2;
+    int32_t ht_log2;            /* BUILD: 0 = direct-address table (ht_len entries from ht_min);
+                                   n > 0 = open-addressing table of 2^n slots over the keys
+                                   ht_min .. ht_min + ht_len - 1 (sdb_ht_build_keys_oa layout) */
 } sdb_chain_desc;
 
 /* Launch one fused pass.  The descriptor is read on the host (copied into
@@ -459,6 +487,11 @@ typedef struct sdb_engine_config {
     int32_t order_by;           /* 1: sdb_engine_execute orders result rows by the plan's last SORT
                                    collation on the device (sdb_sort_rows); 0: rows in the order the
                                    reference gives them (its SORT is a pass-through) */
+    int32_t join_tables;        /* 0: a join's table is direct-address over the build key range (the
+                                   reference's), or open-addressing (sdb_ht_build_keys_oa) when the
+                                   range is sparse: at least 2^20 keys and 8 x the open-addressing
+                                   slots (16 x the build rows); 1: always direct-address; 2: always
+                                   open-addressing.  Results are the same either way. */
 } sdb_engine_config;
 
 /* Plan text.  Every entry that takes plan_json reads two dialects: the

@@ -47,7 +47,7 @@ class Operand(ctypes.Structure):
 class ChainOp(ctypes.Structure):
     _fields_ = [("kind", c_int32), ("cmp_op", c_int32), ("logic_op", c_int32), ("bin_op", c_int32),
                 ("a", Operand), ("b", Operand), ("lo", c_int32), ("hi", c_int32), ("out_reg", c_int32),
-                ("pad", c_int32), ("ht", c_void_p), ("out_col", c_void_p)]
+                ("ht_log2", c_int32), ("ht", c_void_p), ("out_col", c_void_p)]
 
 
 class ChainDesc(ctypes.Structure):
@@ -57,12 +57,12 @@ class ChainDesc(ctypes.Structure):
                 ("key_min", c_int32 * CHAIN_MAX_KEYS), ("key_max", c_int32 * CHAIN_MAX_KEYS), ("P", c_uint64),
                 ("out_keys", c_void_p * CHAIN_MAX_KEYS), ("out_sum", c_void_p), ("occ", c_void_p),
                 ("build_key", Operand), ("build_val", Operand), ("ht_out", c_void_p), ("ht_min", c_int32),
-                ("ht_len", c_int32), ("ht_zeroed", c_int32), ("pad2", c_int32)]
+                ("ht_len", c_int32), ("ht_zeroed", c_int32), ("ht_log2", c_int32)]
 
 
 class EngineConfig(ctypes.Structure):
     _fields_ = [("arena_bytes", c_uint64), ("segment_rows", c_uint64), ("fuse", c_int32), ("profile", c_int32),
-                ("stream", c_void_p), ("plan_cache", c_int32), ("order_by", c_int32)]
+                ("stream", c_void_p), ("plan_cache", c_int32), ("order_by", c_int32), ("join_tables", c_int32)]
 
 
 class BatchStats(ctypes.Structure):
@@ -110,6 +110,11 @@ _SIGS = {
     "sdb_probe_semi": (c_int, [_P, _P, _P, c_uint64, _P, c_int32, c_int32, _P]),
     "sdb_ht_build_kv": (c_int, [_P, _P, _P, c_uint64, _P, c_int32, c_int32, _P]),
     "sdb_probe_full": (c_int, [_P, _P, _P, _P, c_uint64, _P, c_int32, c_int32, _P]),
+    "sdb_oa_log2_slots": (c_int, [c_uint64]),
+    "sdb_ht_build_keys_oa": (c_int, [_P, _P, c_uint64, _P, c_int, c_int32, c_int32, c_int, _P]),
+    "sdb_probe_semi_oa": (c_int, [_P, _P, _P, c_uint64, _P, c_int, c_int32, c_int32, _P]),
+    "sdb_ht_build_kv_oa": (c_int, [_P, _P, _P, c_uint64, _P, c_int, c_int32, c_int32, c_int, _P]),
+    "sdb_probe_full_oa": (c_int, [_P, _P, _P, _P, c_uint64, _P, c_int, c_int32, c_int32, _P]),
     "sdb_compact_scratch_bytes": (c_size_t, [c_uint64]),
     "sdb_compact_row_ids": (c_int, [_P, c_uint64, _P, _P, _P, c_size_t, _P]),
     "sdb_compact_row_ids_noalloc": (c_int, [_P, c_uint64, _P, _P, _P]),

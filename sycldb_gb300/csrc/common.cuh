@@ -76,6 +76,73 @@ __host__ __device__ __forceinline__ int64_t ht_slot(int32_t x, int32_t len, int3
     return (int64_t)(d % len);
 }
 
+// ---- open-addressing join tables (sparse key ranges) -------------------------
+// A join table over keys [min, max] whose range is much wider than the build
+// side's rows is kept as 2^lg slots of linear probing instead of one entry
+// per key of the range (the reference's direct-address HASH).  A slot's
+// 32-bit word is tag << 1 | flag with tag = key - min + 1 (range < 2^31, so
+// the tag fits 31 bits; word 0 = empty slot); a key/value table pairs the
+// word with the value (int2 {word, value}).  Inserts claim an empty slot
+// with atomicCAS; a key's flag and value are then stored as the direct
+// table stores them (the reference's unordered writes), so probes see the
+// same hits and values as with the direct table.  Tables are sized at least
+// twice the build side's rows, so an insert always finds a slot; every
+// probe loop is still bounded by the slot count.
+__host__ __device__ __forceinline__ uint32_t oa_tag(int32_t key, int32_t mn)
+{
+    return (uint32_t)key - (uint32_t)mn + 1u;
+}
+
+__host__ __device__ __forceinline__ uint32_t oa_home(uint32_t tag, int lg)
+{
+    return (tag * 2654435761u) >> (32 - lg);
+}
+
+// Looks tag up in a table of 2^lg slots whose words are STRIDE words apart
+// (1: keys table, 2: key/value table).  Returns the slot, or -1 when the key
+// is absent.
+template <int STRIDE>
+__device__ __forceinline__ int64_t oa_find(const uint32_t *words, int lg, uint32_t tag)
+{
+    const uint32_t mask = (uint32_t)((1ull << lg) - 1);
+    uint32_t h = oa_home(tag, lg);
+    for (uint64_t i = 0; i <= mask; i++) {
+        const uint32_t w = __ldg(words + (uint64_t)h * STRIDE);
+        if (w == 0) return -1;
+        if ((w >> 1) == tag) return (int64_t)h;
+        h = (h + 1) & mask;
+    }
+    return -1;
+}
+
+// Writes (tag, live) into the table: a live row claims the key's slot (or
+// its empty home run) and sets its flag, a dead row clears the flag of a key
+// already present (absent reads as a miss already).  Returns the slot
+// written (the caller stores a live row's value there), -1 when nothing was
+// written, -2 when the table had no free slot (sized too small).
+template <int STRIDE>
+__device__ __forceinline__ int64_t oa_put(uint32_t *words, int lg, uint32_t tag, bool live)
+{
+    const uint32_t mask = (uint32_t)((1ull << lg) - 1);
+    const uint32_t want = (tag << 1) | (live ? 1u : 0u);
+    uint32_t h = oa_home(tag, lg);
+    for (uint64_t i = 0; i <= mask; i++) {
+        uint32_t *p = words + (uint64_t)h * STRIDE;
+        uint32_t w = *p;
+        if (w == 0) {
+            if (!live) return -1;
+            w = atomicCAS(p, 0u, want);
+            if (w == 0) return (int64_t)h;
+        }
+        if ((w >> 1) == tag) {
+            atomicExch(p, want);
+            return (int64_t)h;
+        }
+        h = (h + 1) & mask;
+    }
+    return -2;
+}
+
 // Group-by slot: hash = sum_j (k_j - min_j) * mult_j in wrapping int, then
 // `hash %= prod_ranges` with hash converted to uint64 and the result stored
 // back into an int.

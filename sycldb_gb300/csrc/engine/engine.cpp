@@ -365,6 +365,7 @@ struct KernelData {
     int32_t *res = nullptr;            // fill / perform result, full-join value output
     void *ht = nullptr;
     int32_t ht_min = 0, ht_max = 0, ht_len = 0;
+    int ht_log2 = 0;        // 0: direct-address table; n: open-addressing table of 2^n slots
     bool ht_fresh = false;  // builds: the table is still all zero (the first segment's build)
     uint64_t *agg_res = nullptr;
     std::vector<const int32_t *> keys;  // group-by
@@ -387,12 +388,23 @@ struct KernelData {
         case KernelType::PerformOperationKernelLiteralFirst: return sdb_binop_lc(res, la, b, bin, in, n, st);
         case KernelType::PerformOperationKernelLiteralSecond: return sdb_binop_cl(res, a, lb, bin, in, n, st);
         case KernelType::BuildKeysHTKernel:
+            if (ht_log2)
+                return sdb_ht_build_keys_oa(a, in, n, static_cast<uint32_t *>(ht), ht_log2, ht_min,
+                                            (int32_t)((uint32_t)ht_min + (uint32_t)ht_len - 1u), ht_fresh ? 1 : 0, st);
             return sdb_ht_build_keys(a, in, n, static_cast<uint8_t *>(ht), ht_min, ht_len, st);
         case KernelType::FilterJoinKernel:
+            if (ht_log2)
+                return sdb_probe_semi_oa(a, in, out, n, static_cast<const uint32_t *>(ht), ht_log2, ht_min, ht_max, st);
             return sdb_probe_semi(a, in, out, n, static_cast<const uint8_t *>(ht), ht_min, ht_max, st);
         case KernelType::BuildKeyValsHTKernel:
+            if (ht_log2)
+                return sdb_ht_build_kv_oa(a, b, in, n, static_cast<int32_t *>(ht), ht_log2, ht_min,
+                                          (int32_t)((uint32_t)ht_min + (uint32_t)ht_len - 1u), ht_fresh ? 1 : 0, st);
             return sdb_ht_build_kv(a, b, in, n, static_cast<int32_t *>(ht), ht_min, ht_len, st);
         case KernelType::FullJoinKernel:
+            if (ht_log2)
+                return sdb_probe_full_oa(a, res, in, out, n, static_cast<const int32_t *>(ht), ht_log2, ht_min, ht_max,
+                                         st);
             return sdb_probe_full(a, res, in, out, n, static_cast<const int32_t *>(ht), ht_min, ht_max, st);
         case KernelType::AggregateOperationKernel: return sdb_sum_i32_u64(a, in, n, agg_res, st);
         case KernelType::GroupByAggregateKernel:
@@ -586,6 +598,7 @@ struct Fuser {
                     op.lo = k.ht_min;
                     op.hi = k.ht_max;
                     op.ht = k.ht;
+                    op.ht_log2 = k.ht_log2;
                     cur = k.out;
                     break;
                 case KernelType::FullJoinKernel:
@@ -595,6 +608,7 @@ struct Fuser {
                     op.lo = k.ht_min;
                     op.hi = k.ht_max;
                     op.ht = k.ht;
+                    op.ht_log2 = k.ht_log2;
                     op.out_reg = nregs;
                     op.out_col = k.res;
                     regmap[k.res] = nregs++;
@@ -656,6 +670,7 @@ struct Fuser {
                     c.ht_out = k.ht;
                     c.ht_min = k.ht_min;
                     c.ht_len = k.ht_len;
+                    c.ht_log2 = k.ht_log2;
                     c.ht_zeroed = k.ht_fresh ? 1 : 0;
                     terminal = true;
                     break;
@@ -1351,9 +1366,18 @@ public:
         if (len <= 0) throw Error(SDB_ERR_NOMEM, "join key range too large");
         auto lsg = segs();
         auto rsg = right.segs();
+        // table layout: the reference's direct-address table over [mn, mx], or
+        // open addressing (2^lg slots, at least twice the build rows) for a
+        // sparse key range; the probes see the same hits and values
+        int lg = 0;
+        if (E.cfg.join_tables != 1 && right.nrows <= (1ull << 30)) {
+            const int cand = sdb_oa_log2_slots(std::max<uint64_t>(right.nrows, 1));
+            const bool sparse = (uint64_t)len >= (1ull << 20) && (uint64_t)len >= 8 * (1ull << cand);
+            if (cand > 0 && (E.cfg.join_tables == 2 || sparse)) lg = cand;
+        }
         if (rel.joinType == "semi") {
             // Column::build_keys_hash_table: models/models.hpp:1413-1452
-            uint8_t *ht = E.mm.alloc_zero<uint8_t>((uint64_t)len);
+            void *ht = lg ? (void *)E.mm.alloc_zero<uint32_t>(1ull << lg) : (void *)E.mm.alloc_zero<uint8_t>((uint64_t)len);
             std::vector<KernelBundle> hb;
             for (size_t s = 0; s < rsg.size(); s++) {
                 KernelBundle b;
@@ -1365,6 +1389,7 @@ public:
                 k.ht = ht;
                 k.ht_min = mn;
                 k.ht_len = len;
+                k.ht_log2 = lg;
                 k.ht_fresh = s == 0;  // alloc_zero; later segments keep the reference's segment order
                 b.add_kernel(k);
                 hb.push_back(b);
@@ -1384,6 +1409,7 @@ public:
                 k.ht = ht;
                 k.ht_min = mn;
                 k.ht_max = mx;
+                k.ht_log2 = lg;
                 b.add_kernel(k);
                 ops.push_back(b);
             }
@@ -1400,7 +1426,7 @@ public:
             for (size_t i = 0; i < right.current_columns.size(); i++) current_columns.push_back(nullptr);
             current_columns[gidx] = &nc;
             // Column::build_key_vals_hash_table: models/models.hpp:1509-1548
-            int32_t *ht = E.mm.alloc_zero<int32_t>(2 * (uint64_t)len);
+            int32_t *ht = E.mm.alloc_zero<int32_t>(2 * (lg ? (1ull << lg) : (uint64_t)len));
             std::vector<KernelBundle> hb;
             for (size_t s = 0; s < rsg.size(); s++) {
                 KernelBundle b;
@@ -1413,6 +1439,7 @@ public:
                 k.ht = ht;
                 k.ht_min = mn;
                 k.ht_len = len;
+                k.ht_log2 = lg;
                 k.ht_fresh = s == 0;  // alloc_zero; later segments keep the reference's segment order
                 b.add_kernel(k);
                 hb.push_back(b);
@@ -1433,6 +1460,7 @@ public:
                 k.ht = ht;
                 k.ht_min = mn;
                 k.ht_max = mx;
+                k.ht_log2 = lg;
                 nc.segments[s].min = gmm.first;
                 nc.segments[s].max = gmm.second;
                 b.add_kernel(k);
@@ -2703,6 +2731,7 @@ int sdb_engine_create(const sdb_engine_config *cfg, sdb_engine **out)
         E.mm.init(budget, E.stream);
         E.prof.on = E.cfg.profile != 0;
         if (E.cfg.plan_cache < 0) throw sdb::Error(SDB_ERR_INVALID, "plan_cache must be >= 0");
+        if (E.cfg.join_tables < 0 || E.cfg.join_tables > 2) throw sdb::Error(SDB_ERR_INVALID, "join_tables must be 0, 1 or 2");
         SDB_CUDA(cudaEventCreate(&E.plan_a));
         SDB_CUDA(cudaEventCreate(&E.plan_b));
         SDB_CUDA(cudaStreamSynchronize(E.stream));

@@ -206,10 +206,23 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
             fetch<STREAM>(op.a, T, need, a);
             const uint8_t *ht = static_cast<const uint8_t *>(op.ht);
             uint8_t h[ITEMS];
+            if (op.ht_log2) {  // open-addressing table
+                const uint32_t *w = static_cast<const uint32_t *>(op.ht);
 #pragma unroll
-            for (int k = 0; k < ITEMS; k++) {
-                h[k] = 0;
-                if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) h[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+                for (int k = 0; k < ITEMS; k++) {
+                    h[k] = 0;
+                    if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) {
+                        const int64_t s = sdb::oa_find<1>(w, op.ht_log2, sdb::oa_tag(a[k], op.lo));
+                        h[k] = s >= 0 ? (uint8_t)(__ldg(w + s) & 1u) : 0;
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < ITEMS; k++) {
+                    h[k] = 0;
+                    if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi)
+                        h[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+                }
             }
             uint32_t m = 0;
 #pragma unroll
@@ -222,10 +235,26 @@ __device__ __forceinline__ void run_ops(const LC &Lc, Tile<NREGS, ITEMS> &T)
             fetch<STREAM>(op.a, T, need, a);
             const int2 *ht = static_cast<const int2 *>(op.ht);
             int2 e[ITEMS];
+            if (op.ht_log2) {  // open-addressing table: hit = the word's flag bit
 #pragma unroll
-            for (int k = 0; k < ITEMS; k++) {
-                e[k] = make_int2(0, 0);
-                if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) e[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+                for (int k = 0; k < ITEMS; k++) {
+                    e[k] = make_int2(0, 0);
+                    if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi) {
+                        const int64_t s = sdb::oa_find<2>(static_cast<const uint32_t *>(op.ht), op.ht_log2,
+                                                          sdb::oa_tag(a[k], op.lo));
+                        if (s >= 0) {
+                            e[k] = __ldg(ht + s);
+                            e[k].x &= 1;
+                        }
+                    }
+                }
+            } else {
+#pragma unroll
+                for (int k = 0; k < ITEMS; k++) {
+                    e[k] = make_int2(0, 0);
+                    if (((need >> k) & 1u) && a[k] >= op.lo && a[k] <= op.hi)
+                        e[k] = __ldg(ht + ((uint32_t)a[k] - (uint32_t)op.lo));
+                }
             }
             uint32_t m = 0;
 #pragma unroll
@@ -313,6 +342,23 @@ __device__ __forceinline__ void build_store(const sdb_chain_desc &d, uint32_t ro
 {
     const bool kv = d.terminal == SDB_TERM_BUILD_KV;
     const uint32_t len = (uint32_t)d.ht_len;  // > 0
+    if (d.ht_log2) {  // open-addressing table over keys ht_min .. ht_min + len - 1
+        uint32_t *w = static_cast<uint32_t *>(d.ht_out);
+#pragma unroll
+        for (int k = 0; k < ITEMS; k++) {
+            if (!((rows >> k) & 1u)) continue;
+            const bool hit = (live >> k) & 1u;
+            if ((uint32_t)key[k] - (uint32_t)d.ht_min >= len) {
+                atomicAdd(&g_errors, 1ull);
+                continue;
+            }
+            const uint32_t tag = sdb::oa_tag(key[k], d.ht_min);
+            const int64_t h = kv ? sdb::oa_put<2>(w, d.ht_log2, tag, hit) : sdb::oa_put<1>(w, d.ht_log2, tag, hit);
+            if (h == -2) atomicAdd(&g_errors, 1ull);
+            else if (kv && h >= 0 && hit) static_cast<int32_t *>(d.ht_out)[2 * h + 1] = val[k];
+        }
+        return;
+    }
 #pragma unroll
     for (int k = 0; k < ITEMS; k++) {
         if (!((rows >> k) & 1u)) continue;
@@ -1892,6 +1938,8 @@ bool convert(const ChainLaunch &C, int nregs, Launch &D)
         d.out_reg = o.out_reg;
         d.ht = o.ht;
         d.out_col = o.out_col;
+        // open-addressing tables go through the general pass
+        if ((o.kind == SDB_OP_SEMI_PROBE || o.kind == SDB_OP_FULL_PROBE) && o.ht_log2) return false;
         if (o.kind == SDB_OP_SEMI_PROBE && !D.bitmap_ht) {
             const uint64_t len = (uint64_t)((int64_t)o.hi - (int64_t)o.lo + 1);
             if (len >= 1 && len <= kBitmapMax) {
@@ -2412,6 +2460,11 @@ int sdb_chain_prepare(const sdb_chain_desc *c, void *launch_out, size_t launch_b
             if (!operand_ok(op.a, nregs, vec, &why)) goto bad;
             if (!op.ht) { why = "probe without a hash table"; goto bad; }
             if (op.kind == SDB_OP_FULL_PROBE && !sdb::aligned(op.ht, 8)) { why = "key/value table must be 8-byte aligned"; goto bad; }
+            if (op.ht_log2 < 0 || op.ht_log2 > 31) { why = "ht_log2 outside [0,31]"; goto bad; }
+            if (op.ht_log2 && (!sdb::aligned(op.ht, 4) || op.lo > op.hi || (uint32_t)op.hi - (uint32_t)op.lo >= 0x7fffffffu)) {
+                why = "open-addressing probe: table not aligned, or key range empty or of 2^31 keys or more";
+                goto bad;
+            }
             if (op.kind == SDB_OP_FULL_PROBE) {
                 if (op.out_reg < 0 || op.out_reg >= SDB_CHAIN_MAX_REGS) { why = "out_reg out of range"; goto bad; }
                 nregs = std::max(nregs, op.out_reg + 1);
@@ -2471,6 +2524,11 @@ int sdb_chain_prepare(const sdb_chain_desc *c, void *launch_out, size_t launch_b
         const bool kv = c->terminal == SDB_TERM_BUILD_KV;
         if (!c->ht_out || c->ht_len <= 0) { why = "a build needs ht_out and ht_len > 0"; goto bad; }
         if (kv && !sdb::aligned(c->ht_out, 8)) { why = "key/value table must be 8-byte aligned"; goto bad; }
+        if (c->ht_log2 < 0 || c->ht_log2 > 31) { why = "ht_log2 outside [0,31]"; goto bad; }
+        if (c->ht_log2 && (!sdb::aligned(c->ht_out, 4) || c->ht_len == 0x7fffffff)) {
+            why = "open-addressing build: table not aligned or 2^31 keys or more";
+            goto bad;
+        }
         if (!operand_ok(c->build_key, nregs, vec, &why)) goto bad;
         if (kv && !operand_ok(c->build_val, nregs, vec, &why)) goto bad;
         *term_out = T_BUILD;

@@ -550,6 +550,105 @@ struct ProbeFull {
     }
 };
 
+// ------------------------------------------- K10 - K13 on open-addressing tables
+// The same builds and probes over a table of 2^lg slots (sdb::oa_put /
+// oa_find): a build row writes its key's slot as the direct-address build
+// writes key - min (live: hit and value, dead: miss); `fresh` (the table is
+// all zero and no other build writes it) skips dead rows, whose miss the
+// empty table already reads.
+__global__ void __launch_bounds__(kMaxBlock) k_build_keys_oa(const int32_t *key, const uint8_t *flags, uint64_t n,
+                                                            uint32_t *ht, int lg, int32_t mn, int32_t mx, int fresh)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const bool live = flags[r] != 0;
+        if (!live && fresh) continue;
+        const int32_t k = key[r];
+        if (k < mn || k > mx || sdb::oa_put<1>(ht, lg, sdb::oa_tag(k, mn), live) == -2) atomicAdd(&g_errors, 1ull);
+    }
+}
+
+__global__ void __launch_bounds__(kMaxBlock) k_build_kv_oa(const int32_t *key, const int32_t *val, const uint8_t *flags,
+                                                          uint64_t n, int32_t *ht2, int lg, int32_t mn, int32_t mx,
+                                                          int fresh)
+{
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t r = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += stride) {
+        const bool live = flags[r] != 0;
+        if (!live && fresh) continue;
+        const int32_t k = key[r];
+        if (k < mn || k > mx) {
+            atomicAdd(&g_errors, 1ull);
+            continue;
+        }
+        const int64_t h = sdb::oa_put<2>(reinterpret_cast<uint32_t *>(ht2), lg, sdb::oa_tag(k, mn), live);
+        if (h == -2) atomicAdd(&g_errors, 1ull);
+        else if (h >= 0 && live) ht2[2 * h + 1] = val[r];
+    }
+}
+
+struct ProbeSemiOA {
+    const int32_t *key; const uint8_t *in; uint8_t *out; const uint32_t *ht; int lg; int32_t mn, mx;
+    __device__ bool one(int32_t k, bool fin) const
+    {
+        if (!fin || k < mn || k > mx) return false;
+        const int64_t h = sdb::oa_find<1>(ht, lg, sdb::oa_tag(k, mn));
+        return h >= 0 && (__ldg(ht + h) & 1u);
+    }
+    __device__ void group(uint64_t r0) const
+    {
+        uint32_t f = ldf8(in, r0), m = 0;
+        if (f) {
+            int32_t k[8];
+            ld8(key, r0, k);
+#pragma unroll
+            for (int j = 0; j < 8; j++) m |= (uint32_t)one(k[j], (f >> j) & 1u) << j;
+        }
+        stf8(out, r0, m);
+    }
+    __device__ void row(uint64_t r) const { out[r] = in[r] ? one(key[r], true) : 0; }
+};
+
+struct ProbeFullOA {
+    const int32_t *key; int32_t *val_out; const uint8_t *in; uint8_t *out; const int32_t *ht2; int lg; int32_t mn, mx;
+    __device__ bool one(int32_t k, bool fin, int32_t &v) const
+    {
+        if (!fin || k < mn || k > mx) return false;
+        const int64_t h = sdb::oa_find<2>(reinterpret_cast<const uint32_t *>(ht2), lg, sdb::oa_tag(k, mn));
+        if (h < 0) return false;
+        const int2 e = __ldg(reinterpret_cast<const int2 *>(ht2) + h);
+        v = e.y;
+        return (e.x & 1) != 0;
+    }
+    __device__ void group(uint64_t r0) const
+    {
+        uint32_t f = ldf8(in, r0), m = 0;
+        if (f) {
+            int32_t k[8];
+            ld8(key, r0, k);
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                int32_t v;
+                if (one(k[j], (f >> j) & 1u, v)) {
+                    val_out[r0 + j] = v;
+                    m |= 1u << j;
+                }
+            }
+        }
+        stf8(out, r0, m);
+    }
+    __device__ void row(uint64_t r) const
+    {
+        int32_t v;
+        if (in[r] && one(key[r], true, v)) {
+            val_out[r] = v;
+            out[r] = 1;
+        } else {
+            out[r] = 0;
+        }
+    }
+};
+
 // ---------------------------------------------------------------- K14, K15
 constexpr int kCompactRowsPerThread = 16;
 constexpr int kCompactChunk = kThreads * kCompactRowsPerThread;  // rows per block-chunk
@@ -987,6 +1086,75 @@ int sdb_probe_full(const int32_t *key, int32_t *val_out, const uint8_t *in, uint
     if (sdb::aligned(ht2, 8))
         return launch_map(n, vec, ProbeFull<true>{key, val_out, in, out, ht2, min, max}, s, "sdb_probe_full", SDB_OPK_PROBE_FULL);
     return launch_map(n, vec, ProbeFull<false>{key, val_out, in, out, ht2, min, max}, s, "sdb_probe_full", SDB_OPK_PROBE_FULL);
+}
+
+int sdb_oa_log2_slots(uint64_t build_rows)
+{
+    if (build_rows > (1ull << 30)) return sdb_set_error(SDB_ERR_INVALID, "sdb_oa_log2_slots: more than 2^30 rows");
+    int lg = 4;
+    while ((1ull << lg) < 2 * build_rows) lg++;
+    return lg;
+}
+
+// Checks the arguments every open-addressing entry shares.
+static int oa_check(const char *what, int lg, int32_t mn, int32_t mx, const void *ht, uintptr_t align)
+{
+    if (lg < 1 || lg > 31) return sdb_set_error(SDB_ERR_INVALID, "%s: log2_slots=%d outside [1,31]", what, lg);
+    if (mn > mx || (uint32_t)mx - (uint32_t)mn >= 0x7fffffffu)
+        return sdb_set_error(SDB_ERR_INVALID, "%s: key range [%d,%d] empty or 2^31 keys or more", what, mn, mx);
+    if (!sdb::aligned(ht, align)) return sdb_set_error(SDB_ERR_INVALID, "%s: table not %d-byte aligned", what, (int)align);
+    return SDB_OK;
+}
+
+int sdb_ht_build_keys_oa(const int32_t *key, const uint8_t *flags, uint64_t n, uint32_t *ht, int log2_slots,
+                         int32_t min, int32_t max, int fresh, sdb_stream_t stream)
+{
+    SDB_REQUIRE_ALIGNED(nat4({key}), "sdb_ht_build_keys_oa");
+    if (n && (!key || !flags || !ht)) return sdb_set_error(SDB_ERR_INVALID, "sdb_ht_build_keys_oa: NULL buffer");
+    int st = oa_check("sdb_ht_build_keys_oa", log2_slots, min, max, ht, 4);
+    if (st != SDB_OK || n == 0) return st;
+    const LaunchShape sh = op_shape(SDB_OPK_BUILD_KEYS, n, 8);
+    k_build_keys_oa<<<grid_of(n, sh), sh.block, 0, (cudaStream_t)stream>>>(key, flags, n, ht, log2_slots, min, max,
+                                                                          fresh);
+    return sdb_check_launch("sdb_ht_build_keys_oa");
+}
+
+int sdb_probe_semi_oa(const int32_t *key, const uint8_t *in, uint8_t *out, uint64_t n, const uint32_t *ht,
+                      int log2_slots, int32_t min, int32_t max, sdb_stream_t stream)
+{
+    SDB_REQUIRE_ALIGNED(nat4({key}), "sdb_probe_semi_oa");
+    if (n && (!key || !in || !out || !ht)) return sdb_set_error(SDB_ERR_INVALID, "sdb_probe_semi_oa: NULL buffer");
+    int st = oa_check("sdb_probe_semi_oa", log2_slots, min, max, ht, 4);
+    if (st != SDB_OK) return st;
+    bool vec = col_ok(key) && flags_ok(in) && flags_ok(out);
+    return launch_map(n, vec, ProbeSemiOA{key, in, out, ht, log2_slots, min, max}, (cudaStream_t)stream,
+                      "sdb_probe_semi_oa", SDB_OPK_PROBE_SEMI);
+}
+
+int sdb_ht_build_kv_oa(const int32_t *key, const int32_t *val, const uint8_t *flags, uint64_t n, int32_t *ht2,
+                       int log2_slots, int32_t min, int32_t max, int fresh, sdb_stream_t stream)
+{
+    SDB_REQUIRE_ALIGNED(nat4({key, val}), "sdb_ht_build_kv_oa");
+    if (n && (!key || !val || !flags || !ht2)) return sdb_set_error(SDB_ERR_INVALID, "sdb_ht_build_kv_oa: NULL buffer");
+    int st = oa_check("sdb_ht_build_kv_oa", log2_slots, min, max, ht2, 8);
+    if (st != SDB_OK || n == 0) return st;
+    const LaunchShape sh = op_shape(SDB_OPK_BUILD_KV, n, 8);
+    k_build_kv_oa<<<grid_of(n, sh), sh.block, 0, (cudaStream_t)stream>>>(key, val, flags, n, ht2, log2_slots, min,
+                                                                        max, fresh);
+    return sdb_check_launch("sdb_ht_build_kv_oa");
+}
+
+int sdb_probe_full_oa(const int32_t *key, int32_t *val_out, const uint8_t *in, uint8_t *out, uint64_t n,
+                      const int32_t *ht2, int log2_slots, int32_t min, int32_t max, sdb_stream_t stream)
+{
+    SDB_REQUIRE_ALIGNED(nat4({key, val_out}), "sdb_probe_full_oa");
+    if (n && (!key || !val_out || !in || !out || !ht2))
+        return sdb_set_error(SDB_ERR_INVALID, "sdb_probe_full_oa: NULL buffer");
+    int st = oa_check("sdb_probe_full_oa", log2_slots, min, max, ht2, 8);
+    if (st != SDB_OK) return st;
+    bool vec = col_ok(key) && flags_ok(in) && flags_ok(out);
+    return launch_map(n, vec, ProbeFullOA{key, val_out, in, out, ht2, log2_slots, min, max}, (cudaStream_t)stream,
+                      "sdb_probe_full_oa", SDB_OPK_PROBE_FULL);
 }
 
 size_t sdb_compact_scratch_bytes(uint64_t n)

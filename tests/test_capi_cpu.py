@@ -345,3 +345,28 @@ def test_plan_check_rejects_malformed_graphs():
     for p in bad:
         assert L.sdb_plan_check(json.dumps(p).encode(), None, None, 0) == capi.SDB_ERR_INVALID, json.dumps(p)
         assert capi.last_error()
+
+
+def test_open_addressing_entries_check_on_the_host():
+    """sdb_oa_log2_slots sizes a table at least twice the build rows; the
+    open-addressing entries and chain ops refuse bad slot counts, key ranges
+    and alignment before touching a device."""
+    L = capi.lib()
+    assert L.sdb_oa_log2_slots(0) == 4
+    assert L.sdb_oa_log2_slots(8) == 4
+    assert L.sdb_oa_log2_slots(9) == 5
+    assert L.sdb_oa_log2_slots(1 << 20) == 21
+    assert L.sdb_oa_log2_slots((1 << 30) + 1) == capi.SDB_ERR_INVALID
+    assert L.sdb_probe_semi_oa(None, None, None, 0, None, 0, 1, 10, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_probe_semi_oa(None, None, None, 0, None, 32, 1, 10, None) == capi.SDB_ERR_INVALID
+    assert L.sdb_probe_semi_oa(None, None, None, 0, None, 8, 10, 1, None) == capi.SDB_ERR_INVALID  # empty range
+    assert L.sdb_probe_full_oa(None, None, None, None, 0, None, 8, -(1 << 31), (1 << 31) - 1, None) == \
+        capi.SDB_ERR_INVALID  # 2^32 keys
+    assert L.sdb_probe_full_oa(None, None, None, None, 0, 0x1004, 8, 1, 10, None) == capi.SDB_ERR_INVALID  # align
+    assert L.sdb_ht_build_kv_oa(None, None, None, 0, 0x1000, 8, 1, 10, 1, None) == capi.SDB_OK
+    d = _star_desc()
+    d.ops[1].ht_log2 = 40
+    assert L.sdb_chain_registers(ctypes.byref(d)) == capi.SDB_ERR_INVALID
+    d.ops[1].ht_log2 = 12
+    assert L.sdb_chain_registers(ctypes.byref(d)) == 2
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 0  # open-addressing probes: the general pass
