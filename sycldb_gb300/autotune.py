@@ -49,13 +49,17 @@ DEFAULT_TABLE = os.path.join(HERE, "tuning", "gb300.json")
 VARIANTS = (0, 1, 2, 3, 4, 5, 6, 7, 8)
 TERMINALS = {"flags": 0, "sum": 1, "groupby": 2}
 
-OP_SEARCH_RANGE, OP_SEMI_PROBE = 1, 3  # SDB_OP_* kinds of a chain's first op
+OP_SEARCH_RANGE, OP_SEMI_PROBE, OP_FULL_PROBE = 1, 3, 4  # SDB_OP_* kinds of a chain's first op
 
 # benchmark plan shapes: (name, terminal, registers, first op, fact columns, plan builder)
 SHAPES = [
     ("filter_sum", "sum", 1, OP_SEARCH_RANGE, ssb.QUERY_COLUMNS["q1"], lambda: plans.plan_filter_sum(1994)),
     ("date_join", "groupby", 2, OP_SEARCH_RANGE, ssb.QUERY_COLUMNS["q2"], lambda: plans.plan_date_join(1994)),
     ("star", "groupby", 2, OP_SEMI_PROBE, ssb.QUERY_COLUMNS["star"], lambda: plans.plan_star(2, 11)),
+    # three full probes (the fused pass tests the supplier table's bitmap first;
+    # the tuning key is the chain as the executor hands it over)
+    ("flight3", "groupby", 3, OP_FULL_PROBE, ssb.QUERY_COLUMNS["flight3"],
+     lambda: plans.plan_customer_supplier_date(2)),
 ]
 
 
@@ -148,7 +152,7 @@ def tune(sizes: Iterable[int] = (1 << 20, 1 << 22, 1 << 24, 1 << 26, 120_000_000
         torch.cuda.synchronize()
         with Engine(fuse=True, profile=True) as eng:
             eng.load_table("lineorder", fact)
-            for t in ("supplier", "part", "ddate"):
+            for t in ("supplier", "customer", "part", "ddate"):
                 eng.load_table(t, dims[t])
             for name, term, nregs, first_op, _, build in shapes:
                 plan = build()

@@ -803,6 +803,7 @@ struct Launch {
     uint32_t *occ;
     const uint8_t *bitmap_ht;  // semi-join table staged as a bitmap (NULL: none)
     uint32_t bitmap_len;       // its entries
+    int32_t bitmap_kv;         // 1: bitmap_ht is a key/value table (int2 entries, bit = x == 1)
     int32_t nregs;             // registers the chain uses (an instantiation needs NREGS >= nregs)
 };
 
@@ -868,6 +869,19 @@ struct FilterSumBind : Dyn {
     __host__ __device__ static constexpr int out(int i) { return i == 3 ? 0 : kAny; }
     __host__ __device__ static constexpr int value() { return breg(0); }
     __host__ __device__ static constexpr int n_keys() { return 0; }
+};
+
+// Three full probes with the smallest table pre-tested (SSB flight 3 after
+// prefilter_by_bitmap): bitmap test of slot 1; full(slot 0) -> r0;
+// full(slot 1) -> r1 again for its value; full(slot 2) -> r2; group by
+// (r0, r1, r2), sum slot 3.
+struct Flight3Bind : Dyn {
+    static constexpr bool bound = true;
+    __host__ __device__ static constexpr int a(int i) { return i == 1 ? bslot(0) : (i == 3 ? bslot(2) : bslot(1)); }
+    __host__ __device__ static constexpr int out(int i) { return i == 0 ? kAny : i - 1; }
+    __host__ __device__ static constexpr int value() { return bslot(3); }
+    __host__ __device__ static constexpr int n_keys() { return 3; }
+    __host__ __device__ static constexpr int key(int q) { return q < 3 ? breg(q) : kAny; }
 };
 
 // Slots op i of a bound shape reads.
@@ -1291,6 +1305,25 @@ __device__ __forceinline__ void stage_bitmap(const Launch &L, uint32_t *s_bits)
 {
     if (!L.bitmap_ht) return;
     const uint32_t words = (L.bitmap_len + 31) / 32;
+    if (L.bitmap_kv) {  // a key/value table: entry j's occupancy word x == 1
+        const int4 *q = reinterpret_cast<const int4 *>(L.bitmap_ht);  // two entries per int4
+        for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
+            uint32_t bits = 0;
+            const uint32_t e0 = w * 32;
+            if (e0 + 32 <= L.bitmap_len) {
+#pragma unroll
+                for (int j = 0; j < 16; j++) {
+                    const int4 v = __ldg(q + e0 / 2 + j);
+                    bits |= ((uint32_t)(v.x == 1) | ((uint32_t)(v.z == 1) << 1)) << (2 * j);
+                }
+            } else {
+                const int2 *e = reinterpret_cast<const int2 *>(L.bitmap_ht);
+                for (uint32_t j = 0; j < 32 && e0 + j < L.bitmap_len; j++) bits |= (uint32_t)(e[e0 + j].x == 1) << j;
+            }
+            s_bits[w] = bits;
+        }
+        return;
+    }
     for (uint32_t w = threadIdx.x; w < words; w += blockDim.x) {
         uint32_t bits = 0;
         const uint32_t e0 = w * 32;
@@ -1899,6 +1932,52 @@ inline uint32_t op_slots(const Op &o)
     return slot_bit(o.a) | (uses_b ? slot_bit(o.b) : 0u);
 }
 
+// Chains of two or three full probes (a star join whose dimensions all give
+// values, e.g. SSB flight 3): the probe whose table is the smallest (at most
+// kBitmapMax entries, 16-byte aligned) is first tested against a
+// shared-memory bitmap of its table's occupancy, the other probes run on the
+// rows that pass, and the tested probe runs again right after the first of
+// them, for its value (a hit, by the test).  The same rows survive and every
+// register gets the same value, so results do not change; the probes of the
+// rows the bitmap rejects are skipped, and the first op becomes a bitmap test
+// the passes can compact after.
+void prefilter_by_bitmap(Launch &D, int terminal)
+{
+    if (terminal == SDB_TERM_FLAGS || D.flags_out || D.bitmap_ht || D.n_ops < 2 || D.n_ops > 3) return;
+    int j = -1;
+    uint64_t best = ~0ull;
+    for (int i = 0; i < D.n_ops; i++) {
+        const Op &o = D.ops[i];
+        if (o.kind != SDB_OP_FULL_PROBE || o.out_col || o.a.src != 0) return;
+        const uint64_t len = (uint64_t)((int64_t)o.hi - (int64_t)o.lo + 1);
+        if (len >= 1 && len <= kBitmapMax && sdb::aligned(o.ht, 16) && len < best) {
+            best = len;
+            j = i;
+        }
+    }
+    if (j < 0) return;
+    Op ops[kMaxOps];
+    int n = 0;
+    ops[n] = D.ops[j];
+    ops[n].kind = SDB_OP_SEMI_PROBE;
+    ops[n].smem_bits = 1;
+    n++;
+    bool again = false;
+    for (int i = 0; i < D.n_ops; i++) {
+        if (i == j) continue;
+        ops[n++] = D.ops[i];
+        if (!again) {
+            ops[n++] = D.ops[j];
+            again = true;
+        }
+    }
+    for (int i = 0; i < n; i++) D.ops[i] = ops[i];
+    D.n_ops = n;
+    D.bitmap_ht = static_cast<const uint8_t *>(D.ops[0].ht);
+    D.bitmap_len = (uint32_t)best;
+    D.bitmap_kv = 1;
+}
+
 // Converts a checked chain into a dense launch.  Returns false when the chain
 // reads more than kSlots distinct columns, has too many ops or registers.
 bool convert(const ChainLaunch &C, int nregs, Launch &D)
@@ -1967,9 +2046,10 @@ bool convert(const ChainLaunch &C, int nregs, Launch &D)
     D.P = c.P;
     D.out_sum = c.out_sum;
     D.occ = c.occ;
+    prefilter_by_bitmap(D, c.terminal);
     // slots a row still needs after the first op
     D.tail_slots = 0;
-    for (int k = 1; k < c.n_ops; k++) D.tail_slots |= op_slots(D.ops[k]);
+    for (int k = 1; k < D.n_ops; k++) D.tail_slots |= op_slots(D.ops[k]);
     if (c.terminal != SDB_TERM_FLAGS) D.tail_slots |= slot_bit(D.value);
     for (int j = 0; j < D.n_keys; j++) D.tail_slots |= slot_bit(D.keys[j]);
     D.late_slots = 0;
@@ -2083,7 +2163,20 @@ int with_shape(const Launch &D, int term, int compact, F &f, bool bind = false)
     // full + full -> group-by
     if (r2 && term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
         return f.template run<Dyn, T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
-    // three full probes -> three-key group-by (SSB flight 3: customer, supplier, date)
+    // three full probes, the smallest table pre-tested by its bitmap
+    // (prefilter_by_bitmap) -> three-key group-by (SSB flight 3)
+    if (D.nregs <= 4 && term == T_GROUP && n == 4 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_FULL_PROBE &&
+        k[2] == SDB_OP_FULL_PROBE && k[3] == SDB_OP_FULL_PROBE) {
+        if (c1 && bind &&
+            bound_ok<Flight3Bind, T_GROUP, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>(D))
+            return f.template run<Flight3Bind, T_GROUP, 4, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE,
+                                  SDB_OP_FULL_PROBE>();
+        return c1 ? f.template run<Dyn, T_GROUP, 4, 1, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE,
+                                   SDB_OP_FULL_PROBE>()
+                  : f.template run<Dyn, T_GROUP, 4, 5, SDB_OP_SEMI_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE,
+                                   SDB_OP_FULL_PROBE>();
+    }
+    // three full probes -> three-key group-by (none of the tables small enough for a bitmap)
     if (D.nregs <= 4 && term == T_GROUP && n == 3 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE &&
         k[2] == SDB_OP_FULL_PROBE)
         return f.template run<Dyn, T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();

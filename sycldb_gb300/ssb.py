@@ -59,6 +59,7 @@ QUERY_COLUMNS = {
     "q1": (5, 8, 9, 11),        # filter-project-sum
     "q2": (5, 9, 11),           # filter + date join + group-by
     "star": (3, 4, 5, 12),      # three-way star join
+    "flight3": (2, 4, 5, 12),   # customer, supplier, date joins -> three-key group-by
 }
 
 

@@ -295,14 +295,44 @@ def _filter_sum_desc():
     return d
 
 
+def _flight3_desc():
+    """SSB flight 3 as the fuser emits it: full probes on custkey (-> r0),
+    suppkey (-> r1) and orderdate (-> r2); group by (r0, r1, r2) summing
+    revenue.  The supplier table is the smallest."""
+    d = capi.ChainDesc()
+    d.n = 1 << 20
+    d.n_ops = 3
+    for i, (col, lo, hi, ht) in enumerate(((0x10000000, 1, 600000, 0x1000000), (0x20000000, 1, 40000, 0x2000000),
+                                           (0x30000000, 19920101, 19981230, 0x3000000))):
+        o = d.ops[i]
+        o.kind, o.lo, o.hi, o.ht, o.out_reg = capi.OP_FULL_PROBE, lo, hi, ht, i
+        _col(o.a, col)
+    d.terminal = capi.TERM_GROUPBY
+    _col(d.value, 0x40000000)
+    d.n_keys = 3
+    for q in range(3):
+        _reg(d.keys[q], q)
+        d.key_min[q], d.key_max[q] = 0, 30
+        d.out_keys[q] = 0x500000 + 0x10000 * q
+    d.P, d.out_sum, d.occ = 31 * 31 * 31, 0x600000, 0x700000
+    return d
+
+
 def test_hot_shapes_take_their_bound_pass():
     """The star join, date join and filter-project-sum chains in the form
     the fuser emits map to their bound pass (2); an operand elsewhere (the
     star's group keys swapped, a column in place of the select's literal)
     keeps the shape's run-time-bound pass (1)."""
     L = capi.lib()
-    for d in (_star_desc(), _date_join_desc(), _filter_sum_desc()):
+    for d in (_star_desc(), _date_join_desc(), _filter_sum_desc(), _flight3_desc()):
         assert L.sdb_chain_specialised(ctypes.byref(d)) == 2
+    d = _flight3_desc()  # every table too large for a bitmap: no pre-test, no compaction
+    d.ops[1].hi = 1 << 20
+    d.ops[2].lo, d.ops[2].hi = 0, 1 << 20
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
+    d = _flight3_desc()  # the supplier table 8-byte aligned only: no bitmap from it, the date table instead
+    d.ops[1].ht = 0x2000008
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
     d = _star_desc(keys=(0, 1))
     assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
     d = _filter_sum_desc()
