@@ -738,7 +738,7 @@ struct Fuser {
     static bool split(const sdb_chain_desc &c, uint8_t *scratch, sdb_chain_desc &a, sdb_chain_desc &b)
     {
         if ((c.terminal != SDB_TERM_SUM && c.terminal != SDB_TERM_GROUPBY) || !scratch) return false;
-        if (columns(c) <= 4 || sdb_chain_specialised(&c) == 1) return false;
+        if (columns(c) <= 4 || sdb_chain_specialised(&c) >= 1) return false;
         sdb_chain_desc A = c, B = c;
         A.n_ops = B.n_ops = 0;
         for (int k = 0; k < c.n_ops; k++) {
@@ -756,7 +756,7 @@ struct Fuser {
         A.terminal = SDB_TERM_FLAGS;
         A.flags_out = scratch;
         B.flags_in = scratch;
-        if (sdb_chain_specialised(&A) != 1 || sdb_chain_specialised(&B) != 1) return false;
+        if (sdb_chain_specialised(&A) < 1 || sdb_chain_specialised(&B) < 1) return false;
         a = A;
         b = B;
         return true;
