@@ -12,6 +12,7 @@
 #pragma once
 
 #include <cctype>
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <cstdlib>
@@ -47,6 +48,9 @@ struct range {
 template <int D = 1>
 struct item {
     size_t v;
+    item() : v(0) {}
+    item(size_t x) : v(x) {}
+    item(id<D> x) : v(x.v) {}
     operator size_t() const { return v; }
     size_t operator[](int) const { return v; }
     size_t get_id(int) const { return v; }
@@ -55,32 +59,73 @@ struct item {
 struct event {
     void wait() {}
     void wait_and_throw() {}
+    static void wait(const std::vector<event> &) {}
+    static void wait_and_throw(const std::vector<event> &) {}
     bool operator==(const event &) const { return true; }
     bool operator!=(const event &) const { return false; }
     template <typename T>
     uint64_t get_profiling_info() const { return 0; }
 };
 
-enum class backend { host = 0, ocl = 1, omp = 2, cuda = 3, hip = 4, level_zero = 5 };
+enum class backend { host = 0, ocl = 1, omp = 2, cuda = 3, hip = 4, level_zero = 5, ext_oneapi_cuda = 3,
+                     ext_oneapi_hip = 4, ext_oneapi_level_zero = 5 };
 
+struct platform;
+
+// Device and platform queries: each info descriptor names the type it returns.
 namespace info {
 namespace device {
-struct name {};
-struct global_mem_size {};
+struct name { using return_type = std::string; };
+struct vendor { using return_type = std::string; };
+struct global_mem_size { using return_type = uint64_t; };
+struct max_compute_units { using return_type = uint32_t; };
+struct platform { using return_type = sycl::platform; };
 }  // namespace device
+namespace platform {
+struct name { using return_type = std::string; };
+}  // namespace platform
 namespace event_profiling {
 struct command_start {};
 struct command_end {};
 }  // namespace event_profiling
 }  // namespace info
 
+struct platform {
+    template <typename T>
+    typename T::return_type get_info() const { return "host-shim"; }
+};
+
+// One device: the host, on which every work-item runs in turn.
 struct device {
     template <typename T>
-    std::string get_info() const { return "host-shim"; }
+    typename T::return_type get_info() const
+    {
+        using R = typename T::return_type;
+        if constexpr (std::is_same_v<R, std::string>) return "host-shim";
+        else if constexpr (std::is_same_v<R, uint64_t>) return (uint64_t)1 << 34;
+        else if constexpr (std::is_same_v<R, uint32_t>) return 1u;
+        else return R{};
+    }
     backend get_backend() const { return backend::host; }
     bool is_gpu() const { return false; }
     bool is_cpu() const { return true; }
     bool is_host() const { return true; }
+    static std::vector<device> get_devices() { return {device{}}; }
+};
+
+struct default_selector_t {};
+inline constexpr default_selector_t default_selector_v{};
+
+namespace property {
+namespace queue {
+struct in_order {};
+struct enable_profiling {};
+}  // namespace queue
+}  // namespace property
+
+struct property_list {
+    template <typename... P>
+    property_list(P...) {}
 };
 
 template <typename T = void>
@@ -147,7 +192,12 @@ public:
     void parallel_for(range<1> r, reduction_desc<T, Op> red, K k)
     {
         reducer<T> rd{red.init_identity ? T(0) : *red.ptr};
-        for (size_t i = 0; i < r.size(); i++) k(id<1>(i), rd);
+        for (size_t i = 0; i < r.size(); i++) {
+            if constexpr (std::is_invocable_v<K &, id<1>, reducer<T> &>)
+                k(id<1>(i), rd);
+            else
+                k(item<1>(i), rd);
+        }
         *red.ptr = rd.acc;
     }
 
@@ -173,6 +223,12 @@ private:
 
 class queue {
 public:
+    queue() = default;
+    queue(default_selector_t) {}
+    queue(const device &) {}
+    template <typename P>
+    queue(const device &, const P &) {}
+    void wait_and_throw() {}
     template <typename F>
     event submit(F f)
     {
@@ -186,6 +242,28 @@ public:
         for (size_t i = 0; i < n; i++) p[i] = v;
         return event{};
     }
+    template <typename T, typename Deps>
+    event fill(T *p, const T &v, size_t n, const Deps &)
+    {
+        return fill(p, v, n);
+    }
+    template <typename Name = void, typename K>
+    event single_task(K k)
+    {
+        k();
+        return event{};
+    }
+    template <typename Name = void, typename Deps, typename K>
+    event single_task(const Deps &, K k)
+    {
+        k();
+        return event{};
+    }
+    template <typename K>
+    event parallel_for(range<1> r, K k)
+    {
+        return submit([&](handler &h) { h.parallel_for(r, k); });
+    }
     event memset(void *p, int v, size_t n)
     {
         std::memset(p, v, n);
@@ -195,6 +273,16 @@ public:
     {
         std::memcpy(d, s, n);
         return event{};
+    }
+    template <typename Deps>
+    event memcpy(void *d, const void *s, size_t n, const Deps &)
+    {
+        return memcpy(d, s, n);
+    }
+    template <typename T>
+    event copy(const T *s, T *d, size_t n)
+    {
+        return memcpy(d, s, n * sizeof(T));
     }
     void wait() {}
     device get_device() const { return device{}; }
