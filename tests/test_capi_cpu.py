@@ -252,7 +252,7 @@ def _date_join_desc():
     d.n = 1 << 20
     d.n_ops = 3
     o = d.ops[0]
-    o.kind, o.lo, o.hi, o.logic_op = capi.OP_SEARCH_RANGE, 4, 6, capi.AND
+    o.kind, o.lo, o.hi, o.logic_op = capi.OP_SEARCH_RANGE, 4, 6, capi.NONE  # the fuser's first op
     _col(o.a, 0x10000000)
     o = d.ops[1]
     o.kind, o.lo, o.hi, o.ht, o.out_reg = capi.OP_FULL_PROBE, 19920101, 19981230, 0x300000, 0
