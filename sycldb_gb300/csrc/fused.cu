@@ -756,7 +756,9 @@ namespace dense {
 // lo <= a <= hi (empty when lo > hi).
 __device__ __forceinline__ bool in_range(int32_t a, int32_t lo, int32_t hi) { return a >= lo && a <= hi; }
 
-constexpr int kItems = 4;
+constexpr int kItems = 4;       // rows per thread per tile
+constexpr int kQ = kItems / 4;  // 16-byte copies per thread, slot and tile
+static_assert(kItems % 4 == 0 && kItems <= 8, "tile rows per thread: 4 or 8");
 constexpr int kSlots = 4;
 // Slots per ring stage: CARRY 3 stages only its first two slots (the late
 // ones, renumbered last, are not staged) and spends the space on more stages.
@@ -914,9 +916,9 @@ __host__ __device__ constexpr uint32_t bound_late()
     return bound_tail<B, TERM, KS...>() & ~e;
 }
 
-// Tile rows are staged in shared memory by cp.async: thread t's four rows
-// (tile + 4t .. 4t + 3) of every chain column arrive as one 16-byte copy per
-// column into a ring of STAGES (2 or 3) stages, issued STAGES - 1 tiles
+// Tile rows are staged in shared memory by cp.async: thread t's kItems rows
+// (tile + kItems t ..) of every chain column arrive as kItems / 4 16-byte
+// copies per column into a ring of STAGES stages, issued STAGES - 1 tiles
 // ahead.  Each thread reads back only what it copied, so no block barrier is
 // needed.
 
@@ -933,7 +935,7 @@ template <int NREGS>
 struct State {
     int32_t reg[NREGS][kItems];
     const uint32_t *bits;  // shared-memory bitmap of the staged semi-join table
-    const int4 *stage;  // this thread's copies of the current tile: stage[slot * kThreads]
+    const int4 *stage;  // this thread's copies of the current tile: stage[slot * kThreads * kQ + q]
     uint64_t base;      // row of item 0 (items are base .. base + 3)
     uint32_t valid, live;
 };
@@ -942,8 +944,11 @@ template <int NREGS>
 __device__ __forceinline__ void fetch4(const Src &s, const State<NREGS> &S, int32_t (&v)[kItems])
 {
     if (s.src == 0) {
-        const int4 q = S.stage[s.idx * kThreads];
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+#pragma unroll
+        for (int q = 0; q < kQ; q++) {
+            const int4 x = S.stage[s.idx * kThreads * kQ + q];
+            v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+        }
     } else if (s.src == 1) {
 #pragma unroll
         for (int k = 0; k < kItems; k++) v[k] = S.reg[0][k];
@@ -978,8 +983,11 @@ __device__ __forceinline__ void fetch4c(const Src &s, const State<NREGS> &S, int
     if constexpr (C == kAny) {
         fetch4(s, S, v);
     } else if constexpr (C < 8) {
-        const int4 q = S.stage[C * kThreads];
-        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+#pragma unroll
+        for (int q = 0; q < kQ; q++) {
+            const int4 x = S.stage[C * kThreads * kQ + q];
+            v[4 * q] = x.x; v[4 * q + 1] = x.y; v[4 * q + 2] = x.z; v[4 * q + 3] = x.w;
+        }
     } else if constexpr (C < kLitCode) {
         static_assert(C - 8 < NREGS, "bound register outside the instantiation");
 #pragma unroll
@@ -1107,8 +1115,8 @@ template <int NREGS>
 struct Row {
     static constexpr int kRegs = NREGS;
     int32_t reg[NREGS];
-    const int32_t *wstage;  // the warp's 128 staged rows of slot 0 (slot s at + s * 4 * kThreads)
-    uint32_t r;             // row within the warp's 128
+    const int32_t *wstage;  // the warp's 32 x kItems staged rows of slot 0 (slot s at + s * kItems * kThreads)
+    uint32_t r;             // row within the warp's 32 x kItems
     uint64_t grow;          // global row
     bool live;
 };
@@ -1140,7 +1148,7 @@ __device__ __forceinline__ int32_t fetch1(const Src &s, const VRow<NREGS> &R)
 template <int NREGS>
 __device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
 {
-    if (s.src == 0) return R.wstage[s.idx * 4 * kThreads + R.r];
+    if (s.src == 0) return R.wstage[s.idx * kItems * kThreads + R.r];
     if (s.src == 1) {
         int32_t v = R.reg[0];
 #pragma unroll
@@ -1173,7 +1181,7 @@ __device__ __forceinline__ int32_t fetch1c(const Src &s, const Row<NREGS> &R)
     if constexpr (C == kAny) {
         return fetch1(s, R);
     } else if constexpr (C < 8) {
-        return R.wstage[C * 4 * kThreads + R.r];
+        return R.wstage[C * kItems * kThreads + R.r];
     } else if constexpr (C < kLitCode) {
         static_assert(C - 8 < NREGS, "bound register outside the instantiation");
         return R.reg[C - 8];
@@ -1350,12 +1358,17 @@ __device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nstag
                                            uint64_t tile)
 {
     const uint64_t r0 = tile + (uint64_t)kItems * threadIdx.x;
-    if (r0 < n) {
-        const uint64_t left = n - r0;
-        const uint32_t bytes = left >= kItems ? 16u : (uint32_t)(left * 4);
 #pragma unroll
-        for (int sl = 0; sl < SS; sl++)
-            if (sl < nstaged) cp_async16(&s_buf[(st * SS + sl) * kThreads + threadIdx.x], slot[sl] + r0, bytes);
+    for (int q = 0; q < kQ; q++) {
+        const uint64_t r = r0 + 4 * q;
+        if (r < n) {
+            const uint64_t left = n - r;
+            const uint32_t bytes = left >= 4 ? 16u : (uint32_t)(left * 4);
+#pragma unroll
+            for (int sl = 0; sl < SS; sl++)
+                if (sl < nstaged)
+                    cp_async16(&s_buf[((st * SS + sl) * kThreads + threadIdx.x) * kQ + q], slot[sl] + r, bytes);
+        }
     }
     cp_async_commit();
 }
@@ -1557,11 +1570,11 @@ __device__ __forceinline__ int32_t tail_value(const Launch &L, const int32_t *ws
         constexpr uint32_t late = CARRY == 3 ? bound_late<B, TERM, SPLIT, KS...>() : 0u;
         if constexpr (!((tail >> SL) & 1u)) return 0;
         else if constexpr ((late >> SL) & 1u) return (int32_t)(uint32_t)(row0 + r);
-        else return ws[SL * 4 * kThreads + r];
+        else return ws[SL * kItems * kThreads + r];
     } else {
         if (!((L.tail_slots >> SL) & 1u)) return 0;
         if (CARRY == 3 && ((L.late_slots >> SL) & 1u)) return (int32_t)(uint32_t)(row0 + r);
-        return ws[SL * 4 * kThreads + r];
+        return ws[SL * kItems * kThreads + r];
     }
 }
 
@@ -1576,7 +1589,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
     constexpr int kDenseOps = kCompact ? SPLIT : N;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     constexpr int SS = stage_slots<CARRY>();
-    S.stage = &s_buf[st * SS * kThreads + threadIdx.x];
+    S.stage = &s_buf[(st * SS * kThreads + threadIdx.x) * kQ];
     S.base = tile + (uint64_t)kItems * threadIdx.x;
     if (S.base + kItems <= L.n) {
         S.valid = (1u << kItems) - 1u;
@@ -1612,7 +1625,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
         for (int k = 0; k < kItems; k++)
             if ((S.live >> k) & 1u) list[pos++] = (uint8_t)(lane * kItems + k);
         __syncwarp();
-        const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[st * SS * kThreads + warp * 32]);
+        const int32_t *ws = reinterpret_cast<const int32_t *>(&s_buf[(st * SS * kThreads + warp * 32) * kQ]);
         if constexpr (CARRY > 0) {
             // entries 0 .. carry-1 are the carried rows (entry j in lane j),
             // then this tile's survivors
@@ -1683,7 +1696,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             // missing rows are read and not used
             int32_t v[kItems];
             fetch4(L.value, S, v);
-            uint32_t h[kItems] = {0, 0, 0, 0};
+            uint32_t h[kItems] = {};
 #pragma unroll
             for (int kk = 0; kk < SDB_CHAIN_MAX_KEYS; kk++)
                 if (kk < L.n_keys) {
@@ -1736,10 +1749,10 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr int SS = stage_slots<CARRY>();
-    extern __shared__ int4 s_buf[];  // [kStages][SS][kThreads], then the semi-join bitmap
+    extern __shared__ int4 s_buf[];  // [kStages][SS][kThreads][kQ], then the semi-join bitmap
     __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
     __shared__ unsigned long long s_sum[TERM == T_GROUP ? kDenseCap : 1];
-    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 128 row offsets
+    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // per warp: 32 x kItems row offsets
     __shared__ uint64_t s_part[kThreads / 32];
     __shared__ uint8_t s_l2src[CARRY >= 2 ? kThreads : 1];
     uint32_t carry = 0;  // rows the warp carries (warp-uniform)
@@ -1747,7 +1760,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
     Level2<NREGS> Q;
     Q.src = s_l2src + (CARRY >= 2 ? (threadIdx.x & ~31u) : 0u);
     const bool direct = L.P <= kDenseCap;
-    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads);
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads * kQ);
     group_table_reset<TERM>(s_key, s_sum);
     stage_bitmap(L, s_bits);
     if (TERM == T_GROUP || L.bitmap_ht) __syncthreads();
@@ -1815,7 +1828,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
     __shared__ Launch s_L;
     __shared__ uint32_t s_next;
     constexpr int SS = stage_slots<CARRY>();
-    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads);
+    uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads * kQ);
 
     State<NREGS> S;
     S.bits = s_bits;
@@ -1881,7 +1894,7 @@ template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int...
 int launch_stages(const Launch &L, cudaStream_t s)
 {
     auto kern = k_dense<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
-    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (int)sizeof(int4);
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * kQ * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
     static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
@@ -2325,7 +2338,7 @@ int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, ui
                  cudaStream_t s)
 {
     auto kern = k_batch<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
-    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (int)sizeof(int4);
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * kQ * (int)sizeof(int4);
     const int smem = ring + (int)(bitmap_words * 4);
     static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
