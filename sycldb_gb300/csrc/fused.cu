@@ -756,9 +756,12 @@ namespace dense {
 // lo <= a <= hi (empty when lo > hi).
 __device__ __forceinline__ bool in_range(int32_t a, int32_t lo, int32_t hi) { return a >= lo && a <= hi; }
 
-constexpr int kItems = 4;       // rows per thread per tile
-constexpr int kQ = kItems / 4;  // 16-byte copies per thread, slot and tile
-static_assert(kItems % 4 == 0 && kItems <= 8, "tile rows per thread: 4 or 8");
+constexpr int kItems = 4;  // rows per thread per tile of the passes without late slots
+// Rows per thread per tile: CARRY 3 (late slots, two staged columns) takes 8
+// -- the same shared memory per stage as four columns of 4 rows -- the others
+// 4.  A thread copies items / 4 16-byte pieces per staged column and tile.
+template <int CARRY>
+__host__ __device__ constexpr int items_of() { return CARRY == 3 ? 8 : kItems; }
 constexpr int kSlots = 4;
 // Slots per ring stage: CARRY 3 stages only its first two slots (the late
 // ones, renumbered last, are not staged) and spends the space on more stages.
@@ -931,18 +934,20 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-template <int NREGS>
+template <int NREGS, int IT = kItems>
 struct State {
-    int32_t reg[NREGS][kItems];
+    static constexpr int kIt = IT;
+    int32_t reg[NREGS][IT];
     const uint32_t *bits;  // shared-memory bitmap of the staged semi-join table
-    const int4 *stage;  // this thread's copies of the current tile: stage[slot * kThreads * kQ + q]
-    uint64_t base;      // row of item 0 (items are base .. base + 3)
+    const int4 *stage;  // this thread's copies of the current tile: stage[slot * kThreads * IT / 4 + q]
+    uint64_t base;      // row of item 0 (items are base .. base + IT - 1)
     uint32_t valid, live;
 };
 
-template <int NREGS>
-__device__ __forceinline__ void fetch4(const Src &s, const State<NREGS> &S, int32_t (&v)[kItems])
+template <int NREGS, int IT>
+__device__ __forceinline__ void fetch4(const Src &s, const State<NREGS, IT> &S, int32_t (&v)[IT])
 {
+    constexpr int kItems = IT, kQ = IT / 4;
     if (s.src == 0) {
 #pragma unroll
         for (int q = 0; q < kQ; q++) {
@@ -964,9 +969,10 @@ __device__ __forceinline__ void fetch4(const Src &s, const State<NREGS> &S, int3
     }
 }
 
-template <int NREGS>
-__device__ __forceinline__ void set_regs(State<NREGS> &S, int r, const int32_t (&v)[kItems], uint32_t mask)
+template <int NREGS, int IT>
+__device__ __forceinline__ void set_regs(State<NREGS, IT> &S, int r, const int32_t (&v)[IT], uint32_t mask)
 {
+    constexpr int kItems = IT;
 #pragma unroll
     for (int i = 0; i < NREGS; i++)
         if (r == i) {
@@ -977,9 +983,10 @@ __device__ __forceinline__ void set_regs(State<NREGS> &S, int r, const int32_t (
 }
 
 // fetch4 / set_regs with the operand's binding code C (kAny: at run time).
-template <int C, int NREGS>
-__device__ __forceinline__ void fetch4c(const Src &s, const State<NREGS> &S, int32_t (&v)[kItems])
+template <int C, int NREGS, int IT>
+__device__ __forceinline__ void fetch4c(const Src &s, const State<NREGS, IT> &S, int32_t (&v)[IT])
 {
+    constexpr int kItems = IT, kQ = IT / 4;
     if constexpr (C == kAny) {
         fetch4(s, S, v);
     } else if constexpr (C < 8) {
@@ -998,9 +1005,10 @@ __device__ __forceinline__ void fetch4c(const Src &s, const State<NREGS> &S, int
     }
 }
 
-template <int OUT, int NREGS>
-__device__ __forceinline__ void set_regs_c(State<NREGS> &S, int r, const int32_t (&v)[kItems], uint32_t mask)
+template <int OUT, int NREGS, int IT>
+__device__ __forceinline__ void set_regs_c(State<NREGS, IT> &S, int r, const int32_t (&v)[IT], uint32_t mask)
 {
+    constexpr int kItems = IT;
     if constexpr (OUT == kAny) {
         set_regs(S, r, v, mask);
     } else {
@@ -1011,16 +1019,19 @@ __device__ __forceinline__ void set_regs_c(State<NREGS> &S, int r, const int32_t
     }
 }
 
-__device__ __forceinline__ void store4(int32_t *col, uint64_t base, const int32_t (&v)[kItems], uint32_t mask)
+template <int IT>
+__device__ __forceinline__ void store4(int32_t *col, uint64_t base, const int32_t (&v)[IT], uint32_t mask)
 {
+    constexpr int kItems = IT;
 #pragma unroll
     for (int k = 0; k < kItems; k++)
         if ((mask >> k) & 1u) col[base + k] = v[k];
 }
 
-template <int K, int NREGS, int A, int BB, int OUT>
-__device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
+template <int K, int A, int BB, int OUT, int NREGS, int IT>
+__device__ __forceinline__ void step(const Op &op, State<NREGS, IT> &S)
 {
+    constexpr int kItems = IT;
     int32_t a[kItems], b[kItems];
     if (K == SDB_OP_SELECT || K == SDB_OP_SEARCH_RANGE || K == SDB_OP_SEARCH_POINTS) {
         const bool and_op = op.logic == SDB_AND;
@@ -1100,18 +1111,18 @@ __device__ __forceinline__ void step(const Op &op, State<NREGS> &S)
     }
 }
 
-template <class B, int NREGS, int BEGIN, int... KS, int... IS>
-__device__ __forceinline__ void run_steps(const Launch &L, State<NREGS> &S, std::integer_sequence<int, IS...>)
+template <class B, int NREGS, int BEGIN, int... KS, int IT, int... IS>
+__device__ __forceinline__ void run_steps(const Launch &L, State<NREGS, IT> &S, std::integer_sequence<int, IS...>)
 {
     constexpr int kinds[] = {KS...};
-    (step<kinds[BEGIN + IS], NREGS, B::a(BEGIN + IS), B::b(BEGIN + IS), B::out(BEGIN + IS)>(L.ops[BEGIN + IS], S), ...);
+    (step<kinds[BEGIN + IS], B::a(BEGIN + IS), B::b(BEGIN + IS), B::out(BEGIN + IS)>(L.ops[BEGIN + IS], S), ...);
 }
 
 // Sparse phase: after op SPLIT - 1 each warp compacts its surviving rows
 // (ballot-free: a warp prefix sum of the lanes' live-bit counts) into a
 // shared-memory list, and the remaining ops run one row per lane over that
 // dense list instead of over mostly-dead 4-row groups.
-template <int NREGS>
+template <int NREGS, int IT = kItems>
 struct Row {
     static constexpr int kRegs = NREGS;
     int32_t reg[NREGS];
@@ -1145,10 +1156,10 @@ __device__ __forceinline__ int32_t fetch1(const Src &s, const VRow<NREGS> &R)
     return s.lit;
 }
 
-template <int NREGS>
-__device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS> &R)
+template <int NREGS, int IT>
+__device__ __forceinline__ int32_t fetch1(const Src &s, const Row<NREGS, IT> &R)
 {
-    if (s.src == 0) return R.wstage[s.idx * kItems * kThreads + R.r];
+    if (s.src == 0) return R.wstage[s.idx * IT * kThreads + R.r];
     if (s.src == 1) {
         int32_t v = R.reg[0];
 #pragma unroll
@@ -1175,13 +1186,13 @@ __device__ __forceinline__ int32_t fetch1c(const Src &s, const VRow<NREGS> &R)
     }
 }
 
-template <int C, int NREGS>
-__device__ __forceinline__ int32_t fetch1c(const Src &s, const Row<NREGS> &R)
+template <int C, int NREGS, int IT>
+__device__ __forceinline__ int32_t fetch1c(const Src &s, const Row<NREGS, IT> &R)
 {
     if constexpr (C == kAny) {
         return fetch1(s, R);
     } else if constexpr (C < 8) {
-        return R.wstage[C * kItems * kThreads + R.r];
+        return R.wstage[C * IT * kThreads + R.r];
     } else if constexpr (C < kLitCode) {
         static_assert(C - 8 < NREGS, "bound register outside the instantiation");
         return R.reg[C - 8];
@@ -1353,10 +1364,11 @@ __device__ __forceinline__ void stage_bitmap(const Launch &L, uint32_t *s_bits)
 // tile + 4t .. +3) into ring stage `st` (SS slots per stage); rows past the
 // end are zero-filled or skipped.  Always commits one group (possibly empty) so every thread
 // counts groups the same way.
-template <int STAGES, int SS>
+template <int STAGES, int SS, int IT>
 __device__ __forceinline__ void issue_tile(const int32_t *const *slot, int nstaged, uint64_t n, int4 *s_buf, int st,
                                            uint64_t tile)
 {
+    constexpr int kItems = IT, kQ = IT / 4;
     const uint64_t r0 = tile + (uint64_t)kItems * threadIdx.x;
 #pragma unroll
     for (int q = 0; q < kQ; q++) {
@@ -1570,16 +1582,17 @@ __device__ __forceinline__ int32_t tail_value(const Launch &L, const int32_t *ws
         constexpr uint32_t late = CARRY == 3 ? bound_late<B, TERM, SPLIT, KS...>() : 0u;
         if constexpr (!((tail >> SL) & 1u)) return 0;
         else if constexpr ((late >> SL) & 1u) return (int32_t)(uint32_t)(row0 + r);
-        else return ws[SL * kItems * kThreads + r];
+        else return ws[SL * items_of<CARRY>() * kThreads + r];
     } else {
         if (!((L.tail_slots >> SL) & 1u)) return 0;
         if (CARRY == 3 && ((L.late_slots >> SL) & 1u)) return (int32_t)(uint32_t)(row0 + r);
-        return ws[SL * kItems * kThreads + r];
+        return ws[SL * items_of<CARRY>() * kThreads + r];
     }
 }
 
 template <int TERM, class B, int NREGS, int SPLIT, int CARRY, int... KS>
-__device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, const int4 *s_buf, int st, uint64_t tile,
+__device__ __forceinline__ void tile_body(const Launch &L, State<NREGS, items_of<CARRY>()> &S, const int4 *s_buf, int st,
+                                          uint64_t tile,
                                           uint8_t *s_list, uint32_t *s_key, unsigned long long *s_sum,
                                           const uint32_t *s_bits, bool direct, uint64_t &acc, uint32_t &carry,
                                           int4 &ce, Level2<NREGS> &Q)
@@ -1587,6 +1600,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
     constexpr int N = sizeof...(KS);
     constexpr bool kCompact = SPLIT <= N;
     constexpr int kDenseOps = kCompact ? SPLIT : N;
+    constexpr int kItems = items_of<CARRY>(), kQ = kItems / 4;
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     constexpr int SS = stage_slots<CARRY>();
     S.stage = &s_buf[(st * SS * kThreads + threadIdx.x) * kQ];
@@ -1667,7 +1681,7 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS> &S, cons
             carry = rem;
             __syncwarp();
         } else {
-            Row<NREGS> R;
+            Row<NREGS, kItems> R;
             R.wstage = ws;
             for (uint32_t b = 0; b < total; b += 32) {
                 const uint32_t idx = b + lane;
@@ -1748,6 +1762,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
 {
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    constexpr int kItems = items_of<CARRY>(), kQ = kItems / 4;
     constexpr int SS = stage_slots<CARRY>();
     extern __shared__ int4 s_buf[];  // [kStages][SS][kThreads][kQ], then the semi-join bitmap
     __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
@@ -1767,7 +1782,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
     const uint64_t stride = (uint64_t)gridDim.x * kTile;
 
-    State<NREGS> S;
+    State<NREGS, kItems> S;
     S.bits = s_bits;
 #pragma unroll
     for (int r = 0; r < NREGS; r++)
@@ -1777,10 +1792,10 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
 
     uint64_t tile = (uint64_t)blockIdx.x * kTile;
 #pragma unroll
-    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages, SS>(L.slot, L.nstaged, L.n, s_buf, p, tile + p * stride);
+    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages, SS, kItems>(L.slot, L.nstaged, L.n, s_buf, p, tile + p * stride);
     int st = 0;
     for (; tile < L.n; tile += stride) {
-        issue_tile<kStages, SS>(L.slot, L.nstaged, L.n, s_buf, (st + kStages - 1) % kStages,
+        issue_tile<kStages, SS, kItems>(L.slot, L.nstaged, L.n, s_buf, (st + kStages - 1) % kStages,
                                 tile + (kStages - 1) * stride);
         cp_async_wait<kStages - 1>();
         tile_body<TERM, B, NREGS, SPLIT, CARRY, KS...>(L, S, s_buf, st, tile, s_list, s_key, s_sum, s_bits, direct, acc,
@@ -1819,6 +1834,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
     Q.src = s_l2src + (CARRY >= 2 ? (threadIdx.x & ~31u) : 0u);
     constexpr int kStages = STAGES;
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    constexpr int kItems = items_of<CARRY>(), kQ = kItems / 4;
     constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
     extern __shared__ int4 s_buf[];
     __shared__ uint32_t s_key[TERM == T_GROUP ? kDenseCap : 1];
@@ -1830,7 +1846,7 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
     constexpr int SS = stage_slots<CARRY>();
     uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads * kQ);
 
-    State<NREGS> S;
+    State<NREGS, kItems> S;
     S.bits = s_bits;
 #pragma unroll
     for (int r = 0; r < NREGS; r++)
@@ -1863,14 +1879,14 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>())
 #pragma unroll
         for (int p = 0; p < kStages - 1; p++) {
             const uint32_t t = span.t0 + p;
-            if (t < span.t1) issue_tile<kStages, SS>(s_L.slot, s_L.nstaged, n, s_buf, p, (uint64_t)t * kTile);
+            if (t < span.t1) issue_tile<kStages, SS, kItems>(s_L.slot, s_L.nstaged, n, s_buf, p, (uint64_t)t * kTile);
             else cp_async_commit();
         }
         int st = 0;
         for (uint32_t t = span.t0; t < span.t1; t++) {
             const uint32_t tn = t + kStages - 1;
             if (tn < span.t1)
-                issue_tile<kStages, SS>(s_L.slot, s_L.nstaged, n, s_buf, (st + kStages - 1) % kStages,
+                issue_tile<kStages, SS, kItems>(s_L.slot, s_L.nstaged, n, s_buf, (st + kStages - 1) % kStages,
                                         (uint64_t)tn * kTile);
             else cp_async_commit();
             cp_async_wait<kStages - 1>();
@@ -1894,7 +1910,7 @@ template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int...
 int launch_stages(const Launch &L, cudaStream_t s)
 {
     auto kern = k_dense<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
-    const int ring = STAGES * stage_slots<CARRY>() * kThreads * kQ * (int)sizeof(int4);
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (items_of<CARRY>() / 4) * (int)sizeof(int4);
     const int smem = ring + (L.bitmap_ht ? (int)(((L.bitmap_len + 31) / 32) * 4) : 0);
     static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
@@ -1904,7 +1920,7 @@ int launch_stages(const Launch &L, cudaStream_t s)
     int per_sm = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
         per_sm = 1;
-    const uint64_t tile = (uint64_t)kThreads * kItems;
+    const uint64_t tile = (uint64_t)kThreads * items_of<CARRY>();
     uint64_t blocks = (L.n + tile - 1) / tile;
     const uint64_t cap = (uint64_t)num_sms() * per_sm;
     if (blocks > cap) blocks = cap;
@@ -1917,8 +1933,8 @@ int launch_stages(const Launch &L, cudaStream_t s)
 
 // Ring stages 3 or 2; rows carried between tiles (carry 1; 2: and the second
 // compaction level) only with compaction and a 2-stage ring; carry 3 (as 2,
-// and late slots) with a 4-stage ring of two slots, for a launch that
-// prepare_late accepted.
+// and late slots) with a 2-stage ring of two slots and 8-row tiles per thread,
+// for a launch that prepare_late accepted.
 template <class B, int TERM, int NREGS, int SPLIT, int... KS>
 int launch(const Launch &L, int stages, int carry, cudaStream_t s)
 {
@@ -1926,9 +1942,9 @@ int launch(const Launch &L, int stages, int carry, cudaStream_t s)
     constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
     if constexpr (B::bound) {  // bound passes are carry-3 passes (with_shape binds only those)
         static_assert(kLate, "a bound shape needs the second level");
-        return launch_stages<B, TERM, NREGS, 4, SPLIT, 3, KS...>(L, s);
+        return launch_stages<B, TERM, NREGS, 2, SPLIT, 3, KS...>(L, s);
     } else {
-        if (kLate && carry == 3) return launch_stages<Dyn, TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(L, s);
+        if (kLate && carry == 3) return launch_stages<Dyn, TERM, NREGS, 2, SPLIT, kLate ? 3 : 0, KS...>(L, s);
         if (stages >= 3) return launch_stages<Dyn, TERM, NREGS, 3, SPLIT, 0, KS...>(L, s);
         if (kCompact && carry >= 2) return launch_stages<Dyn, TERM, NREGS, 2, SPLIT, kCompact ? 2 : 0, KS...>(L, s);
         if (kCompact && carry == 1) return launch_stages<Dyn, TERM, NREGS, 2, SPLIT, kCompact ? 1 : 0, KS...>(L, s);
@@ -2338,7 +2354,7 @@ int batch_stages(const Launch *launches, const Span *spans, uint32_t n_spans, ui
                  cudaStream_t s)
 {
     auto kern = k_batch<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
-    const int ring = STAGES * stage_slots<CARRY>() * kThreads * kQ * (int)sizeof(int4);
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (items_of<CARRY>() / 4) * (int)sizeof(int4);
     const int smem = ring + (int)(bitmap_words * 4);
     static const bool attr = [&] {  // once per instantiation, thread-safe
         cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + (int)(kBitmapMax / 8));
@@ -2373,10 +2389,10 @@ struct BatchLauncher {
         constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
         if constexpr (B::bound) {  // bound passes are carry-3 passes
             static_assert(kLate, "a bound shape needs the second level");
-            return batch_stages<B, TERM, NREGS, 4, SPLIT, 3, KS...>(launches, spans, n_spans, head, bitmap_words, s);
+            return batch_stages<B, TERM, NREGS, 2, SPLIT, 3, KS...>(launches, spans, n_spans, head, bitmap_words, s);
         } else {
             if (kLate && carry == 3)
-                return batch_stages<Dyn, TERM, NREGS, 4, SPLIT, kLate ? 3 : 0, KS...>(launches, spans, n_spans, head,
+                return batch_stages<Dyn, TERM, NREGS, 2, SPLIT, kLate ? 3 : 0, KS...>(launches, spans, n_spans, head,
                                                                                     bitmap_words, s);
             if (stages >= 3)
                 return batch_stages<Dyn, TERM, NREGS, 3, SPLIT, 0, KS...>(launches, spans, n_spans, head,
@@ -2452,7 +2468,7 @@ constexpr int kLevel2Variant = 7;    // as 6, plus a second compaction after the
 constexpr int kLateVariant = 8;      // as 7, the columns read only after the second compaction loaded per row
 constexpr int kMaxVariant = 8;
 
-int variant_stages(int v) { return v == kLateVariant ? 4 : ((v == kCompact2Variant || v >= kCarryVariant) ? 2 : 3); }
+int variant_stages(int v) { return (v == kCompact2Variant || v >= kCarryVariant) ? 2 : 3; }
 int variant_carry(int v)
 {
     return v == kLateVariant ? 3 : (v == kLevel2Variant ? 2 : (v == kCarryVariant ? 1 : 0));
@@ -2808,18 +2824,24 @@ int plan_batch(const sdb_chain_desc *chains, int n_chains, BatchPlan &bp)
         BatchPlan::G &G = groups[g];
         for (const Item &it : of[g]->items) {
             if (G.carry && !dense::can_carry(it.D, G.term)) G.carry = 0;  // every chain of the launch must allow it
-            const uint32_t c = (uint32_t)G.launches.size();
             G.launches.push_back(it.D);
             if (G.carry == 3 && !dense::prepare_late(G.launches.back(), G.term)) {
                 G.carry = 2;  // as variant 7
                 G.stages = 2;
             }
             if (it.D.bitmap_ht) G.bitmap_words = std::max<uint32_t>(G.bitmap_words, (it.D.bitmap_len + 31) / 32);
-            for (uint64_t t = 0; t < it.tiles; t += S)
-                G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + S, it.tiles), 0});
         }
         if (G.carry != 3)  // chains readied for carry 3 before the group fell back
             for (dense::Launch &x : G.launches) dense::run_all_staged(x);
+        // spans in the launch's tiles (carry 3: 8 rows per thread, spans of half
+        // as many tiles)
+        const uint64_t tile = (uint64_t)kThreads * (G.carry == 3 ? dense::items_of<3>() : dense::kItems);
+        const uint64_t span = G.carry == 3 ? std::max<uint64_t>(S / 2, 1) : S;
+        for (uint32_t c = 0; c < (uint32_t)G.launches.size(); c++) {
+            const uint64_t tiles = (G.launches[c].n + tile - 1) / tile;
+            for (uint64_t t = 0; t < tiles; t += span)
+                G.spans.push_back({c, (uint32_t)t, (uint32_t)std::min<uint64_t>(t + span, tiles), 0});
+        }
         G.bound = G.carry == 3;
         for (const dense::Launch &x : G.launches) {
             dense::BoundProbe p;
