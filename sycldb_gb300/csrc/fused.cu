@@ -889,6 +889,19 @@ struct Flight3Bind : Dyn {
     __host__ __device__ static constexpr int key(int q) { return q < 3 ? breg(q) : kAny; }
 };
 
+// Flight 4's second pass (its semi joins run first into the incoming flags):
+// full(slot 0) -> r0; full(slot 1) -> r1; r2 = slot 2 op slot 3; group by
+// (r1, r0), sum r2.
+struct Flight4Bind : Dyn {
+    static constexpr bool bound = true;
+    __host__ __device__ static constexpr int a(int i) { return bslot(i); }
+    __host__ __device__ static constexpr int b(int i) { return i == 2 ? bslot(3) : kAny; }
+    __host__ __device__ static constexpr int out(int i) { return i; }
+    __host__ __device__ static constexpr int value() { return breg(2); }
+    __host__ __device__ static constexpr int n_keys() { return 2; }
+    __host__ __device__ static constexpr int key(int q) { return q == 0 ? breg(1) : (q == 1 ? breg(0) : kAny); }
+};
+
 // Slots op i of a bound shape reads.
 template <class B, int... KS>
 __host__ __device__ constexpr uint32_t bound_op_bits(int i)
@@ -901,12 +914,14 @@ __host__ __device__ constexpr uint32_t bound_op_bits(int i)
 }
 
 // The tail and late slot masks of a bound shape (what convert and
-// late_slots_of compute from the launch).
-template <class B, int TERM, int... KS>
+// late_slots_of compute from the launch): the tail is what a compacted row
+// keeps -- the slots the ops after the first read (from the first on when
+// the rows are compacted on their incoming flags, SPLIT 0).
+template <class B, int TERM, int SPLIT, int... KS>
 __host__ __device__ constexpr uint32_t bound_tail()
 {
     uint32_t m = 0;
-    for (int i = 1; i < (int)sizeof...(KS); i++) m |= bound_op_bits<B, KS...>(i);
+    for (int i = SPLIT == 0 ? 0 : 1; i < (int)sizeof...(KS); i++) m |= bound_op_bits<B, KS...>(i);
     if (TERM != T_FLAGS) m |= code_bit(B::value());
     for (int q = 0; q < B::n_keys(); q++) m |= code_bit(B::key(q));
     return m;
@@ -916,7 +931,7 @@ __host__ __device__ constexpr uint32_t bound_late()
 {
     uint32_t e = 0;
     for (int i = 0; i <= SPLIT && i < (int)sizeof...(KS); i++) e |= bound_op_bits<B, KS...>(i);
-    return bound_tail<B, TERM, KS...>() & ~e;
+    return bound_tail<B, TERM, SPLIT, KS...>() & ~e;
 }
 
 // Tile rows are staged in shared memory by cp.async: thread t's kItems rows
@@ -1578,7 +1593,7 @@ template <int CARRY, class B, int TERM, int SPLIT, int SL, int... KS>
 __device__ __forceinline__ int32_t tail_value(const Launch &L, const int32_t *ws, uint32_t r, uint64_t row0)
 {
     if constexpr (B::bound) {
-        constexpr uint32_t tail = bound_tail<B, TERM, KS...>();
+        constexpr uint32_t tail = bound_tail<B, TERM, SPLIT, KS...>();
         constexpr uint32_t late = CARRY == 3 ? bound_late<B, TERM, SPLIT, KS...>() : 0u;
         if constexpr (!((tail >> SL) & 1u)) return 0;
         else if constexpr ((late >> SL) & 1u) return (int32_t)(uint32_t)(row0 + r);
@@ -1614,9 +1629,15 @@ __device__ __forceinline__ void tile_body(const Launch &L, State<NREGS, items_of
     }
     if (L.flags_in && S.valid) {
         uint32_t m = 0;
+        if (kItems == 8 && S.valid == 0xffu && sdb::aligned(L.flags_in, 8)) {  // 8 flags in one load
+            const uint64_t f = *reinterpret_cast<const uint64_t *>(L.flags_in + S.base);
 #pragma unroll
-        for (int k = 0; k < kItems; k++)
-            if ((S.valid >> k) & 1u) m |= (uint32_t)(L.flags_in[S.base + k] != 0) << k;
+            for (int k = 0; k < 8; k++) m |= (uint32_t)(((f >> (8 * k)) & 0xffu) != 0) << k;
+        } else {
+#pragma unroll
+            for (int k = 0; k < kItems; k++)
+                if ((S.valid >> k) & 1u) m |= (uint32_t)(L.flags_in[S.base + k] != 0) << k;
+        }
         S.live = m;
     } else {
         S.live = S.valid;
@@ -1940,7 +1961,7 @@ int launch(const Launch &L, int stages, int carry, cudaStream_t s)
 {
     constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
     constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
-    if constexpr (B::bound) {  // bound passes are carry-3 passes (with_shape binds only those)
+    if constexpr (B::bound || SPLIT == 0) {  // bound and SPLIT-0 passes are carry-3 passes
         static_assert(kLate, "a bound shape needs the second level");
         return launch_stages<B, TERM, NREGS, 2, SPLIT, 3, KS...>(L, s);
     } else {
@@ -2104,7 +2125,7 @@ uint32_t late_slots_of(const Launch &D)
 // selection, no literal fill); ops before the split produce no register.
 bool can_compact(const Launch &D, int term, int split)
 {
-    if (term == T_FLAGS || D.flags_out || split < 1 || split > D.n_ops) return false;
+    if (term == T_FLAGS || D.flags_out || split < 0 || split > D.n_ops) return false;
     for (int i = 0; i < D.n_ops; i++) {
         const Op &o = D.ops[i];
         const bool makes_reg = o.kind == SDB_OP_FULL_PROBE || o.kind == SDB_OP_BINOP || o.kind == SDB_OP_FILL;
@@ -2120,14 +2141,17 @@ bool can_compact(const Launch &D, int term, int split)
 }
 
 // Whether compacted rows can be carried from one tile to the next: besides
-// compaction after the first op, no op after it writes a column (a carried
-// row keeps its slot values, not its row number).
+// compaction after the first op (or, with incoming flags, before it), no op
+// after it writes a column (a carried row keeps its slot values, not its row
+// number).
 bool can_carry(const Launch &D, int term)
 {
-    if (!can_compact(D, term, 1)) return false;
     for (int i = 1; i < D.n_ops; i++)
         if (D.ops[i].out_col) return false;
-    return true;
+    if (can_compact(D, term, 1)) return true;
+    // or compaction on the incoming flags, before the first op (which then
+    // writes no column either)
+    return D.flags_in && !D.ops[0].out_col && can_compact(D, term, 0);
 }
 
 // Whether D's operands are exactly binding B's (and the slot masks the bound
@@ -2156,7 +2180,7 @@ bool bound_ok(const Launch &D)
     }
     constexpr uint32_t late = bound_late<B, TERM, SPLIT, KS...>();
     const uint32_t all = (1u << D.nslot) - 1u, staged = (1u << D.nstaged) - 1u;
-    return D.tail_slots == bound_tail<B, TERM, KS...>() && D.late_slots == late && late == (all & ~staged);
+    return D.tail_slots == bound_tail<B, TERM, SPLIT, KS...>() && D.late_slots == late && late == (all & ~staged);
 }
 
 // Calls f.run<B, TERM, NREGS, SPLIT, KS...>() for the instantiation that
@@ -2185,10 +2209,18 @@ int with_shape(const Launch &D, int term, int compact, F &f, bool bind = false)
     // two semi probes -> flags (the flag-only front of a chain split in two)
     if (r2 && term == T_FLAGS && n == 2 && k[0] == SDB_OP_SEMI_PROBE && k[1] == SDB_OP_SEMI_PROBE)
         return f.template run<Dyn, T_FLAGS, 2, 3, SDB_OP_SEMI_PROBE, SDB_OP_SEMI_PROBE>();
-    // full + full + projection -> group-by (SSB flight 4 after its semi joins)
+    // full + full + projection -> group-by (SSB flight 4 after its semi joins);
+    // under carry 3 (bind), with incoming flags, the rows are compacted on
+    // those flags before the first probe (SPLIT 0)
     if (D.nregs <= 4 && term == T_GROUP && n == 3 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE &&
-        k[2] == SDB_OP_BINOP)
+        k[2] == SDB_OP_BINOP) {
+        if (bind && compact && D.flags_in && can_compact(D, term, 0)) {
+            if (bound_ok<Flight4Bind, T_GROUP, 0, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>(D))
+                return f.template run<Flight4Bind, T_GROUP, 4, 0, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+            return f.template run<Dyn, T_GROUP, 4, 0, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+        }
         return f.template run<Dyn, T_GROUP, 4, 4, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE, SDB_OP_BINOP>();
+    }
     // full + full -> group-by
     if (r2 && term == T_GROUP && n == 2 && k[0] == SDB_OP_FULL_PROBE && k[1] == SDB_OP_FULL_PROBE)
         return f.template run<Dyn, T_GROUP, 2, 3, SDB_OP_FULL_PROBE, SDB_OP_FULL_PROBE>();
@@ -2242,6 +2274,7 @@ struct LateProbe {
     int run()
     {
         constexpr bool kLate = SPLIT <= (int)sizeof...(KS) && use_level2<SPLIT, KS...>(3);
+        if (SPLIT == 0 && kLate) D.tail_slots |= op_slots(D.ops[0]);  // rows compacted before the first op
         D.late_slots = kLate ? late_slots_of<SPLIT>(D) : 0u;
         return SDB_OK;
     }
@@ -2251,7 +2284,7 @@ struct LateProbe {
 void set_late_slots(Launch &D, int term)
 {
     LateProbe p{D};
-    if (with_shape(D, term, 1, p) != SDB_OK) D.late_slots = 0;
+    if (with_shape(D, term, 1, p, true) != SDB_OK) D.late_slots = 0;
 }
 
 // Readies D for carry 3: finds its late slots and renumbers the slots so the
@@ -2387,7 +2420,7 @@ struct BatchLauncher {
     {
         constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
         constexpr bool kLate = kCompact && use_level2<SPLIT, KS...>(3);
-        if constexpr (B::bound) {  // bound passes are carry-3 passes
+        if constexpr (B::bound || SPLIT == 0) {  // bound and SPLIT-0 passes are carry-3 passes
             static_assert(kLate, "a bound shape needs the second level");
             return batch_stages<B, TERM, NREGS, 2, SPLIT, 3, KS...>(launches, spans, n_spans, head, bitmap_words, s);
         } else {

@@ -318,14 +318,46 @@ def _flight3_desc():
     return d
 
 
+def _flight4b_desc():
+    """Flight 4's second pass as the fuser's split emits it: the rows that
+    passed the supplier and part semi joins arrive as flags; full probes on
+    custkey (-> r0) and orderdate (-> r1); r2 = revenue - supplycost; group
+    by (r1, r0) summing r2."""
+    d = capi.ChainDesc()
+    d.n = 1 << 20
+    d.flags_in = 0x800000
+    d.n_ops = 3
+    for i, (col, lo, hi, ht) in enumerate(((0x10000000, 1, 600000, 0x1000000),
+                                           (0x20000000, 19920101, 19981230, 0x3000000))):
+        o = d.ops[i]
+        o.kind, o.lo, o.hi, o.ht, o.out_reg = capi.OP_FULL_PROBE, lo, hi, ht, i
+        _col(o.a, col)
+    o = d.ops[2]
+    o.kind, o.bin_op, o.out_reg = capi.OP_BINOP, capi.SUB, 2
+    _col(o.a, 0x30000000)
+    _col(o.b, 0x40000000)
+    d.terminal = capi.TERM_GROUPBY
+    _reg(d.value, 2)
+    d.n_keys = 2
+    for q, r in enumerate((1, 0)):
+        _reg(d.keys[q], r)
+        d.key_min[q], d.key_max[q] = 0, 30
+        d.out_keys[q] = 0x500000 + 0x10000 * q
+    d.P, d.out_sum, d.occ = 31 * 31, 0x600000, 0x700000
+    return d
+
+
 def test_hot_shapes_take_their_bound_pass():
     """The star join, date join and filter-project-sum chains in the form
     the fuser emits map to their bound pass (2); an operand elsewhere (the
     star's group keys swapped, a column in place of the select's literal)
     keeps the shape's run-time-bound pass (1)."""
     L = capi.lib()
-    for d in (_star_desc(), _date_join_desc(), _filter_sum_desc(), _flight3_desc()):
+    for d in (_star_desc(), _date_join_desc(), _filter_sum_desc(), _flight3_desc(), _flight4b_desc()):
         assert L.sdb_chain_specialised(ctypes.byref(d)) == 2
+    d = _flight4b_desc()  # without incoming flags nothing to compact on before the first probe
+    d.flags_in = 0
+    assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
     d = _flight3_desc()  # every table too large for a bitmap: no pre-test, no compaction
     d.ops[1].hi = 1 << 20
     d.ops[2].lo, d.ops[2].hi = 0, 1 << 20

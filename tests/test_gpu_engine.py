@@ -187,7 +187,7 @@ def test_variant_8_runs_the_hot_shapes_bound():
     ds = datasets.dataset(0.05)
     pls = [plans.plan_star(2, 11), plans.plan_date_join(1995), plans.plan_filter_sum(1994),
            plans.plan_star(1, 3, 1993, 1996, 12), plans.plan_customer_supplier_date(2),
-           plans.plan_customer_supplier_date(0, 1993, 1997, (3, 17))]
+           plans.plan_customer_supplier_date(0, 1993, 1997, (3, 17)), plans.plan_profit(1), plans.plan_profit(3, (2, 4))]
     try:
         with Engine(arena_bytes=1 << 30, fuse=True) as eng:
             capi.force_chain_variant(8)
