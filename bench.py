@@ -1026,7 +1026,10 @@ def run_served(args, rank, world, local, pg, stream):
             "served": {"qps": nreq / swall, "p50_ms": _pct(slat, 50), "p99_ms": _pct(slat, 99),
                        "batches": st["batches"] - st0["batches"],
                        "mean_batch": (st["batched_plans"] - st0["batched_plans"]) / max(1, st["batches"] - st0["batches"]),
-                       "max_inflight_plans": st["max_inflight_plans"], "peak_device_bytes": st["peak_device_bytes"]},
+                       "max_inflight_plans": st["max_inflight_plans"], "peak_device_bytes": st["peak_device_bytes"],
+                       "dispatcher_ms_per_request": {
+                           "sizing": (st["sizing_us"] - st0["sizing_us"]) / 1e3 / max(1, nreq),
+                           "record_and_enqueue": (st["launch_us"] - st0["launch_us"]) / 1e3 / max(1, nreq)}},
             "plain": {"qps": nreq / pwall, "p50_ms": _pct(plat, 50), "p99_ms": _pct(plat, 99)},
             "bit_exact": exact,
         })

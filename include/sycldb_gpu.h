@@ -674,6 +674,8 @@ typedef struct sdb_server_stats {
     uint64_t peak_pinned_bytes;
     uint64_t budget_bytes;
     uint64_t direct_plans;             /* requests run at once through the plain path (idle server) */
+    uint64_t sizing_us;                /* dispatcher host time in sizing passes (microseconds) */
+    uint64_t launch_us;                /* dispatcher host time recording and enqueueing batches */
 } sdb_server_stats;
 
 int sdb_server_create(sdb_engine *eng, const sdb_server_config *cfg, sdb_server **out);

@@ -80,7 +80,8 @@ class ServerConfig(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(f, c_uint64) for f in ("submitted", "completed", "failed", "batches", "batched_plans",
                                         "max_batch_plans", "max_inflight_plans", "peak_device_bytes",
-                                        "peak_pinned_bytes", "budget_bytes", "direct_plans")]
+                                        "peak_pinned_bytes", "budget_bytes", "direct_plans", "sizing_us",
+                                        "launch_us")]
 
 
 SDB_BATCH_EAGER = 1

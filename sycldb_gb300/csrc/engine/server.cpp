@@ -186,6 +186,17 @@ struct sdb_server {
 
     bool size_request(Request &r)
     {
+        const auto t0 = Clock::now();
+        struct Tally {  // the pass's host time, however it ends
+            Clock::time_point t0;
+            sdb_server *s;
+            ~Tally()
+            {
+                const auto us = std::chrono::duration_cast<std::chrono::microseconds>(Clock::now() - t0).count();
+                std::lock_guard<std::mutex> g(s->mu);
+                s->st.sizing_us += (uint64_t)us;
+            }
+        } tally{t0, this};
         try {
             r.size = sdb::batch_size(eng, {r.plan});
             r.dev_need = RegionPool::round(r.size.arena) + RegionPool::round(r.size.zero) +
@@ -254,8 +265,15 @@ struct sdb_server {
             s.pin_bytes = pin_bytes;
             s.reqs.assign(std::make_move_iterator(waiting.begin()), std::make_move_iterator(waiting.begin() + k));
             waiting.erase(waiting.begin(), waiting.begin() + k);
+            const auto t_launch = Clock::now();
             try {
                 s.batch = sdb::batch_launch_external(eng, plans, z, dev + doff, dev_bytes, pinned + poff, pin_bytes, s.ss);
+                {
+                    const auto us =
+                        std::chrono::duration_cast<std::chrono::microseconds>(Clock::now() - t_launch).count();
+                    std::lock_guard<std::mutex> g(mu);
+                    st.launch_us += (uint64_t)us;
+                }
                 cudaError_t e = cudaEventRecord(s.done, s.ss.main);
                 if (e != cudaSuccess) throw sdb::Error(SDB_ERR_CUDA, cudaGetErrorString(e));
             } catch (const std::exception &x) {
