@@ -6,8 +6,9 @@
 * ``oracle/_ref/libsdb_ref.so``: the reference's own kernel headers
   (kernels/*.hpp and kernels/types.cpp of the SYCLDB repository), compiled
   where they lie against the host SYCL shim in ``oracle/ref_shim``.  Built
-  only when the reference checkout is present (``SYCLDB_REFERENCE`` or
-  /root/reference); it is a checker for the restatement, never a product path.
+  only when the reference checkout is present (``SYCLDB_REFERENCE``, else a
+  ``reference`` directory beside the repository's own); it is a checker for
+  the restatement, never a product path.
 * ``oracle/_ref/libsdb_ref_exec.so`` and ``libsdb_ref_exec_seg4096.so``: the
   reference's own executor (executor/, operations/preprocessing.cpp and
   memory_manager.cpp, runtime/runtime.cpp, models/*.hpp through them,
@@ -29,7 +30,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("SYCLDB_REFERENCE", "/root/reference")
+# The SYCLDB checkout: SYCLDB_REFERENCE, else <parent of the repository>/reference.
+REFERENCE = os.environ.get("SYCLDB_REFERENCE") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 
 def _newer(out: str, srcs) -> bool:

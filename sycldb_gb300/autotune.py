@@ -21,7 +21,10 @@ the unfused path) take a tuned launch shape instead: threads per block
 kernel and log2 rows bucket (``sdb_op_tune_set``; ``op_entries`` of the
 table).  The join tables are direct-address (the reference's HASH is the
 identity on its range, kernels/join.hpp:11-15), so there is no load factor
-to pick, and the shared-memory group table of the specialised passes has a
+to pick; the open-addressing tables taken for sparse key ranges have a fixed
+sizing rule (the smallest power of two at least twice the build rows, load
+at most 0.5), chosen with the engine's ``join_tables`` option rather than
+tuned; and the shared-memory group table of the specialised passes has a
 fixed 512-slot capacity.  The tuner times every
 variant on the plan shapes of the benchmark at several fact sizes, picks the
 fastest per tuning key -- (terminal, register class, kind of the chain's
@@ -70,8 +73,10 @@ def rows_bucket(n: int) -> int:
 
 OP_BLOCKS = (128, 256, 512)
 OP_PER_SM = (2, 4, 8, 16)
-LOAD_FACTOR_NOTE = ("no load-factor axis: every join table is direct-address over its key range "
-                    "(kernels/join.hpp:11-15), so its size is fixed by the build column's min/max")
+LOAD_FACTOR_NOTE = ("no load-factor axis: the join tables are direct-address over their key range "
+                    "(kernels/join.hpp:11-15), so their size is fixed by the build column's min/max; "
+                    "the open-addressing tables of sparse key ranges take the smallest power of two "
+                    "at least twice the build rows (load at most 0.5), a fixed rule")
 
 
 def load_ops(table: dict) -> int:
