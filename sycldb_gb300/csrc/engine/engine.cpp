@@ -1689,7 +1689,7 @@ struct sdb_batch {
     cudaStream_t bs = nullptr;              // the stream a run goes on
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join;
-    cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr, ev_in = nullptr;
+    cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr;
     // around the chain batch: before its builds, after them, before the
     // aggregating chains (after the plans' mid work), after them
     cudaEvent_t ev_c0 = nullptr, ev_cb = nullptr, ev_cm = nullptr, ev_c1 = nullptr;
@@ -1715,7 +1715,7 @@ struct sdb_batch {
         if (graph) cudaGraphDestroy(graph);
         for (auto s : side) cudaStreamDestroy(s);
         for (auto e : join) cudaEventDestroy(e);
-        for (auto e : {fork, ev_a, ev_b, ev_in, ev_c0, ev_cb, ev_cm, ev_c1})
+        for (auto e : {fork, ev_a, ev_b, ev_c0, ev_cb, ev_cm, ev_c1})
             if (e) cudaEventDestroy(e);
         if (bs) cudaStreamDestroy(bs);
         if (host) cudaFreeHost(host);
@@ -2471,7 +2471,6 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
         B.join.push_back(e);
     }
     SDB_CUDA(cudaEventCreateWithFlags(&B.fork, cudaEventDisableTiming));
-    SDB_CUDA(cudaEventCreateWithFlags(&B.ev_in, cudaEventDisableTiming));
     SDB_CUDA(cudaEventCreate(&B.ev_a));
     SDB_CUDA(cudaEventCreate(&B.ev_b));
     SDB_CUDA(cudaEventCreate(&B.ev_c0));
@@ -2501,18 +2500,19 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
 
 void batch_run(Engine &E, sdb_batch &B, sdb_result **out)
 {
-    SDB_CUDA(cudaEventRecord(B.ev_in, E.stream));
-    SDB_CUDA(cudaStreamWaitEvent(B.bs, B.ev_in, 0));
-    SDB_CUDA(cudaEventRecord(B.ev_a, B.bs));
+    // in the engine's own stream order (the graph was captured on B.bs; a
+    // graph launches into any stream), so no cross-stream event sits before it
+    cudaStream_t s = E.stream;
+    SDB_CUDA(cudaEventRecord(B.ev_a, s));
     if (B.exec) {
-        SDB_CUDA(cudaGraphLaunch(B.exec, B.bs));
+        SDB_CUDA(cudaGraphLaunch(B.exec, s));
     } else {
         const uint64_t l0 = sdb_launch_count();
-        replay(B, B.bs);
+        replay(B, s);
         B.kernels = (int)(sdb_launch_count() - l0);
     }
-    SDB_CUDA(cudaEventRecord(B.ev_b, B.bs));
-    SDB_CUDA(cudaStreamSynchronize(B.bs));
+    SDB_CUDA(cudaEventRecord(B.ev_b, s));
+    SDB_CUDA(cudaEventSynchronize(B.ev_b));
     float ms = 0;
     SDB_CUDA(cudaEventElapsedTime(&ms, B.ev_a, B.ev_b));
     B.last_ms = ms;

@@ -1797,11 +1797,17 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
     Q.src = s_l2src + (CARRY >= 2 ? (threadIdx.x & ~31u) : 0u);
     const bool direct = L.P <= kDenseCap;
     uint32_t *s_bits = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads * kQ);
+    constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
+    const uint64_t stride = (uint64_t)gridDim.x * kTile;
+    uint64_t tile = (uint64_t)blockIdx.x * kTile;
+    // the first tiles' copies go out before the group table and the bitmap
+    // are set up (the ring lies before the bitmap in shared memory), so
+    // their DRAM latency overlaps the bitmap's L2 reads
+#pragma unroll
+    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages, SS, kItems>(L.slot, L.nstaged, L.n, s_buf, p, tile + p * stride);
     group_table_reset<TERM>(s_key, s_sum);
     stage_bitmap(L, s_bits);
     if (TERM == T_GROUP || L.bitmap_ht) __syncthreads();
-    constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
-    const uint64_t stride = (uint64_t)gridDim.x * kTile;
 
     State<NREGS, kItems> S;
     S.bits = s_bits;
@@ -1811,9 +1817,6 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
         for (int k = 0; k < kItems; k++) S.reg[r][k] = 0;
     uint64_t acc = 0;
 
-    uint64_t tile = (uint64_t)blockIdx.x * kTile;
-#pragma unroll
-    for (int p = 0; p < kStages - 1; p++) issue_tile<kStages, SS, kItems>(L.slot, L.nstaged, L.n, s_buf, p, tile + p * stride);
     int st = 0;
     for (; tile < L.n; tile += stride) {
         issue_tile<kStages, SS, kItems>(L.slot, L.nstaged, L.n, s_buf, (st + kStages - 1) % kStages,

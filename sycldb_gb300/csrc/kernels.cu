@@ -765,6 +765,7 @@ __global__ void __launch_bounds__(kMaxBlock) k_gather(const T *src, const int32_
 // rows [t*per, (t+1)*per), counts its flagged rows, a block scan gives its
 // first output position, then it copies its rows' values in row order.
 constexpr uint32_t kSmallCompactMax = 65536;
+static_assert(kSmallCompactMax <= 1024u * 64u, "k_compact_gather_small keeps a thread's flags in a 64-bit mask");
 constexpr int kSmallCompactCols = 8;
 struct SmallCompact {
     const void *flags;  // uint8 flags, or uint32 occupancy words (flag = word != 0)
@@ -782,10 +783,19 @@ __global__ void __launch_bounds__(1024) k_compact_gather_small(const __grid_cons
     const F *flags = static_cast<const F *>(a.flags);
     __shared__ uint32_t s_warp[32];
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const uint32_t per = (a.n + 1023u) / 1024u;
+    const uint32_t per = (a.n + 1023u) / 1024u;  // at most 64: n <= kSmallCompactMax
     const uint32_t b = min(threadIdx.x * per, a.n), e = min(b + per, a.n);
-    uint32_t cnt = 0;
-    for (uint32_t i = b; i < e; i++) cnt += flags[i] != 0;
+    // the thread's run of flags as a bit mask, eight independent loads at a
+    // time (one latency per eight flags instead of one per flag)
+    uint64_t m = 0;
+    for (uint32_t j = b; j < e; j += 8) {
+        F f[8];
+#pragma unroll
+        for (int k = 0; k < 8; k++) f[k] = j + k < e ? flags[j + k] : F(0);
+#pragma unroll
+        for (int k = 0; k < 8; k++) m |= (uint64_t)(f[k] != 0) << (j - b + k);
+    }
+    const uint32_t cnt = __popcll(m);
     uint32_t x = cnt;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
@@ -806,15 +816,39 @@ __global__ void __launch_bounds__(1024) k_compact_gather_small(const __grid_cons
     __syncthreads();
     uint32_t pos = x - cnt + (warp ? s_warp[warp - 1] : 0);
     if (threadIdx.x == 1023) *a.count = pos + cnt;
-    for (uint32_t i = b; i < e; i++) {
-        if (!flags[i]) continue;
-        for (int c = 0; c < a.ncols; c++) {
-            if (a.wide[c])
-                static_cast<uint64_t *>(a.dst[c])[pos] = static_cast<const uint64_t *>(a.src[c])[i];
-            else
-                static_cast<int32_t *>(a.dst[c])[pos] = static_cast<const int32_t *>(a.src[c])[i];
+    // two live rows per round, every column of both loaded before any store
+    while (m) {
+        const uint32_t i0 = b + (uint32_t)__ffsll((long long)m) - 1u;
+        m &= m - 1;
+        const bool two = m != 0;
+        const uint32_t i1 = two ? b + (uint32_t)__ffsll((long long)m) - 1u : i0;
+        if (two) m &= m - 1;
+        uint64_t v0[kSmallCompactCols], v1[kSmallCompactCols];
+#pragma unroll
+        for (int c = 0; c < kSmallCompactCols; c++) {
+            if (c < a.ncols) {
+                if (a.wide[c]) {
+                    v0[c] = static_cast<const uint64_t *>(a.src[c])[i0];
+                    v1[c] = static_cast<const uint64_t *>(a.src[c])[i1];
+                } else {
+                    v0[c] = (uint32_t) static_cast<const int32_t *>(a.src[c])[i0];
+                    v1[c] = (uint32_t) static_cast<const int32_t *>(a.src[c])[i1];
+                }
+            }
         }
-        pos++;
+#pragma unroll
+        for (int c = 0; c < kSmallCompactCols; c++) {
+            if (c < a.ncols) {
+                if (a.wide[c]) {
+                    static_cast<uint64_t *>(a.dst[c])[pos] = v0[c];
+                    if (two) static_cast<uint64_t *>(a.dst[c])[pos + 1] = v1[c];
+                } else {
+                    static_cast<int32_t *>(a.dst[c])[pos] = (int32_t)(uint32_t)v0[c];
+                    if (two) static_cast<int32_t *>(a.dst[c])[pos + 1] = (int32_t)(uint32_t)v1[c];
+                }
+            }
+        }
+        pos += two ? 2u : 1u;
     }
 }
 
