@@ -26,9 +26,11 @@ to result rows in host memory.
   served     SF50 fact (300M rows x 17 columns) resident; a seeded Poisson
              stream of mixed plans (filter-sum, date join, star join, star join
              with year/brand windows) replayed open-loop through the request
-             server (continuous batching, 60 GB admission budget) and through
-             the plain one-at-a-time path: queries/s and p50/p99 latency per
-             arrival rate, results compared request by request
+             server (continuous batching, 60 GB admission budget, shared
+             scans: two plans' fact chains over the same rows in one paired
+             pass) and through the plain one-at-a-time path: queries/s and
+             p50/p99 latency per arrival rate, results compared request by
+             request
   widened    the SSB flight-3 and flight-4 shapes at SF20 (rows/s, fused-pass
              roofline), device ORDER BY throughput and the columnar loader
              (--no-widened skips it)
@@ -127,6 +129,8 @@ def parse_args():
     ap.add_argument("--served-rates", default="50,200,500,1000,2000",
                     help="Poisson arrival rates (queries/s) of the served form; empty skips it")
     ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival span per rate (at least 100 requests)")
+    ap.add_argument("--no-shared-scans", action="store_true",
+                    help="served form: every fact chain on its own (no paired passes)")
     return ap.parse_args()
 
 
@@ -988,7 +992,7 @@ def run_served(args, rank, world, local, pg, stream):
 
     sf = 50.0
     n = ssb.fact_rows(sf)
-    eng = Engine(fuse=True, stream=stream.cuda_stream)
+    eng = Engine(fuse=True, stream=stream.cuda_stream, shared_scans=not args.no_shared_scans)
     fact = ssb.gen_lineorder_device(n, range(17), sf, salt=rank)
     eng.load_table("lineorder", fact)
     for t, c in dims_host(sf).items():
@@ -1027,6 +1031,7 @@ def run_served(args, rank, world, local, pg, stream):
                        "batches": st["batches"] - st0["batches"],
                        "mean_batch": (st["batched_plans"] - st0["batched_plans"]) / max(1, st["batches"] - st0["batches"]),
                        "max_inflight_plans": st["max_inflight_plans"], "peak_device_bytes": st["peak_device_bytes"],
+                       "paired_chains": st["paired_chains"] - st0["paired_chains"],
                        "dispatcher_ms_per_request": {
                            "sizing": (st["sizing_us"] - st0["sizing_us"]) / 1e3 / max(1, nreq),
                            "record_and_enqueue": (st["launch_us"] - st0["launch_us"]) / 1e3 / max(1, nreq)}},
@@ -1041,7 +1046,9 @@ def run_served(args, rank, world, local, pg, stream):
                         "plan mix 1/4 each: filter-project-sum (one-year window, discount range, quantity bound), "
                         "filter + date join + group by year, star join, star join with year and brand windows" % n,
             "latency": "host wall clock from each request's scheduled arrival to its result on the host",
-            "budget_bytes": 60 << 30, "slots": 4, "rates": out, "clocks": clk}
+            "budget_bytes": 60 << 30, "slots": 4, "rates": out, "clocks": clk,
+            "shared_scans": "off" if args.no_shared_scans else
+            "on: two fact chains of one shape over the same rows run as one paired pass (paired_chains)"}
 
 
 def main():

@@ -409,6 +409,29 @@ int sdb_chain_registers(const sdb_chain_desc *chain);
  * negative status if it is invalid.  Host-only. */
 int sdb_chain_specialised(const sdb_chain_desc *chain);
 
+/* ------------------------------------------------------------ paired pass
+ * The shared scan of a batch: two aggregating chains that scan the same fact
+ * rows in one pass.  No counterpart in the reference, which runs each
+ * query's kernels on their own (models/execution.hpp:528-650,
+ * executor/ddor_executor.cpp:22-245); the results are those of calling
+ * sdb_fused_chain on each chain.  Two chains pair when the single-chain pass
+ * would run both as the same bound variant-8 instantiation of a served shape
+ * (star join, date join, filter-project-sum), with the same staged columns
+ * (the columns the pass copies into shared memory) over the same rows and no
+ * incoming or outgoing flags; their literals, tables, late columns and
+ * outputs are their own.  Each tile is then copied once and both chains run
+ * on it, each with its own group table and semi-join bitmap. */
+/* 1 when a and b can share one paired pass, else 0.  Host-only. */
+int sdb_chain_pairable(const sdb_chain_desc *a, const sdb_chain_desc *b);
+/* 1 and *key when c can take part in a paired pass, else 0: chains that can
+ * pair have equal keys (equal keys are then checked with
+ * sdb_chain_pairable), so a batch groups its chains in one pass over them.
+ * Host-only. */
+int sdb_chain_pair_key(const sdb_chain_desc *c, uint64_t *key);
+/* Runs a and b as one paired pass on `stream`; SDB_ERR_UNSUPPORTED (nothing
+ * launched) when they cannot pair. */
+int sdb_chain_launch_pair(const sdb_chain_desc *a, const sdb_chain_desc *b, sdb_stream_t stream);
+
 /* ------------------------------------------------------------ chain batches
  * Many fused chains in one persistent launch per chain shape.  No counterpart
  * in the reference, which runs one plan at a time (executor/ddor_executor.cpp:
@@ -492,6 +515,10 @@ typedef struct sdb_engine_config {
                                    range is sparse: at least 2^20 keys and 8 x the open-addressing
                                    slots (16 x the build rows); 1: always direct-address; 2: always
                                    open-addressing.  Results are the same either way. */
+    int32_t no_shared_scans;    /* 0: a batch (and a served batch) runs pairs of its plans' fact chains
+                                   that scan the same rows as one paired pass each
+                                   (sdb_chain_launch_pair); 1: every chain on its own.  Results are
+                                   the same either way. */
 } sdb_engine_config;
 
 /* Plan text.  Every entry that takes plan_json reads two dialects: the
@@ -613,6 +640,7 @@ typedef struct sdb_batch_stats {
     double last_pre_ms;       /* zeroing and the plans' unbatched work before the aggregating chains */
     double last_post_ms;      /* after it: final flags, compaction, gathers, result copies */
     double last_build_ms;     /* the chain batch's hash-table builds (one launch; 0: none) */
+    int32_t paired_chains;    /* fact chains run two by two in paired passes (sdb_chain_launch_pair) */
 } sdb_batch_stats;
 
 int sdb_engine_batch_prepare(sdb_engine *eng, const char *const *plans_json, int n_plans, int flags,
@@ -676,6 +704,7 @@ typedef struct sdb_server_stats {
     uint64_t direct_plans;             /* requests run at once through the plain path (idle server) */
     uint64_t sizing_us;                /* dispatcher host time in sizing passes (microseconds) */
     uint64_t launch_us;                /* dispatcher host time recording and enqueueing batches */
+    uint64_t paired_chains;            /* fact chains run two by two in paired passes */
 } sdb_server_stats;
 
 int sdb_server_create(sdb_engine *eng, const sdb_server_config *cfg, sdb_server **out);

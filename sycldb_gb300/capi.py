@@ -62,14 +62,16 @@ class ChainDesc(ctypes.Structure):
 
 class EngineConfig(ctypes.Structure):
     _fields_ = [("arena_bytes", c_uint64), ("segment_rows", c_uint64), ("fuse", c_int32), ("profile", c_int32),
-                ("stream", c_void_p), ("plan_cache", c_int32), ("order_by", c_int32), ("join_tables", c_int32)]
+                ("stream", c_void_p), ("plan_cache", c_int32), ("order_by", c_int32), ("join_tables", c_int32),
+                ("no_shared_scans", c_int32)]
 
 
 class BatchStats(ctypes.Structure):
     _fields_ = [("n_plans", c_int32), ("kernels_per_run", c_int32), ("graph", c_int32), ("chain_launches", c_int32),
                 ("batched_chains", c_int32), ("batched_builds", c_int32), ("arena_bytes", c_uint64), ("zero_bytes", c_uint64),
                 ("host_bytes", c_uint64), ("last_run_ms", c_double), ("last_chain_ms", c_double),
-                ("last_pre_ms", c_double), ("last_post_ms", c_double), ("last_build_ms", c_double)]
+                ("last_pre_ms", c_double), ("last_post_ms", c_double), ("last_build_ms", c_double),
+                ("paired_chains", c_int32)]
 
 
 class ServerConfig(ctypes.Structure):
@@ -81,7 +83,7 @@ class ServerStats(ctypes.Structure):
     _fields_ = [(f, c_uint64) for f in ("submitted", "completed", "failed", "batches", "batched_plans",
                                         "max_batch_plans", "max_inflight_plans", "peak_device_bytes",
                                         "peak_pinned_bytes", "budget_bytes", "direct_plans", "sizing_us",
-                                        "launch_us")]
+                                        "launch_us", "paired_chains")]
 
 
 SDB_BATCH_EAGER = 1
@@ -138,6 +140,9 @@ _SIGS = {
     "sdb_chain_tune_get_op": (c_int, [c_int, c_int, c_int, c_uint64]),
     "sdb_chain_registers": (c_int, [POINTER(ChainDesc)]),
     "sdb_chain_specialised": (c_int, [POINTER(ChainDesc)]),
+    "sdb_chain_pairable": (c_int, [POINTER(ChainDesc), POINTER(ChainDesc)]),
+    "sdb_chain_pair_key": (c_int, [POINTER(ChainDesc), POINTER(c_uint64)]),
+    "sdb_chain_launch_pair": (c_int, [POINTER(ChainDesc), POINTER(ChainDesc), c_void_p]),
     "sdb_fused_launch_counts": (c_int, [POINTER(c_uint64), POINTER(c_uint64)]),
     "sdb_chain_batch_scratch_bytes": (c_size_t, [POINTER(ChainDesc), c_int]),
     "sdb_chain_batch_create": (c_int, [POINTER(ChainDesc), c_int, _P, c_size_t, _P, POINTER(c_void_p)]),
@@ -237,12 +242,21 @@ def fused_launch_counts() -> tuple:
 
 
 def force_chain_variant(variant: int):
-    """Sets every tuning-table entry to `variant` (-1 restores the defaults)."""
+    """Sets every tuning-table entry to `variant`.  -1 restores the process's
+    table: the built-in defaults, then the committed autotuner table again if
+    an engine of this process loaded it."""
     L = lib()
     for term in range(3):
         for nregs in (1, 4, 8):
             for b in range(40):
                 check(L.sdb_chain_tune_set(term, nregs, 1 << b, variant))
+    if variant == -1:
+        from . import engine
+
+        if engine._TUNING_LOADED:
+            from . import autotune
+
+            autotune.load_default()
 
 
 def plan_to_idl(plan) -> dict:

@@ -63,6 +63,9 @@ sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string>
 // Plan p's result (caller frees it with sdb_result_free).
 sdb_result *batch_take_result(const sdb_batch *b, size_t p);
 
+// Fact chains the batch runs in paired passes (shared scans).
+int batch_paired_chains(const sdb_batch *b);
+
 void batch_destroy(sdb_batch *b);
 
 // Runs one plan with the engine's plain path (sdb_engine_execute).

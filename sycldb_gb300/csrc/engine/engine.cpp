@@ -770,6 +770,8 @@ struct Fuser {
 struct DevOp {
     const char *name;
     std::function<int(cudaStream_t)> fn;
+    bool has_chain = false;  // an aggregating fused chain (`chain`), which a shared scan may pair
+    sdb_chain_desc chain{};
 };
 
 // A batch runs every plan's `pre` work, then every batched hash-table build
@@ -783,6 +785,8 @@ struct PlanRecord {
 
 struct Recorder {
     std::vector<PlanRecord> plans;
+    std::vector<DevOp> shared_pre;       // paired fact scans of leading pre chains, before the pre work
+    std::vector<DevOp> shared;           // paired fact scans of leading mid chains, after the builds
     std::vector<sdb_chain_desc> chains;  // chains for sdb_chain_batch
     bool batch_chains = true;            // aggregating chains into the chain batch
     bool batch_builds = true;            // hash-table builds into its build launch
@@ -839,11 +843,16 @@ struct Engine {
 
     // Every device operation of a plan goes through here: run now on the
     // engine's stream, or recorded for a batch.
-    void dev(const char *name, std::function<int(cudaStream_t)> fn)
+    void dev(const char *name, std::function<int(cudaStream_t)> fn, const sdb_chain_desc *chain = nullptr)
     {
         if (rec) {
             PlanRecord &pr = rec->plans.back();
-            (pr.after ? pr.post : (pr.builds ? pr.mid : pr.pre)).push_back({name, std::move(fn)});
+            DevOp op{name, std::move(fn)};
+            if (chain) {
+                op.has_chain = true;
+                op.chain = *chain;
+            }
+            (pr.after ? pr.post : (pr.builds ? pr.mid : pr.pre)).push_back(std::move(op));
             return;
         }
         cudaEvent_t a = nullptr;
@@ -924,7 +933,8 @@ struct Engine {
             pr->after = true;
         } else {
             dev(build ? "build_chain" : "fused_chain",
-                [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); });
+                [c](cudaStream_t s) { return sdb_fused_chain(&c, (sdb_stream_t)s); },
+                build || c.terminal == SDB_TERM_FLAGS ? nullptr : &c);
         }
         if (c.flags_out) written(c.flags_out);
     }
@@ -1686,7 +1696,7 @@ struct sdb_batch {
     sdb::MemoryManager rmm;  // result region: counts and result columns of every plan
     char *rbase = nullptr;   // its base; B.host mirrors it byte for byte
     size_t rbytes = 0;
-    cudaStream_t bs = nullptr;              // the stream a run goes on
+    cudaStream_t bs = nullptr;              // the stream the graph is captured on
     std::vector<cudaStream_t> side;
     std::vector<cudaEvent_t> join;
     cudaEvent_t fork = nullptr, ev_a = nullptr, ev_b = nullptr;
@@ -1698,6 +1708,7 @@ struct sdb_batch {
     cudaGraphExec_t exec = nullptr;
     int kernels = 0;
     int chain_groups = 0;
+    int paired = 0;  // fact chains run in paired passes (two per pass)
     double last_ms = 0;
     // false: streams, events, staging and arena belong to the caller (a
     // server slot), the batch runs once
@@ -2337,6 +2348,77 @@ void record_plans(Engine &E, sdb_batch &B, MemoryManager &mm, MemoryManager &rmm
     }
 }
 
+// Shared scans: plans of the batch whose fact chains scan the same rows in
+// the same bound pass run those chains two by two, one paired pass each
+// (sdb_chain_launch_pair: each tile copied once, both chains evaluated on it),
+// on the main stream.  Only a plan's leading chains of a phase move -- none
+// of the plan's work in that phase runs before them -- into a paired stage
+// right before the phase: the pre phase (plans without batched builds) or
+// the mid phase (after the builds).  Never two chains of one plan.  Results
+// are those of the chains run apart.
+void pair_phase(sdb_batch &B, std::vector<DevOp> PlanRecord::*list, std::vector<DevOp> &out)
+{
+    struct Cand {
+        uint64_t key;
+        size_t plan, idx;
+        bool used;
+    };
+    std::vector<Cand> cands;
+    for (size_t p = 0; p < B.rec.plans.size(); p++) {
+        const std::vector<DevOp> &ops = B.rec.plans[p].*list;
+        for (size_t i = 0; i < ops.size() && ops[i].has_chain; i++) {
+            uint64_t key = 0;
+            if (sdb_chain_pair_key(&ops[i].chain, &key) == 1) cands.push_back({key, p, i, false});
+        }
+    }
+    // equal keys side by side, in plan order within a key
+    std::stable_sort(cands.begin(), cands.end(), [](const Cand &a, const Cand &b) { return a.key < b.key; });
+    int paired = 0;
+    for (size_t a = 0; a < cands.size(); a++) {
+        if (cands[a].used) continue;
+        const sdb_chain_desc &x = (B.rec.plans[cands[a].plan].*list)[cands[a].idx].chain;
+        for (size_t b = a + 1; b < cands.size() && cands[b].key == cands[a].key; b++) {
+            if (cands[b].used || cands[b].plan == cands[a].plan) continue;
+            const sdb_chain_desc &y = (B.rec.plans[cands[b].plan].*list)[cands[b].idx].chain;
+            if (sdb_chain_pairable(&x, &y) != 1) continue;
+            cands[a].used = cands[b].used = true;
+            const sdb_chain_desc cx = x, cy = y;
+            out.push_back({"paired_chains", [cx, cy](cudaStream_t s) {
+                               return sdb_chain_launch_pair(&cx, &cy, (sdb_stream_t)s);
+                           }});
+            paired += 2;
+            break;
+        }
+    }
+    if (!paired) return;
+    B.paired += paired;
+    std::vector<std::vector<char>> moved(B.rec.plans.size());
+    for (const Cand &c : cands)
+        if (c.used) {
+            auto &m = moved[c.plan];
+            if (m.size() <= c.idx) m.resize(c.idx + 1, 0);
+            m[c.idx] = 1;
+        }
+    for (size_t p = 0; p < B.rec.plans.size(); p++) {
+        if (moved[p].empty()) continue;
+        std::vector<DevOp> keep;
+        std::vector<DevOp> &ops = B.rec.plans[p].*list;
+        for (size_t i = 0; i < ops.size(); i++)
+            if (i >= moved[p].size() || !moved[p][i]) keep.push_back(std::move(ops[i]));
+        ops = std::move(keep);
+    }
+}
+
+void pair_chains(Engine &E, sdb_batch &B)
+{
+    B.rec.shared_pre.clear();
+    B.rec.shared.clear();
+    B.paired = 0;
+    if (E.cfg.no_shared_scans) return;
+    pair_phase(B, &PlanRecord::pre, B.rec.shared_pre);
+    pair_phase(B, &PlanRecord::mid, B.rec.shared);
+}
+
 void replay(sdb_batch &B, cudaStream_t main)
 {
     if (B.mm.zused()) SDB_CUDA(cudaMemsetAsync(B.mm.zero_base(), 0, B.mm.zused(), main));
@@ -2365,10 +2447,12 @@ void replay(sdb_batch &B, cudaStream_t main)
     auto mark = [&](cudaEvent_t e) {
         if (B.cb && e && B.timed) SDB_CUDA(cudaEventRecordWithFlags(e, main, rf));
     };
+    for (const DevOp &op : B.rec.shared_pre) check(op.fn(main));  // paired fact scans
     phase(&PlanRecord::pre);
     mark(B.ev_c0);
     if (B.cb) check(sdb_chain_batch_launch_part(B.cb, 0, (sdb_stream_t)main));  // builds
     mark(B.ev_cb);
+    for (const DevOp &op : B.rec.shared) check(op.fn(main));  // paired fact scans
     phase(&PlanRecord::mid);
     mark(B.ev_cm);
     if (B.cb) check(sdb_chain_batch_launch_part(B.cb, 1, (sdb_stream_t)main));  // aggregating chains
@@ -2446,6 +2530,7 @@ void batch_prepare(Engine &E, sdb_batch &B, const std::vector<std::string> &plan
     B.mm.init_sized(used + cb_bytes + 256, zused, E.stream);
     B.rmm.init_sized(rused, 256, E.stream);
     record_plans(E, B, B.mm, B.rmm, plans);
+    pair_chains(E, B);
     if (!B.rec.chains.empty()) {
         void *scratch = B.mm.alloc<uint8_t>(cb_bytes);
         check(sdb_chain_batch_create(B.rec.chains.data(), (int)B.rec.chains.size(), scratch, cb_bytes,
@@ -2627,6 +2712,7 @@ sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string>
     record_plans(E, B, B.mm, B.rmm, plans);
     if (B.mm.used() != z.arena || B.mm.zused() != z.zero || B.rmm.used() != z.staging)
         throw Error(SDB_ERR_INVALID, "batch sizing mismatch");
+    pair_chains(E, B);
     if (cb_bytes + z.staging > pinned_bytes) throw Error(SDB_ERR_INVALID, "batch staging too small");
     B.host = pinned + cb_bytes;
     B.host_bytes = z.staging;
@@ -2644,6 +2730,8 @@ sdb_batch *batch_launch_external(sdb_engine *eng, const std::vector<std::string>
 }
 
 sdb_result *batch_take_result(const sdb_batch *B, size_t p) { return unpack_result(*B, p); }
+
+int batch_paired_chains(const sdb_batch *B) { return B->paired; }
 
 sdb_result *execute_plain(sdb_engine *eng, const std::string &plan) { return execute_plan(eng->E, plan).release(); }
 
@@ -2954,6 +3042,7 @@ int sdb_batch_info(const sdb_batch *b, sdb_batch_stats *info)
     info->last_pre_ms = b->last_pre_ms;
     info->last_post_ms = b->last_post_ms;
     info->last_build_ms = b->last_build_ms;
+    info->paired_chains = b->paired;
     return SDB_OK;
 }
 

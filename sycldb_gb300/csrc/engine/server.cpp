@@ -273,6 +273,7 @@ struct sdb_server {
                         std::chrono::duration_cast<std::chrono::microseconds>(Clock::now() - t_launch).count();
                     std::lock_guard<std::mutex> g(mu);
                     st.launch_us += (uint64_t)us;
+                    st.paired_chains += (uint64_t)sdb::batch_paired_chains(s.batch);
                 }
                 cudaError_t e = cudaEventRecord(s.done, s.ss.main);
                 if (e != cudaSuccess) throw sdb::Error(SDB_ERR_CUDA, cudaGetErrorString(e));

@@ -23,6 +23,7 @@
 #include <cstdio>
 #include <atomic>
 #include <mutex>
+#include <type_traits>
 #include <cstring>
 #include <utility>
 #include <vector>
@@ -1832,6 +1833,94 @@ __global__ void __launch_bounds__(kThreads, dense_min_blocks<STAGES, CARRY>()) k
     block_flush<TERM>(L, s_key, s_sum, s_part, acc);
 }
 
+// Paired pass: two chains of one bound shape whose staged slots are the same
+// columns over the same rows (two plans of a batch that scan the same fact
+// rows with their own literals and tables).  Each tile is copied into the
+// ring once and both chains run on it, each with its own group table,
+// bitmap, carried rows and second-level rows; late columns are each chain's
+// own.  The host checks that the staged slots, row count and incoming flags
+// (none) agree.
+constexpr int kPair = 2;
+struct LaunchPair {
+    Launch L[kPair];
+    uint32_t bits_off[kPair];  // each chain's bitmap: its first word after the ring
+};
+
+template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
+__global__ void __launch_bounds__(kThreads, 4) k_dense_pair(const __grid_constant__ LaunchPair P)
+{
+    static_assert(B::bound && CARRY == 3, "the paired pass runs the bound carry-3 shapes");
+    constexpr int kStages = STAGES;
+    constexpr bool kCompact = SPLIT <= (int)sizeof...(KS);
+    constexpr int kItems = items_of<CARRY>(), kQ = kItems / 4;
+    constexpr int SS = stage_slots<CARRY>();
+    extern __shared__ int4 s_buf[];  // [kStages][SS][kThreads][kQ], then the chains' bitmaps
+    __shared__ uint32_t s_key[kPair][TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ unsigned long long s_sum[kPair][TERM == T_GROUP ? kDenseCap : 1];
+    __shared__ uint8_t s_list[kCompact ? kThreads * kItems : 1];  // reused by the chains in turn
+    __shared__ uint64_t s_part[kThreads / 32];
+    __shared__ uint8_t s_l2src[kPair][kThreads];
+    const Launch &L0 = P.L[0];  // the staged slots, row count and tiles are L0's (and L1's)
+    uint32_t carry[kPair];
+    int4 ce[kPair];
+    Level2<NREGS> Q[kPair];
+    bool direct[kPair];
+    uint64_t acc[kPair];
+    uint32_t *s_bits[kPair];
+    uint32_t *ring_end = reinterpret_cast<uint32_t *>(s_buf + kStages * SS * kThreads * kQ);
+#pragma unroll
+    for (int c = 0; c < kPair; c++) {
+        carry[c] = 0;
+        ce[c] = make_int4(0, 0, 0, 0);
+        Q[c].src = s_l2src[c] + (threadIdx.x & ~31u);
+        direct[c] = P.L[c].P <= kDenseCap;
+        acc[c] = 0;
+        s_bits[c] = ring_end + P.bits_off[c];
+    }
+    constexpr uint64_t kTile = (uint64_t)kThreads * kItems;
+    const uint64_t stride = (uint64_t)gridDim.x * kTile;
+    uint64_t tile = (uint64_t)blockIdx.x * kTile;
+#pragma unroll
+    for (int p = 0; p < kStages - 1; p++)
+        issue_tile<kStages, SS, kItems>(L0.slot, L0.nstaged, L0.n, s_buf, p, tile + p * stride);
+#pragma unroll
+    for (int c = 0; c < kPair; c++) {
+        group_table_reset<TERM>(s_key[c], s_sum[c]);
+        stage_bitmap(P.L[c], s_bits[c]);
+    }
+    __syncthreads();
+
+    State<NREGS, kItems> S;
+#pragma unroll
+    for (int r = 0; r < NREGS; r++)
+#pragma unroll
+        for (int k = 0; k < kItems; k++) S.reg[r][k] = 0;
+
+    int st = 0;
+    for (; tile < L0.n; tile += stride) {
+        issue_tile<kStages, SS, kItems>(L0.slot, L0.nstaged, L0.n, s_buf, (st + kStages - 1) % kStages,
+                                        tile + (kStages - 1) * stride);
+        cp_async_wait<kStages - 1>();
+#pragma unroll
+        for (int c = 0; c < kPair; c++) {
+            S.bits = s_bits[c];
+            tile_body<TERM, B, NREGS, SPLIT, CARRY, KS...>(P.L[c], S, s_buf, st, tile, s_list, s_key[c], s_sum[c],
+                                                           s_bits[c], direct[c], acc[c], carry[c], ce[c], Q[c]);
+        }
+        st = (st + 1) % kStages;
+    }
+    cp_async_wait<0>();
+#pragma unroll
+    for (int c = 0; c < kPair; c++)
+        drain_carry<TERM, B, NREGS, SPLIT, CARRY, KS...>(P.L[c], carry[c], ce[c], Q[c], s_bits[c], s_key[c], s_sum[c],
+                                                         direct[c], acc[c]);
+#pragma unroll
+    for (int c = 0; c < kPair; c++) {
+        if (c) __syncthreads();  // the first flush has read s_part
+        block_flush<TERM>(P.L[c], s_key[c], s_sum[c], s_part, acc[c]);
+    }
+}
+
 // A run of consecutive tiles of one chain: the unit the batched pass pulls
 // from its work queue.
 struct Span {
@@ -2455,6 +2544,88 @@ struct BoundProbe {
         return SDB_OK;
     }
 };
+
+// The bound shapes with a paired pass: those of the served mix (star join,
+// date join, filter-project-sum).
+template <class B>
+constexpr bool has_pair_pass()
+{
+    return std::is_same<B, StarBind>::value || std::is_same<B, DateJoinBind>::value ||
+           std::is_same<B, FilterSumBind>::value;
+}
+
+template <class B, int TERM, int NREGS, int STAGES, int SPLIT, int CARRY, int... KS>
+int launch_pair_stages(LaunchPair &P, cudaStream_t s)
+{
+    auto kern = k_dense_pair<B, TERM, NREGS, STAGES, SPLIT, CARRY, KS...>;
+    const int ring = STAGES * stage_slots<CARRY>() * kThreads * (items_of<CARRY>() / 4) * (int)sizeof(int4);
+    uint32_t words = 0;
+    for (int c = 0; c < kPair; c++) {
+        P.bits_off[c] = words;
+        if (P.L[c].bitmap_ht) words += (P.L[c].bitmap_len + 31) / 32;
+    }
+    const int smem = ring + (int)(words * 4);
+    static const bool attr = [&] {  // once per instantiation, thread-safe
+        cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, ring + kPair * (int)(kBitmapMax / 8));
+        return true;
+    }();
+    (void)attr;
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem) != cudaSuccess || per_sm < 1)
+        per_sm = 1;
+    const uint64_t tile = (uint64_t)kThreads * items_of<CARRY>();
+    uint64_t blocks = (P.L[0].n + tile - 1) / tile;
+    const uint64_t cap = (uint64_t)num_sms() * per_sm;
+    if (blocks > cap) blocks = cap;
+    if (blocks == 0) blocks = 1;
+    kern<<<(unsigned)blocks, kThreads, smem, s>>>(P);
+    g_dense_launches.fetch_add(1, std::memory_order_relaxed);
+    g_bound_launches.fetch_add(1, std::memory_order_relaxed);
+    return sdb_check_launch("sdb_chain_launch_pair");
+}
+
+// Whether the shape with_shape picks has a paired pass.
+struct PairProbe {
+    bool ok = false;
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        ok = B::bound && has_pair_pass<B>();
+        return SDB_OK;
+    }
+};
+
+// Launches the paired pass for the shape with_shape picks (bound, with a
+// paired pass), else returns SDB_ERR_UNSUPPORTED without launching.
+struct PairLauncher {
+    LaunchPair &P;
+    cudaStream_t s;
+    template <class B, int TERM, int NREGS, int SPLIT, int... KS>
+    int run()
+    {
+        if constexpr (B::bound && has_pair_pass<B>())
+            return launch_pair_stages<B, TERM, NREGS, 2, SPLIT, 3, KS...>(P, s);
+        else
+            return SDB_ERR_UNSUPPORTED;
+    }
+};
+
+// Whether two launches readied for carry 3 (prepare_late) can share one
+// paired pass: the same bound shape, the same staged columns over the same
+// rows, no incoming or outgoing flags.
+bool pairable(const Launch &A, const Launch &B, int term_a, int term_b)
+{
+    if (term_a != term_b || (term_a != T_SUM && term_a != T_GROUP)) return false;
+    if (A.n != B.n || A.n == 0 || A.flags_in || B.flags_in || A.flags_out || B.flags_out) return false;
+    if (A.nstaged != B.nstaged || A.nslot != B.nslot || A.late_slots != B.late_slots) return false;
+    for (int i = 0; i < A.nstaged; i++)
+        if (A.slot[i] != B.slot[i]) return false;
+    ShapeProbe pa, pb;
+    if (with_shape(A, term_a, 1, pa, true) != SDB_OK || with_shape(B, term_b, 1, pb, true) != SDB_OK || pa.id != pb.id)
+        return false;
+    PairProbe pp;
+    return with_shape(A, term_a, 1, pp, true) == SDB_OK && pp.ok;
+}
 
 }  // namespace dense
 
@@ -3114,6 +3285,71 @@ int sdb_chain_specialised(const sdb_chain_desc *chain)
         if (dense::with_shape(D, term, 1, bp, true) == SDB_OK && bp.bound) return 2;
     }
     return 1;
+}
+
+// The paired pass.  A chain takes part as the single-chain pass would run it
+// under its tuned variant: only a carry-3 launch (variant 8) of a bound
+// shape pairs, so each chain's results are those of its own launch.
+static bool pair_launch_of(const sdb_chain_desc *c, dense::Launch &D, int &term)
+{
+    ChainLaunch L;
+    int nregs = 1;
+    term = 0;
+    if (sdb_chain_prepare(c, &L, sizeof L, &nregs, &term) != SDB_OK) return false;
+    if (L.d.n == 0 || term == T_BUILD || term == T_FLAGS) return false;
+    int variant = tune_entry(term, nregs, op_class(L.d), L.d.n);
+    if (variant < 0) variant = kCompact2Variant;
+    if (variant < kDenseVariant || variant_carry(variant) != 3) return false;
+    if (!dense::convert(L, nregs, D)) return false;
+    return dense::can_carry(D, term) && dense::prepare_late(D, term);
+}
+
+int sdb_chain_pair_key(const sdb_chain_desc *c, uint64_t *key)
+{
+    if (!c || !key) return 0;
+    dense::Launch D;
+    int term = 0;
+    if (!pair_launch_of(c, D, term)) return 0;
+    dense::PairProbe pp;
+    if (dense::with_shape(D, term, 1, pp, true) != SDB_OK || !pp.ok) return 0;
+    dense::ShapeProbe sp;
+    dense::with_shape(D, term, 1, sp, true);
+    // FNV-1a over what pairable compares
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+        for (int i = 0; i < 8; i++) {
+            h ^= (v >> (8 * i)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    };
+    mix((uint64_t)sp.id);
+    mix((uint64_t)term);
+    mix(D.n);
+    mix(((uint64_t)D.nstaged << 32) | ((uint64_t)D.nslot << 16) | D.late_slots);
+    for (int i = 0; i < D.nstaged; i++) mix((uint64_t)(uintptr_t)D.slot[i]);
+    *key = h;
+    return 1;
+}
+
+int sdb_chain_pairable(const sdb_chain_desc *a, const sdb_chain_desc *b)
+{
+    if (!a || !b) return 0;
+    dense::Launch A, B;
+    int ta = 0, tb = 0;
+    if (!pair_launch_of(a, A, ta) || !pair_launch_of(b, B, tb)) return 0;
+    return dense::pairable(A, B, ta, tb) ? 1 : 0;
+}
+
+int sdb_chain_launch_pair(const sdb_chain_desc *a, const sdb_chain_desc *b, sdb_stream_t stream)
+{
+    if (!a || !b) return sdb_set_error(SDB_ERR_INVALID, "sdb_chain_launch_pair: NULL chain");
+    dense::LaunchPair P;
+    std::memset(&P, 0, sizeof P);
+    int ta = 0, tb = 0;
+    if (!pair_launch_of(a, P.L[0], ta) || !pair_launch_of(b, P.L[1], tb) || !dense::pairable(P.L[0], P.L[1], ta, tb))
+        return sdb_set_error(SDB_ERR_UNSUPPORTED, "sdb_chain_launch_pair: the chains do not share a paired pass");
+    dense::PairLauncher f{P, (cudaStream_t)stream};
+    return dense::with_shape(P.L[0], ta, 1, f, true);
 }
 
 }  // extern "C"

@@ -93,11 +93,12 @@ def _take_result(r) -> Result:
 
 class Engine:
     def __init__(self, arena_bytes: int = 0, segment_rows: int = 0, fuse: bool = True, profile: bool = False,
-                 stream: Optional[int] = None, plan_cache: int = 0, order_by: bool = False, join_tables: int = 0):
+                 stream: Optional[int] = None, plan_cache: int = 0, order_by: bool = False, join_tables: int = 0,
+                 shared_scans: bool = True):
         L = capi.lib()
         _load_tuning_once()
         cfg = capi.EngineConfig(arena_bytes, segment_rows, 1 if fuse else 0, 1 if profile else 0, stream or None,
-                                plan_cache, 1 if order_by else 0, join_tables)
+                                plan_cache, 1 if order_by else 0, join_tables, 0 if shared_scans else 1)
         h = ctypes.c_void_p()
         capi.check(L.sdb_engine_create(ctypes.byref(cfg), ctypes.byref(h)))
         self._h = h

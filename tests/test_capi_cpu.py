@@ -375,6 +375,64 @@ def test_hot_shapes_take_their_bound_pass():
     assert L.sdb_chain_specialised(ctypes.byref(d)) == 1
 
 
+def test_shared_scans_pair_only_chains_of_one_pass_over_the_same_staged_columns():
+    """sdb_chain_pairable: two chains share a paired pass when the
+    single-chain pass would run both as the same bound variant-8
+    instantiation over the same staged columns and rows; their tables,
+    literals, late columns and outputs may differ."""
+    L = capi.lib()
+    keys = [(capi.TERM_GROUPBY, 2, capi.OP_SEMI_PROBE), (capi.TERM_GROUPBY, 2, capi.OP_SEARCH_RANGE),
+            (capi.TERM_SUM, 2, capi.OP_SEARCH_RANGE), (capi.TERM_GROUPBY, 4, capi.OP_FULL_PROBE)]
+    rows = 1 << 20
+    saved = [L.sdb_chain_tune_get_op(t, r, k, rows) for t, r, k in keys]
+
+    def pairable(a, b):
+        return L.sdb_chain_pairable(ctypes.byref(a), ctypes.byref(b))
+
+    def other_star():
+        d = _star_desc()
+        d.ops[0].ht, d.ops[0].lo, d.ops[0].hi = 0x210000, 1, 30000  # another supplier table and range
+        d.ops[1].ht, d.ops[2].ht = 0x310000, 0x410000
+        d.out_keys[0], d.out_keys[1], d.out_sum, d.occ = 0x800000, 0x810000, 0x820000, 0x830000
+        return d
+
+    try:
+        for t, r, k in keys:
+            assert L.sdb_chain_tune_set_op(t, r, k, rows, 8) == capi.SDB_OK
+        assert pairable(_star_desc(), other_star()) == 1
+
+        def key(d):
+            k = ctypes.c_uint64()
+            return k.value if L.sdb_chain_pair_key(ctypes.byref(d), ctypes.byref(k)) == 1 else None
+
+        assert key(_star_desc()) is not None and key(_star_desc()) == key(other_star())
+        assert len({key(_star_desc()), key(_date_join_desc()), key(_filter_sum_desc())}) == 3
+        assert key(_flight3_desc()) is None
+        assert pairable(_date_join_desc(), _date_join_desc()) == 1
+        assert pairable(_filter_sum_desc(), _filter_sum_desc()) == 1
+        d = other_star()
+        _col(d.value, 0x41000000)  # revenue of another table: a late column, each chain's own
+        _col(d.ops[2].a, 0x31000000)  # orderdate too
+        assert pairable(_star_desc(), d) == 1
+        d = other_star()
+        _col(d.ops[1].a, 0x21000000)  # partkey is staged: not the same columns
+        assert pairable(_star_desc(), d) == 0
+        d = other_star()
+        d.n = (1 << 20) - 1  # other rows
+        assert pairable(_star_desc(), d) == 0
+        d = other_star()
+        d.flags_in = 0x900000  # incoming flags
+        assert pairable(_star_desc(), d) == 0
+        assert pairable(_star_desc(), _date_join_desc()) == 0  # two shapes
+        assert pairable(_star_desc(), _star_desc(keys=(0, 1))) == 0  # the run-time-bound pass
+        assert pairable(_flight3_desc(), _flight3_desc()) == 0  # a bound shape without a paired pass
+        L.sdb_chain_tune_set_op(capi.TERM_GROUPBY, 2, capi.OP_SEMI_PROBE, rows, 7)
+        assert pairable(_star_desc(), other_star()) == 0  # only variant 8 pairs
+    finally:
+        for (t, r, k), v in zip(keys, saved):
+            L.sdb_chain_tune_set_op(t, r, k, rows, v)
+
+
 def test_plan_order_matches_the_oracle_for_every_shape():
     """The engine's DAG order (operations/preprocessing.cpp:14-102, lineorder
     scans deferred) equals the oracle restatement's for every plan builder."""

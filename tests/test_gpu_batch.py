@@ -196,3 +196,38 @@ def test_batch_with_split_and_three_key_chains(chain_batch):
                 assert [r.canonical() for r in b.run()] == alone
     assert alone[0] == datasets.oracle_run(ds, pls[0])
     assert all(len(a) > 0 for a in alone)
+
+
+@pytest.mark.parametrize("segment_rows", [0, 1 << 20])
+def test_shared_scans_pair_plans_over_the_same_rows(tables, segment_rows):
+    """Star, date-join and filter-project-sum plans over one fact table, each
+    with its own literals: a batch runs two chains of one shape over the
+    same rows as one paired pass (each tile staged once), and every plan's
+    rows equal its rows alone, the batch's without shared scans and the
+    oracle's.  With several segments per plan, chains pair segment by
+    segment."""
+    pls = [plans.plan_star(1, 3, fact_tag=8), plans.plan_star(2, 11, fact_tag=8), plans.plan_star(3, 20, fact_tag=8),
+           plans.plan_date_join(1995, fact_tag=8), plans.plan_date_join(1997, fact_tag=8),
+           plans.plan_filter_sum(1994, 1, 3, 25, fact_tag=8), plans.plan_filter_sum(1993, 4, 6, 35, fact_tag=8)]
+    try:
+        capi.force_chain_variant(8)  # the variant that pairs, at every size
+        with make_engine(tables, segment_rows=segment_rows) as eng, \
+                make_engine(tables, segment_rows=segment_rows, shared_scans=False) as apart:
+            alone = [eng.execute(pl).canonical() for pl in pls]
+            assert alone[0] == datasets.oracle_run(tables, pls[0])
+            assert alone[3] == datasets.oracle_run(tables, pls[3])
+            assert alone[5] == datasets.oracle_run(tables, pls[5])
+            paired = {}
+            for name, e in (("shared", eng), ("apart", apart)):
+                for eager in (False, True):
+                    with e.batch(pls, eager=eager, chain_batch="builds") as b:
+                        for _ in range(2):  # replays re-zero the group tables
+                            assert [r.canonical() for r in b.run()] == alone
+                        paired[name, eager] = b.stats()["paired_chains"]
+    finally:
+        capi.force_chain_variant(-1)
+    # a pair of stars (the third alone), of date joins and of filter-sums
+    # (per segment, where a plan's segment chains lead its work)
+    for eager in (False, True):
+        assert paired["apart", eager] == 0
+        assert paired["shared", eager] == 6 if segment_rows == 0 else paired["shared", eager] in (6, 12)
