@@ -106,7 +106,7 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-configs", action="store_true",
                     help="skip the SF1 configurations (filter-project-sum, date join + group-by)")
-    ap.add_argument("--only", default="", choices=["", "configs"],
+    ap.add_argument("--only", default="", choices=["", "configs", "pairs"],
                     help="run one section alone (for profiling): configs")
     ap.add_argument("--config-names", default="",
                     help="comma-separated subset of the SF1 configurations to run (default: all)")
@@ -129,6 +129,7 @@ def parse_args():
     ap.add_argument("--served-rates", default="50,200,500,1000,2000",
                     help="Poisson arrival rates (queries/s) of the served form; empty skips it")
     ap.add_argument("--served-seconds", type=float, default=1.5, help="arrival span per rate (at least 100 requests)")
+    ap.add_argument("--served-slots", type=int, default=4, help="served form: batches in flight at once")
     ap.add_argument("--no-shared-scans", action="store_true",
                     help="served form: every fact chain on its own (no paired passes)")
     return ap.parse_args()
@@ -420,6 +421,11 @@ def run_ours(args, rank, world, local, pg):
         if rank == 0:
             print(json.dumps({"configs": out}), flush=True)
         return 0
+    if args.only == "pairs":
+        out = run_pairs(args, args.sf)
+        if rank == 0:
+            print(json.dumps({"shared_scans": out}), flush=True)
+        return 0
 
     L = capi.lib()
     sf = args.sf
@@ -533,6 +539,7 @@ def run_ours(args, rank, world, local, pg):
     batched = run_batched(args, rank, world, local, pg, stream, peak) if args.batched_runs > 0 else None
     served = run_served(args, rank, world, local, pg, stream) if args.served_rates.strip() else None
     widened = run_widened(args, rank, stream, peak) if not args.no_widened else None
+    shared = run_pairs(args, sf) if not args.no_widened else None
 
     if args.plan == "star":
         config = workload_config(sf, n_groups)
@@ -556,6 +563,7 @@ def run_ours(args, rank, world, local, pg):
         "batched": batched,
         "served": served,
         "widened": widened,
+        "shared_scans": shared,
         "gpu_launches": launches,
         "gpu_launches_note": "kernels of the prepared plan's graph (%d: the dimension builds in one launch, the "
                              "fused chain, the result compaction) x steps; the plain path launches %d per "
@@ -740,6 +748,59 @@ def _pct(xs, q):
         return None
     k = min(len(xs) - 1, max(0, int(round(q / 100.0 * (len(xs) - 1)))))
     return xs[k]
+
+
+def run_pairs(args, sf, reps=15):
+    """Shared scans: for each served shape (star join, date join,
+    filter-project-sum), a batch of two plans with their own literals over
+    one fact table (builds batched, fact chains on their own), run with the
+    paired pass and with each chain on its own: device ms per run (median),
+    results compared plan by plan."""
+    import numpy as np
+    import torch
+
+    from sycldb_gb300 import plans, ssb
+    from sycldb_gb300.engine import Engine
+
+    n = ssb.fact_rows(sf)
+    fact = ssb.gen_lineorder_device(n, (3, 4, 5, 8, 9, 11, 12), sf, salt=0)
+    dims = dims_host(sf)
+    torch.cuda.synchronize()
+    kinds = {
+        "star_join": [plans.plan_star(1, 3), plans.plan_star(2, 11)],
+        "date_join": [plans.plan_date_join(1995), plans.plan_date_join(1997)],
+        "filter_project_sum": [plans.plan_filter_sum(1994, 1, 3, 25), plans.plan_filter_sum(1993, 4, 6, 35)],
+    }
+    out = {}
+    for shared in (True, False):
+        with Engine(shared_scans=shared) as eng:
+            eng.load_table("lineorder", fact)
+            for t, c in dims.items():
+                eng.load_table(t, c)
+            for k, pls in kinds.items():
+                pls = [json.dumps(p) for p in pls]
+                alone = [eng.execute(p).canonical() for p in pls]
+                with eng.batch(pls, chain_batch="builds") as b:
+                    for _ in range(3):
+                        b.run()
+                    ms = []
+                    for _ in range(reps):
+                        got = [r.canonical() for r in b.run()]
+                        assert got == alone, k
+                        ms.append(b.stats()["last_run_ms"])
+                    st = b.stats()
+                e = out.setdefault(k, {})
+                e["paired_ms" if shared else "apart_ms"] = float(np.median(ms))
+                if shared:
+                    e["paired_chains"] = st["paired_chains"]
+    for e in out.values():
+        e["speedup"] = e["apart_ms"] / e["paired_ms"]
+    del fact
+    torch.cuda.empty_cache()
+    return {"workload": "SF%g lineorder (%d rows); per shape a batch of two plans with their own literals, "
+                        "dimension builds in one launch, each fact chain on its own (apart) or both in one "
+                        "paired pass; device ms per run, median of %d" % (sf, n, reps),
+            "results": "each plan's rows equal its rows alone", "shapes": out}
 
 
 def run_widened(args, rank, stream, peak):
@@ -1016,7 +1077,7 @@ def run_served(args, rank, world, local, pg, stream):
         wpl = [p for ps in wk.values() for p in ps[:2]] + [r.plan for r in warm]
         replay_plain(eng, wpl, [0.0] * len(wpl), keep_results=False)
         pst, plat, pres, pwall = replay_plain(eng, pls, at)
-        with Server(eng, budget_bytes=60 << 30) as srv:
+        with Server(eng, budget_bytes=60 << 30, slots=args.served_slots) as srv:
             for p in wpl[:8]:
                 srv.replay([p], [0.0], keep_results=False)
             srv.replay(wpl, [0.0] * len(wpl), keep_results=False)
@@ -1046,7 +1107,7 @@ def run_served(args, rank, world, local, pg, stream):
                         "plan mix 1/4 each: filter-project-sum (one-year window, discount range, quantity bound), "
                         "filter + date join + group by year, star join, star join with year and brand windows" % n,
             "latency": "host wall clock from each request's scheduled arrival to its result on the host",
-            "budget_bytes": 60 << 30, "slots": 4, "rates": out, "clocks": clk,
+            "budget_bytes": 60 << 30, "slots": args.served_slots, "rates": out, "clocks": clk,
             "shared_scans": "off" if args.no_shared_scans else
             "on: two fact chains of one shape over the same rows run as one paired pass (paired_chains)"}
 
