@@ -125,6 +125,8 @@ def test_large_chains_run_on_their_own_in_the_mix():
         with eng.batch(pls[:12]) as b:
             assert [r.canonical() for r in b.run()] == alone[:12]
             assert b.stats()["batched_chains"] == 0  # every fact chain is large
+            # twelve plans of four kinds over one table: some share a scan
+            assert b.stats()["paired_chains"] >= 2
 
 
 def _naive_of(kind, plan, fact, dims):
