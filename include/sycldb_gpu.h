@@ -688,8 +688,9 @@ typedef struct sdb_server_config {
     int32_t slots;            /* batches in flight; 0 = 4 */
     int32_t max_batch;        /* plans per batch; 0 = 64 */
     int32_t streams_per_slot; /* 0 = 4 */
-    int32_t no_direct;        /* 0: a request that arrives at an idle server with nothing else waiting
-                                 runs at once through the plain path (no sizing pass, no batch set-up);
+    int32_t no_direct;        /* 0: while no batch is in flight and at most 4 requests wait, the
+                                 oldest runs at once through the plain path (no sizing pass, no batch
+                                 set-up; first come first served); a longer queue goes into batches;
                                  1: every request goes through a batch */
 } sdb_server_config;
 

@@ -313,6 +313,9 @@ struct sdb_server {
         return false;
     }
 
+    // Longest queue an idle server still serves one request at a time.
+    static constexpr size_t kDirectQueue = 4;
+
     void run()
     {
         cudaSetDevice(device);
@@ -341,14 +344,17 @@ struct sdb_server {
                     incoming.pop_front();
                 }
             }
-            // An idle server with one request and nothing else waiting runs it
-            // at once through the plain path: no sizing pass and no batch
-            // set-up, so a lone request waits no longer than on the plain
-            // path.  Requests that arrive meanwhile wait for it, then go into
-            // batches as usual.
+            // An idle server with a short queue (at most kDirectQueue
+            // waiting) runs the oldest request at once through the plain
+            // path: no sizing pass, no batch set-up, first come first served.
+            // While the device keeps up with the arrivals a request then
+            // waits no longer than on the plain path, and none waits for a
+            // batch that fills up behind it; once the queue grows past that
+            // (the device falls behind), the waiting requests go into
+            // batches, whose shared builds and scans raise throughput.
             // (Only when the budget covers the engine's own memory, which a
             // plain execution uses: no plan then goes past the budget.)
-            if (direct && busy == 0 && waiting.size() == 1 && !waiting.front().sized) {
+            if (direct && busy == 0 && !waiting.empty() && waiting.size() <= kDirectQueue) {
                 Request r = std::move(waiting.front());
                 waiting.pop_front();
                 try {
