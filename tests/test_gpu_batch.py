@@ -231,3 +231,25 @@ def test_shared_scans_pair_plans_over_the_same_rows(tables, segment_rows):
     for eager in (False, True):
         assert paired["apart", eager] == 0
         assert paired["shared", eager] == 6 if segment_rows == 0 else paired["shared", eager] in (6, 12)
+
+
+@pytest.mark.parametrize("part", [0, 1, 4, 5, 6])
+def test_shared_scans_at_tile_edges(tables, part):
+    """The paired pass on fact partitions of 1, 1000, 1025, 4097 and 65,536
+    rows (below one tile, around tile edges): two star plans and two
+    filter-project-sum plans share scans, each plan's rows equal its rows
+    alone and, for the first of each shape, the oracle's."""
+    pls = [plans.plan_star(1, 3, fact_tag=part), plans.plan_star(2, 11, fact_tag=part),
+           plans.plan_filter_sum(1994, 1, 3, 25, fact_tag=part), plans.plan_filter_sum(1993, 4, 6, 35, fact_tag=part)]
+    try:
+        capi.force_chain_variant(8)  # the variant that pairs, at every size
+        with make_engine(tables) as eng:
+            alone = [eng.execute(pl).canonical() for pl in pls]
+            assert alone[0] == datasets.oracle_run(tables, pls[0])
+            assert alone[2] == datasets.oracle_run(tables, pls[2])
+            with eng.batch(pls, chain_batch="builds") as b:
+                for _ in range(2):
+                    assert [r.canonical() for r in b.run()] == alone
+                assert b.stats()["paired_chains"] == 4
+    finally:
+        capi.force_chain_variant(-1)
