@@ -426,6 +426,10 @@ def test_shared_scans_pair_only_chains_of_one_pass_over_the_same_staged_columns(
         assert pairable(_star_desc(), _date_join_desc()) == 0  # two shapes
         assert pairable(_star_desc(), _star_desc(keys=(0, 1))) == 0  # the run-time-bound pass
         assert pairable(_flight3_desc(), _flight3_desc()) == 0  # a bound shape without a paired pass
+        # a launch of chains that cannot pair is refused on the host, before any device work
+        st = L.sdb_chain_launch_pair(ctypes.byref(_star_desc()), ctypes.byref(_date_join_desc()), None)
+        assert st == capi.SDB_ERR_UNSUPPORTED and "paired pass" in capi.last_error()
+        assert L.sdb_chain_launch_pair(None, ctypes.byref(_star_desc()), None) == capi.SDB_ERR_INVALID
         L.sdb_chain_tune_set_op(capi.TERM_GROUPBY, 2, capi.OP_SEMI_PROBE, rows, 7)
         assert pairable(_star_desc(), other_star()) == 0  # only variant 8 pairs
     finally:
