@@ -2363,12 +2363,29 @@ void pair_phase(sdb_batch &B, std::vector<DevOp> PlanRecord::*list, std::vector<
         size_t plan, idx;
         bool used;
     };
+    // whether chain c reads a column that one of the plan's earlier leading
+    // chains writes (a moved chain runs before those)
+    auto reads_any = [](const sdb_chain_desc &c, const std::vector<const int32_t *> &cols) {
+        auto hit = [&](const sdb_operand &o) {
+            return o.kind == SDB_SRC_COL && std::find(cols.begin(), cols.end(), o.col) != cols.end();
+        };
+        for (int k = 0; k < c.n_ops; k++)
+            if (hit(c.ops[k].a) || hit(c.ops[k].b)) return true;
+        if (hit(c.value)) return true;
+        for (int k = 0; k < c.n_keys; k++)
+            if (hit(c.keys[k])) return true;
+        return false;
+    };
     std::vector<Cand> cands;
     for (size_t p = 0; p < B.rec.plans.size(); p++) {
         const std::vector<DevOp> &ops = B.rec.plans[p].*list;
+        std::vector<const int32_t *> written;
         for (size_t i = 0; i < ops.size() && ops[i].has_chain; i++) {
+            const sdb_chain_desc &c = ops[i].chain;
             uint64_t key = 0;
-            if (sdb_chain_pair_key(&ops[i].chain, &key) == 1) cands.push_back({key, p, i, false});
+            if (!reads_any(c, written) && sdb_chain_pair_key(&c, &key) == 1) cands.push_back({key, p, i, false});
+            for (int k = 0; k < c.n_ops; k++)
+                if (c.ops[k].out_col) written.push_back(c.ops[k].out_col);
         }
     }
     // equal keys side by side, in plan order within a key
